@@ -1,0 +1,396 @@
+#!/usr/bin/env python3
+"""Benchmark of the fused ZSC step on GB300.
+
+Workload (default): 256^3 periodic box, 64 bubbles with radii uniform in
+[6, 10] placed by seeded rejection sampling (surface gap >= 3), rhoH = 1,
+rhoL = 0.1, sigma = 1e-3, W = 4, tau_rho = 0.7, Gamma = 1, tau_phi = 1,
+gravity -1e-6 along z, FP32 storage.  A "step" is one lattice Boltzmann
+time step over the whole box (one fused kernel launch).  The state
+(26 x 4 B x 16.8M nodes = 1.75 GB) is far larger than the 129 MB L2, so no
+L2 flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the reference's own step (its nine kernels and three
+halo exchanges, compiled for the host CPU from the reference sources) on the
+host cores, on a slab of the same workload sized so the run stays within a
+few minutes.  For N > 1 (torchrun) every rank runs an independent replica of
+the workload on its own GPU (the step has no cross-GPU exchange here).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "MLUPS + HBM GB/s (FP32 vs FP16-storage) at 256^3; adjoint-to-forward time ratio"
+BYTES_PER_NODE = {"fp32": 26 * 2 * 4, "fp16": 26 * 2 * 2, "bf16": 26 * 2 * 2}
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse_args(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--size", type=int, default=256)
+    ap.add_argument("--bubbles", type=int, default=64)
+    ap.add_argument("--storage", default="fp32")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--stat-every", type=int, default=100, help="lbm_stats cadence inside the e2e run")
+    return ap.parse_args(argv)
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def workload(size: int, nbubbles: int):
+    from lbm_bench_gpu_gb300 import inputs
+    r_range = (6.0, 10.0) if size <= 256 else (6.0, 12.0)
+    return inputs.bubbly(size, nbubbles, r_range=r_range, gravity=-1e-6)
+
+
+def params_for(inp, storage="fp32", device=0):
+    from lbm_bench_gpu_gb300 import capi
+    return capi.make_params(inp.nx, inp.ny, inp.nz, rhoL=inp.rhoL, rhoH=inp.rhoH, tauRho=inp.tauRho,
+                            tauPhi=inp.tauPhi, width=inp.width, sigma=inp.sigma, Gamma=inp.Gamma, Eo=inp.Eo,
+                            rc0=inp.rc0, storage=storage, device=device, compat=True)
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            d = json.loads(p.read_text())
+            return float(d["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+def profiled_traffic(storage: str, size: int):
+    """dram bytes read + written per step-kernel launch from the committed ncu summary."""
+    f = ROOT / "profiles" / f"zsc_step_{storage}_{size}cube.txt"
+    if not f.exists():
+        return None
+    for line in f.read_text().splitlines():
+        if line.strip().startswith("dram_bytes_per_launch"):
+            try:
+                return float(line.split("=")[1].split()[0])
+            except Exception:
+                return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_id: str):
+        self.gpu_id = gpu_id
+        self.proc = None
+        self.out = tempfile.NamedTemporaryFile(prefix="clocks_", suffix=".csv", delete=False)
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu_id}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=self.out, stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        self.out.close()
+
+    def summary(self, t_start: float, t_end: float):
+        try:
+            rows = [l.split(",") for l in Path(self.out.name).read_text().splitlines() if l.strip()]
+        except Exception:
+            rows = []
+        finally:
+            try:
+                os.unlink(self.out.name)
+            except Exception:
+                pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm = [float(r[1]) for r in rows if len(r) > 2 and r[1].strip().replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if len(r) > 2 and r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in rows:
+            for i, n in enumerate(names):
+                if len(r) > 5 + i and r[5 + i].strip().lower().startswith("active"):
+                    reasons.add(n)
+        # samples under load: clocks above the idle floor
+        load = [s for s in sm if s > 0.5 * max(sm)] if sm else []
+        return {"sm_mhz": float(np.median(load)) if load else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def gpu_identity(device: int) -> str:
+    import torch
+    props = torch.cuda.get_device_properties(device)
+    uuid = getattr(props, "uuid", None)
+    if uuid is not None:
+        s = str(uuid)
+        return s if s.startswith("GPU-") else "GPU-" + s
+    return str(device)
+
+
+def cpu_baseline(inp, budget_s: float = 15.0):
+    """The FP64 oracle (C/OpenMP) on the host cores, on the same 256^3 workload,
+    timed over as many steps as fit in ~budget_s."""
+    from oracle.oracle import Oracle
+    from lbm_bench_gpu_gb300 import capi
+    p = params_for(inp)
+    o = Oracle.from_params(p)
+    o.init_bubbles(inp.bubbles)
+    grav = float(capi.derive(p).grav)
+    t0 = time.perf_counter()
+    o.step(1, grav)
+    t1 = time.perf_counter() - t0
+    n = int(max(1, min(20, budget_s / max(t1, 1e-3))))
+    t0 = time.perf_counter()
+    o.step(n, grav)
+    dt = time.perf_counter() - t0
+    nodes = inp.nx * inp.ny * inp.nz
+    o.close()
+    return {"value": nodes * n / dt / 1e6, "unit": "MLUPS", "cores": Oracle.threads(), "kind": "port",
+            "sample": f"FP64 oracle, full {inp.nx}x{inp.ny}x{inp.nz} box, {n} steps after 1 untimed step "
+                      f"({dt:.1f} s)"}
+
+
+def run_ours(args, rank, world, local):
+    import torch
+    from lbm_bench_gpu_gb300 import capi
+
+    torch.cuda.set_device(local)
+    inp = workload(args.size, args.bubbles)
+    p = params_for(inp, args.storage, local)
+    grav = float(capi.derive(p).grav)
+    nodes = inp.nx * inp.ny * inp.nz
+    K, W = args.steps, args.warmup
+
+    lat = capi.Lattice.from_bubbles(p, inp.bubbles)
+    stream = torch.cuda.ExternalStream(lat.stream, device=local)
+    lat.step(W, grav)
+    lat.sync()
+
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    sampler = ClockSampler(gpu_identity(local)) if rank == 0 else None
+    if sampler:
+        sampler.__enter__()
+    t_start = time.time()
+    e0.record(stream)
+    lat.step(K, grav)
+    e1.record(stream)
+    e1.synchronize()
+    t_end = time.time()
+    if sampler:
+        sampler.__exit__(None, None, None)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    ms = e0.elapsed_time(e1)
+    if world > 1:
+        t = torch.tensor([ms], device=f"cuda:{local}", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    s, _ = lat.stats()
+    if s["nonfinite"]:
+        raise RuntimeError("state went non-finite during the bench")
+    lat.close()
+
+    ms_step = ms / K
+    value = world * nodes * K / (ms / 1e3) / 1e6
+    bpn = BYTES_PER_NODE[args.storage]
+    achieved = bpn * nodes / (ms_step / 1e3) / 1e9
+    peak, peak_kind = measured_peaks()
+    traffic = profiled_traffic(args.storage, args.size)
+    result = {
+        "metric": METRIC, "value": round(value, 1), "unit": "MLUPS", "n_gpus": world, "steps": K, "warmup": W,
+        "ms_per_step": round(ms_step, 5), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32" if args.storage == "fp32" else f"f32 ({args.storage} storage)", "data": "synthetic",
+        "config": {"workload": f"bubbly_{args.size}: {args.size}^3 periodic, {args.bubbles} bubbles "
+                               f"R~U{list((6.0, 10.0) if args.size <= 256 else (6.0, 12.0))}, gap>=3, "
+                               "rhoH=1 rhoL=0.1 sigma=1e-3 W=4 tau_rho=0.7 Gamma=1 tau_phi=1, "
+                               "gravity -1e-6 along z",
+                   "nx": inp.nx, "ny": inp.ny, "nz": inp.nz, "bubbles": args.bubbles, "storage": args.storage,
+                   "seed": 20261203, "parallelism": f"replicas x{world}",
+                   "l2": "state 1.75 GB >> 129 MB L2: no flush needed"},
+        "hbm_gbs": round(achieved, 1),
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "traffic": traffic,
+                     "algorithmic_bytes_per_launch": bpn * nodes, "peak_source": peak_kind},
+        "gpu_launches": K,
+    }
+    if sampler:
+        result["clocks"] = sampler.summary(t_start, t_end)
+    if rank == 0 and not args.no_e2e:
+        result["e2e"] = run_e2e(args, inp, p, grav, local)
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        result["cpu_baseline"] = cpu_baseline(inp)
+    return result
+
+
+def run_e2e(args, inp, p, grav, local):
+    """Same metric through the C-ABI with host buffers: lbm_init from pinned host
+    fields (upload inside the timed region), K steps with lbm_stats every
+    `stat_every` steps (scalar diagnostics back to the host, as the reference
+    driver does with stats()), and the final phi, rho, u copied back."""
+    import torch
+    from lbm_bench_gpu_gb300 import capi
+    nodes = inp.nx * inp.ny * inp.nz
+    K = args.steps
+    with capi.Lattice.from_bubbles(p, inp.bubbles) as seed_lat:
+        f0 = seed_lat.fields()
+    shape = (inp.nz, inp.ny, inp.nx)
+    host_in = {k: torch.empty(shape, dtype=torch.float32, pin_memory=True).numpy() for k in f0}
+    host_out = {k: torch.empty(shape, dtype=torch.float32, pin_memory=True).numpy() for k in f0}
+    for k in f0:
+        host_in[k][...] = f0[k]
+    torch.cuda.synchronize()
+    n_stats = 0
+    t0 = time.perf_counter()
+    lat = capi.Lattice.from_fields(p, host_in["phi"], host_in["rho"], host_in["ux"], host_in["uy"], host_in["uz"])
+    done = 0
+    while done < K:
+        n = min(args.stat_every, K - done)
+        lat.step(n, grav)
+        done += n
+        lat.stats()
+        n_stats += 1
+    s = capi.StatsOut()
+    import ctypes as C
+    capi.check(capi.load().lbm_stats(lat._h, C.byref(s), *[capi.fptr(host_out[k]) for k in
+                                                             ("phi", "rho", "ux", "uy", "uz")]), "lbm_stats")
+    dt = time.perf_counter() - t0
+    lat.close()
+    h2d = 5 * nodes * 4
+    d2h = n_stats * 16 * 8 + 5 * nodes * 4 + 16 * 8
+    return {"value": round(nodes * K / dt / 1e6, 1), "unit": "MLUPS",
+            "h2d_bytes_per_step": round(h2d / K, 1), "d2h_bytes_per_step": round(d2h / K, 1),
+            "what": f"lbm_init from pinned host phi/rho/u, {K} x lbm_step with lbm_stats every "
+                    f"{args.stat_every} steps, final fields copied back; wall clock {dt:.3f} s"}
+
+
+def run_reference(args, rank, world):
+    """The reference's own kernels on the host CPU (all threads), on a
+    256 x 256 x nz_s slab of the workload so that W + K steps fit in ~2 min."""
+    from lbm_bench_gpu_gb300 import capi, inputs
+    from oracle.oracle import Oracle, RefCPU, ref_lib
+    if rank != 0:
+        return None
+    if ref_lib() is None:
+        return {"impl": "reference", "unavailable": "reference sources not staged (oracle/_ref/src missing)"}
+    inp = workload(args.size, args.bubbles)
+    K, W = args.steps, args.warmup
+    p = params_for(inp)
+    grav = float(capi.derive(p).grav)
+    o = Oracle.from_params(p)
+    phi_full = o.bubble_phi(inp.bubbles).astype(np.float32)   # (nz+2, ny, nx), reference planes
+    o.close()
+
+    def make_ref(nxs, nys, nzs):
+        d = tempfile.mkdtemp(prefix="refbench_")
+        sub = inputs.Inputs(nx=nxs, ny=nys, nz=nzs, rhoL=inp.rhoL, rhoH=inp.rhoH, tauRho=inp.tauRho,
+                            tauPhi=inp.tauPhi, width=inp.width, sigma=inp.sigma, Gamma=inp.Gamma, Eo=inp.Eo,
+                            bubbles=inp.bubbles[:1])
+        inputs.write_inputs(d, sub)
+        z0 = inp.nz // 2 - nzs // 2
+        slab = np.ascontiguousarray(phi_full[z0:z0 + nzs + 2, :nys, :nxs])
+        return RefCPU(d, phi_override=slab)
+
+    # calibrate: seconds per node-step on a 16-plane slab of the full x-y plane
+    ref = make_ref(inp.nx, inp.ny, 16)
+    ref.step(1, grav)
+    t0 = time.perf_counter()
+    ref.step(2, grav)
+    t_node = (time.perf_counter() - t0) / 2 / (inp.nx * inp.ny * 16)
+    budget = 60.0
+    nodes_per_step = budget / max(1, K + W) / max(t_node, 1e-12)
+    nxs, nys = inp.nx, inp.ny
+    nzs = int(nodes_per_step // (nxs * nys))
+    while nzs < 3 and nys > 32:          # shrink the plane (multiples of 32) before going below 3 planes
+        nys = max(32, nys // 2)
+        nzs = int(nodes_per_step // (nxs * nys))
+    while nzs < 3 and nxs > 32:
+        nxs = max(32, nxs // 2)
+        nzs = int(nodes_per_step // (nxs * nys))
+    nzs = int(max(3, min(inp.nz, nzs)))
+    ref = make_ref(nxs, nys, nzs)
+    ref.step(W, grav)
+    t0 = time.perf_counter()
+    ref.step(K, grav)
+    dt = time.perf_counter() - t0
+    nodes = nxs * nys * nzs
+    value = nodes * K / dt / 1e6
+    sample = (f"reference kernels (src/*.cu compiled for the host CPU), {nxs}x{nys}x{nzs} slab of the "
+              f"{inp.nx}^3 workload, {K} steps after {W} warm-up, {dt:.1f} s")
+    return {"metric": METRIC, "value": round(value, 2), "unit": "MLUPS", "n_gpus": world, "steps": K,
+            "warmup": W, "ms_per_step": round(dt / K * 1e3, 3), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
+            "config": {"workload": f"bubbly_{args.size} (slab {nxs}x{nys}x{nzs})", "nx": nxs, "ny": nys,
+                       "nz": nzs, "storage": "fp32"},
+            "cpu_baseline": {"value": round(value, 2), "unit": "MLUPS", "cores": RefCPU.threads(),
+                             "kind": "reference", "sample": sample},
+            "e2e": {"value": round(value, 2), "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main(argv=None):
+    args = parse_args(argv)
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        res = run_reference(args, rank, world)
+        if res is not None:
+            print(json.dumps(res))
+        return 0
+    if world > 1:
+        import torch
+        torch.cuda.set_device(local)
+        torch.distributed.init_process_group("nccl")
+    res = run_ours(args, rank, world, local)
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(res))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,171 @@
+/*
+ * lbm_gb300.h -- C-ABI of liblbm_gb300.so, a GB300 (sm_103a) implementation of
+ * the Zheng-Shu-Chew free-energy multiphase lattice Boltzmann step
+ * (D3Q7 order-parameter distribution f + D3Q19 momentum distribution g).
+ *
+ * The reference (carlosrosales/lbm_bench_gpu) has no library boundary: its
+ * driver src/main.cu allocates ~40 device arrays, copies constants with
+ * cudaMemcpyToSymbol and launches nine kernels plus three host-staged halo
+ * exchanges per step.  Each entry point below replaces one stage of that
+ * driver; the citation next to it names the reference lines it stands for.
+ *
+ * Conventions
+ *  - Names follow the reference: f = D3Q7 (phi, relaxed with tauPhi),
+ *    g = D3Q19 (momentum, relaxed with tauRho), rho = ZSC mean density n.
+ *  - Host arrays are caller-owned, x fastest: idx = x + nx*(y + ny*z), with
+ *    z in [0, nz) standing for the reference's interior plane k = z + 1.
+ *  - Every function returns an LBM_* status and never aborts.
+ *  - One host thread per context.  lbm_step is asynchronous on the context's
+ *    CUDA stream; every call that hands data back to the host synchronises.
+ */
+#ifndef LBM_GB300_H
+#define LBM_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define LBM_OK 0
+#define LBM_EINVAL 1      /* bad argument or unsupported size */
+#define LBM_ENOMEM 2      /* device or host allocation failed */
+#define LBM_ECUDA 3       /* a CUDA call or a kernel launch failed */
+#define LBM_ENAN 4        /* the state holds NaN or Inf */
+#define LBM_ETIMEOUT 5    /* a bounded device wait gave up */
+#define LBM_EIO 6         /* an input file is missing or malformed */
+#define LBM_ESTATE 7      /* call out of order (e.g. adjoint without a recorded forward) */
+
+/* storage formats of the distributions (arithmetic is always FP32) */
+#define LBM_STORAGE_FP32 0
+#define LBM_STORAGE_FP16 1   /* shifted, scaled half precision */
+#define LBM_STORAGE_BF16 2   /* shifted, scaled bfloat16 */
+
+typedef struct lbm_ctx lbm_ctx;
+
+/* The physical and numerical inputs of properties.in (src/paramread.c:40-59)
+ * plus the radius of the first bubble of discrete.in, which sets the gravity
+ * scale (src/paramread.c:160). */
+typedef struct lbm_params {
+    int nx, ny, nz;           /* xmax ymax zmax: interior nodes */
+    int block_x, block_y;     /* BLOCK_SIZE_X BLOCK_SIZE_Y: validated in compat mode, not used for launch */
+    float rhoL, rhoH;
+    float tauRho, tauPhi;
+    float width, sigma, Gamma;
+    float Eo;
+    float rc0;                /* Rc of the first bubble */
+    int storage;              /* LBM_STORAGE_* */
+    int device;               /* CUDA device ordinal */
+    int compat;               /* 1: reject what src/main.cu:167-173 rejects */
+} lbm_params;
+
+/* The step counters of properties.in (src/paramread.c:41-42). */
+typedef struct lbm_run {
+    int max_step, relax_step, save, stat;
+} lbm_run;
+
+/* Derived constants, src/paramread.c:141-170 (computed in double, stored as float). */
+typedef struct lbm_derived {
+    float phiStar, phiStarSq;
+    float invTauRho, invTauRhoOne, invTauRhoHalf;
+    float eta, eta2, invEta2;
+    float invTauPhi, invTauPhiOne;
+    float alpha, alpha4, kappa;
+    float gravity, grav;      /* grav: the body force of the evolution loop (src/main.cu:397) */
+    float K0, K1, K2, KC0, KC1, KC2;
+} lbm_derived;
+
+/* Statistics over the phi, rho, u arrays.
+ * "compat" values reproduce src/stats.c:39-91 and src/logsave.c:63-167: they
+ * skip the planes x = 0, nx-1 and y = 0, ny-1, as the reference does, and
+ * Pout divides by nx*ny*nz - vol.  The full-domain sums are FP64 over every
+ * node. */
+typedef struct lbm_stats_out {
+    long long step;           /* steps taken since lbm_init */
+    double umax;              /* compat: sqrt(max |u|^2) */
+    double vol;               /* compat: number of nodes with phi >= 0 */
+    double ux_av, uy_av, uz_av;   /* compat: mean u over phi >= 0 */
+    double ref;               /* compat: (0.75 vol / pi)^(1/3) */
+    double p_in, p_out, p_dif, p_err;   /* compat: Laplace-law check */
+    double phi_sum, rho_sum;  /* full domain: sum phi, sum rho */
+    double mom_x, mom_y, mom_z;         /* full domain: sum rho u */
+    double vol_full;          /* full domain: number of nodes with phi >= 0 */
+    double umax_full;         /* full domain: sqrt(max |u|^2) */
+    long long nonfinite;      /* nodes whose phi, rho or u is NaN or Inf */
+} lbm_stats_out;
+
+/* Parse dir/properties.in and dir/discrete.in in the reference's positional
+ * format (src/paramread.c:36-75; header tokens are skipped by count).
+ * bubbles receives up to max_bubbles rows of {xc, yc, zc, Rc}; *nbubbles is
+ * the count in the file.  dir NULL means the current directory. */
+int lbm_read_inputs(const char *dir, lbm_params *p, lbm_run *run, float *bubbles, int max_bubbles,
+                    int *nbubbles);
+
+/* Derived constants for p (src/paramread.c:141-170). */
+int lbm_derive(const lbm_params *p, lbm_derived *d);
+
+/* Create a context and the initial state from host fields, each nx*ny*nz
+ * values: host init -> upload -> init_f/init_g of src/main.cu:213-274.  The
+ * initial equilibrium is at rest (src/init_f.cu:72-78, src/init_g.cu:77-91);
+ * u0 only fills the velocity arrays.  phi_ghost may be NULL (periodic z) or
+ * 2*nx*ny values: the plane below z = 0, then the plane above z = nz-1, which
+ * the reference fills from the bubble geometry (src/init.c:41-59). */
+int lbm_init(lbm_ctx **out, const lbm_params *p, const float *phi0, const float *rho0, const float *ux0,
+             const float *uy0, const float *uz0, const float *phi_ghost);
+
+/* As lbm_init, with the bubble initial condition computed on the GPU
+ * (src/init.c:39-59: phi = -phiStar, then for each bubble in order, nodes with
+ * R <= Rc + width take phiStar*tanh(2(Rc - R)/width); rho = (rhoH + rhoL)/2;
+ * u = 0; ghost planes from the geometry).  bubbles: nbubbles rows of
+ * {xc, yc, zc, Rc} in the reference's coordinates (x, y 0-based, z 1-based). */
+int lbm_init_bubbles(lbm_ctx **out, const lbm_params *p, const float *bubbles, int nbubbles);
+
+/* Advance nsteps time steps with body force grav (0 while relaxing): the loop
+ * bodies of src/main.cu:281-392 and :414-528 without their stats/vtk output.
+ * One fused kernel per step.  Asynchronous on the context's stream. */
+int lbm_step(lbm_ctx *c, int nsteps, float grav);
+
+/* Statistics (see lbm_stats_out) of the phi, rho, u arrays as the reference
+ * holds them: the moments computed at the start of the last step
+ * (src/update_phi.cu, src/update_rho.cu, src/update_velocity.cu), or the
+ * initial fields before any step.  Replaces src/stats.c:28-96 and the pressure
+ * part of src/logsave.c:63-167.  Each non-NULL field pointer receives
+ * nx*ny*nz floats.  s may be NULL.  Returns LBM_ENAN (after filling s) when a
+ * field holds NaN or Inf.  Synchronises. */
+int lbm_stats(lbm_ctx *c, lbm_stats_out *s, float *phi, float *rho, float *ux, float *uy, float *uz);
+
+/* The current distributions in streamed form, as the reference's lower halves
+ * hold them after a step: f as 7 blocks and g as 19 blocks of nx*ny*nz floats
+ * (reference direction order).  NULL skips.  Synchronises. */
+int lbm_get_dist(lbm_ctx *c, float *f, float *g);
+
+/* Replace the state by streamed distributions (same layout as lbm_get_dist),
+ * e.g. to resume from a snapshot.  The phi, rho, u arrays are recomputed as
+ * their moments.  Synchronises. */
+int lbm_set_dist(lbm_ctx *c, const float *f, const float *g);
+
+/* Steps taken since lbm_init. */
+long long lbm_steps_done(const lbm_ctx *c);
+
+/* The context's CUDA stream (a cudaStream_t), for callers that time or order
+ * work around lbm_step. */
+void *lbm_stream(const lbm_ctx *c);
+
+/* Wait for all work queued on the context. */
+int lbm_sync(lbm_ctx *c);
+
+/* Release the context and all its device memory.  NULL is a no-op. */
+void lbm_destroy(lbm_ctx *c);
+
+/* Text for a status code. */
+const char *lbm_strerror(int code);
+
+/* Detail of the last failure on this thread (CUDA error text, file name, ...). */
+const char *lbm_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LBM_GB300_H */

@@ -1,0 +1,240 @@
+"""ctypes bindings of liblbm_gb300.so (the C-ABI in include/lbm_gb300.h).
+
+This is the Python face of the same entry points a C, C++ or Fortran driver
+calls.  There is no fallback: if the library is missing or cannot be loaded,
+``load()`` raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "liblbm_gb300.so"
+
+LBM_OK, LBM_EINVAL, LBM_ENOMEM, LBM_ECUDA, LBM_ENAN, LBM_ETIMEOUT, LBM_EIO, LBM_ESTATE = range(8)
+STORAGE = {"fp32": 0, "fp16": 1, "bf16": 2}
+
+# Every symbol include/lbm_gb300.h declares.
+EXPORTS = [
+    "lbm_read_inputs", "lbm_derive", "lbm_init", "lbm_init_bubbles", "lbm_step", "lbm_stats",
+    "lbm_get_dist", "lbm_set_dist", "lbm_steps_done", "lbm_stream", "lbm_sync", "lbm_destroy",
+    "lbm_strerror", "lbm_last_error",
+]
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
+        ("block_x", C.c_int), ("block_y", C.c_int),
+        ("rhoL", C.c_float), ("rhoH", C.c_float),
+        ("tauRho", C.c_float), ("tauPhi", C.c_float),
+        ("width", C.c_float), ("sigma", C.c_float), ("Gamma", C.c_float),
+        ("Eo", C.c_float), ("rc0", C.c_float),
+        ("storage", C.c_int), ("device", C.c_int), ("compat", C.c_int),
+    ]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class Run(C.Structure):
+    _fields_ = [("max_step", C.c_int), ("relax_step", C.c_int), ("save", C.c_int), ("stat", C.c_int)]
+
+
+class Derived(C.Structure):
+    _fields_ = [(k, C.c_float) for k in (
+        "phiStar", "phiStarSq", "invTauRho", "invTauRhoOne", "invTauRhoHalf", "eta", "eta2", "invEta2",
+        "invTauPhi", "invTauPhiOne", "alpha", "alpha4", "kappa", "gravity", "grav",
+        "K0", "K1", "K2", "KC0", "KC1", "KC2")]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class StatsOut(C.Structure):
+    _fields_ = [("step", C.c_longlong)] + [(k, C.c_double) for k in (
+        "umax", "vol", "ux_av", "uy_av", "uz_av", "ref", "p_in", "p_out", "p_dif", "p_err",
+        "phi_sum", "rho_sum", "mom_x", "mom_y", "mom_z", "vol_full", "umax_full")] + [("nonfinite", C.c_longlong)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class LbmError(RuntimeError):
+    def __init__(self, code: int, what: str, detail: str):
+        super().__init__(f"{what}: status {code} ({detail})")
+        self.code = code
+
+
+_lib: C.CDLL | None = None
+
+_F = C.POINTER(C.c_float)
+
+
+def load(path: str | os.PathLike | None = None) -> C.CDLL:
+    """Load liblbm_gb300.so (raises OSError if it is missing)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise OSError(f"{p} not found: build it with `python -m lbm_bench_gpu_gb300.build`")
+    lib = C.CDLL(str(p))
+    lib.lbm_read_inputs.argtypes = [C.c_char_p, C.POINTER(Params), C.POINTER(Run), _F, C.c_int, C.POINTER(C.c_int)]
+    lib.lbm_derive.argtypes = [C.POINTER(Params), C.POINTER(Derived)]
+    lib.lbm_init.argtypes = [C.POINTER(C.c_void_p), C.POINTER(Params), _F, _F, _F, _F, _F, _F]
+    lib.lbm_init_bubbles.argtypes = [C.POINTER(C.c_void_p), C.POINTER(Params), _F, C.c_int]
+    lib.lbm_step.argtypes = [C.c_void_p, C.c_int, C.c_float]
+    lib.lbm_stats.argtypes = [C.c_void_p, C.POINTER(StatsOut), _F, _F, _F, _F, _F]
+    lib.lbm_get_dist.argtypes = [C.c_void_p, _F, _F]
+    lib.lbm_set_dist.argtypes = [C.c_void_p, _F, _F]
+    lib.lbm_steps_done.argtypes = [C.c_void_p]
+    lib.lbm_steps_done.restype = C.c_longlong
+    lib.lbm_stream.argtypes = [C.c_void_p]
+    lib.lbm_stream.restype = C.c_void_p
+    lib.lbm_sync.argtypes = [C.c_void_p]
+    lib.lbm_destroy.argtypes = [C.c_void_p]
+    lib.lbm_destroy.restype = None
+    lib.lbm_strerror.argtypes = [C.c_int]
+    lib.lbm_strerror.restype = C.c_char_p
+    lib.lbm_last_error.argtypes = []
+    lib.lbm_last_error.restype = C.c_char_p
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def check(code: int, what: str) -> None:
+    if code != LBM_OK:
+        lib = load()
+        detail = lib.lbm_last_error().decode() or lib.lbm_strerror(code).decode()
+        raise LbmError(code, what, detail)
+
+
+def fptr(a: np.ndarray | None):
+    if a is None:
+        return None
+    assert a.dtype == np.float32 and a.flags.c_contiguous
+    return a.ctypes.data_as(_F)
+
+
+def make_params(nx: int, ny: int, nz: int, *, rhoL: float, rhoH: float, tauRho: float, tauPhi: float,
+                width: float, sigma: float, Gamma: float, Eo: float = 0.0, rc0: float = 0.0,
+                block_x: int = 32, block_y: int = 8, storage: str = "fp32", device: int = 0,
+                compat: bool = False) -> Params:
+    p = Params()
+    p.nx, p.ny, p.nz = nx, ny, nz
+    p.block_x, p.block_y = block_x, block_y
+    p.rhoL, p.rhoH, p.tauRho, p.tauPhi = rhoL, rhoH, tauRho, tauPhi
+    p.width, p.sigma, p.Gamma, p.Eo, p.rc0 = width, sigma, Gamma, Eo, rc0
+    p.storage, p.device, p.compat = STORAGE[storage], device, int(compat)
+    return p
+
+
+def read_inputs(directory: str | os.PathLike, max_bubbles: int = 4096):
+    """Parse properties.in / discrete.in with the library's reader.
+
+    Returns (Params, Run, bubbles (nb x 4 float32))."""
+    lib = load()
+    p, r = Params(), Run()
+    buf = np.zeros((max_bubbles, 4), np.float32)
+    nb = C.c_int(0)
+    check(lib.lbm_read_inputs(str(directory).encode(), C.byref(p), C.byref(r), fptr(buf), max_bubbles,
+                              C.byref(nb)), "lbm_read_inputs")
+    if nb.value > max_bubbles:
+        return read_inputs(directory, nb.value)
+    return p, r, buf[: nb.value].copy()
+
+
+def derive(p: Params) -> Derived:
+    d = Derived()
+    check(load().lbm_derive(C.byref(p), C.byref(d)), "lbm_derive")
+    return d
+
+
+class Lattice:
+    """One simulation context on one GPU (owns all its device memory)."""
+
+    def __init__(self, handle: C.c_void_p, params: Params):
+        self._h = handle
+        self.params = params
+        self.shape = (params.nz, params.ny, params.nx)
+        self.n = params.nx * params.ny * params.nz
+
+    @classmethod
+    def from_fields(cls, params: Params, phi, rho, ux=None, uy=None, uz=None, phi_ghost=None) -> "Lattice":
+        lib = load()
+        h = C.c_void_p()
+        arrs = [None if a is None else np.ascontiguousarray(a, np.float32) for a in (phi, rho, ux, uy, uz, phi_ghost)]
+        check(lib.lbm_init(C.byref(h), C.byref(params), *[fptr(a) for a in arrs]), "lbm_init")
+        return cls(h, params)
+
+    @classmethod
+    def from_bubbles(cls, params: Params, bubbles) -> "Lattice":
+        lib = load()
+        h = C.c_void_p()
+        b = np.ascontiguousarray(bubbles, np.float32).reshape(-1, 4)
+        check(lib.lbm_init_bubbles(C.byref(h), C.byref(params), fptr(b) if len(b) else None, len(b)),
+              "lbm_init_bubbles")
+        return cls(h, params)
+
+    def step(self, nsteps: int, grav: float = 0.0) -> None:
+        check(load().lbm_step(self._h, int(nsteps), float(grav)), "lbm_step")
+
+    def stats(self, fields: bool = False, allow_nan: bool = False):
+        """Return (stats dict, fields dict or None)."""
+        s = StatsOut()
+        arrs = [np.empty(self.shape, np.float32) for _ in range(5)] if fields else [None] * 5
+        code = load().lbm_stats(self._h, C.byref(s), *[fptr(a) for a in arrs])
+        if not (allow_nan and code == LBM_ENAN):
+            check(code, "lbm_stats")
+        out = dict(zip(("phi", "rho", "ux", "uy", "uz"), arrs)) if fields else None
+        return s.as_dict(), out
+
+    def fields(self) -> dict:
+        arrs = [np.empty(self.shape, np.float32) for _ in range(5)]
+        check(load().lbm_stats(self._h, None, *[fptr(a) for a in arrs]), "lbm_stats")
+        return dict(zip(("phi", "rho", "ux", "uy", "uz"), arrs))
+
+    def dist(self):
+        f = np.empty((7,) + self.shape, np.float32)
+        g = np.empty((19,) + self.shape, np.float32)
+        check(load().lbm_get_dist(self._h, fptr(f), fptr(g)), "lbm_get_dist")
+        return f, g
+
+    def set_dist(self, f, g) -> None:
+        f = np.ascontiguousarray(f, np.float32)
+        g = np.ascontiguousarray(g, np.float32)
+        check(load().lbm_set_dist(self._h, fptr(f), fptr(g)), "lbm_set_dist")
+
+    @property
+    def steps(self) -> int:
+        return int(load().lbm_steps_done(self._h))
+
+    @property
+    def stream(self) -> int:
+        return int(load().lbm_stream(self._h) or 0)
+
+    def sync(self) -> None:
+        check(load().lbm_sync(self._h), "lbm_sync")
+
+    def close(self) -> None:
+        if self._h:
+            load().lbm_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

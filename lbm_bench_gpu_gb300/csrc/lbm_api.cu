@@ -1,0 +1,325 @@
+// lbm_api.cu -- the C-ABI of liblbm_gb300 (include/lbm_gb300.h).
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "lbm_internal.h"
+
+struct lbm_ctx {
+    lbm_params p;
+    lbm_derived d;
+    lbm::Box box;
+    cudaStream_t stream = nullptr;
+    lbm::State st;
+    bool g_odd_next = false;       // the next step reads g in the AA "odd" layout
+    double *partials = nullptr;    // stats scratch: per-block partial sums
+    size_t partial_count = 0;
+    double *result = nullptr;      // stats result (device)
+    double *result_host = nullptr; // pinned copy
+};
+
+namespace {
+
+int fail(int code, const std::string &msg)
+{
+    lbm::set_error(msg);
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char *what)
+{
+    return fail(e == cudaErrorMemoryAllocation ? LBM_ENOMEM : LBM_ECUDA,
+                std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define LBM_CUDA(call, what)                          \
+    do {                                              \
+        cudaError_t e_ = (call);                      \
+        if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+    } while (0)
+
+int validate(const lbm_params *p)
+{
+    if (!p) return fail(LBM_EINVAL, "params is NULL");
+    if (p->nx < 32 || p->ny < 8 || p->nz < 3)
+        return fail(LBM_EINVAL, "box too small (need nx >= 32, ny >= 8, nz >= 3)");
+    if (p->nx % 32 != 0) return fail(LBM_EINVAL, "nx must be a multiple of 32");
+    if (p->ny % 8 != 0) return fail(LBM_EINVAL, "ny must be a multiple of 8");
+    if (p->compat) {
+        // src/main.cu:167-173
+        if (p->ny % 32 != 0) return fail(LBM_EINVAL, "NY is not a multiple of 32");
+        if (p->block_x * p->block_y > 512) return fail(LBM_EINVAL, "Too many blocks");
+        if (p->nx < p->block_x) return fail(LBM_EINVAL, "BLOCK_SIZE_X is too large");
+        if (p->ny < p->block_y) return fail(LBM_EINVAL, "BLOCK_SIZE_Y is too large");
+    }
+    const double n = (double)p->nx * p->ny * p->nz;
+    if (n * lbm::kQg >= 4294967296.0) return fail(LBM_EINVAL, "box too large for 32-bit element indexing");
+    if (!(p->tauRho > 0.f) || !(p->tauPhi > 0.f) || !(p->width > 0.f))
+        return fail(LBM_EINVAL, "tauRho, tauPhi and width must be positive");
+    if (!(p->rhoH != p->rhoL)) return fail(LBM_EINVAL, "rhoH must differ from rhoL");
+    if (p->Eo != 0.f && !(p->rc0 > 0.f)) return fail(LBM_EINVAL, "rc0 must be positive when Eo is not zero");
+    if (p->storage != LBM_STORAGE_FP32) return fail(LBM_EINVAL, "storage format not supported");
+    return LBM_OK;
+}
+
+// Allocate a context and its buffers; the state is left uninitialised.
+int create(lbm_ctx **out, const lbm_params *p)
+{
+    if (!out) return fail(LBM_EINVAL, "out is NULL");
+    *out = nullptr;
+    int rc = validate(p);
+    if (rc) return rc;
+    LBM_CUDA(cudaSetDevice(p->device), "cudaSetDevice");
+    lbm_ctx *c = new (std::nothrow) lbm_ctx();
+    if (!c) return fail(LBM_ENOMEM, "host allocation");
+    c->p = *p;
+    lbm::derive(c->p, c->d);
+    if (c->p.Eo == 0.f) {
+        c->d.gravity = 0.f;
+        c->d.grav = 0.f;
+    }
+    c->box.nx = p->nx;
+    c->box.ny = p->ny;
+    c->box.nz = p->nz;
+    c->box.nxy = (long long)p->nx * p->ny;
+    c->box.n = c->box.nxy * p->nz;
+    const size_t n = (size_t)c->box.n;
+    cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&c->st.f, sizeof(float) * 2 * lbm::kQf * n);
+    if (e == cudaSuccess) e = cudaMalloc(&c->st.g, sizeof(float) * lbm::kQg * n);
+    if (e == cudaSuccess) e = cudaMalloc(&c->st.mom, sizeof(float) * 5 * n);
+    c->partial_count = lbm::stats_partial_count(c->box);
+    if (e == cudaSuccess) e = cudaMalloc(&c->partials, sizeof(double) * lbm::kStatsValues * c->partial_count);
+    if (e == cudaSuccess) e = cudaMalloc(&c->result, sizeof(double) * lbm::kStatsValues);
+    if (e == cudaSuccess) e = cudaMallocHost(&c->result_host, sizeof(double) * lbm::kStatsValues);
+    if (e != cudaSuccess) {
+        lbm_destroy(c);
+        return cuda_fail(e, "context allocation");
+    }
+    *out = c;
+    return LBM_OK;
+}
+
+float *f_half(lbm_ctx *c, int half) { return c->st.f + (size_t)half * lbm::kQf * c->box.n; }
+
+int finish_init(lbm_ctx *c)
+{
+    c->st.f_cur = 0;
+    c->st.f_streamed = true;
+    c->st.steps = 0;
+    c->g_odd_next = false;
+    LBM_CUDA(cudaStreamSynchronize(c->stream), "initialisation");
+    return LBM_OK;
+}
+
+}  // namespace
+
+extern "C" int lbm_init(lbm_ctx **out, const lbm_params *p, const float *phi0, const float *rho0, const float *ux0,
+                        const float *uy0, const float *uz0, const float *phi_ghost)
+{
+    if (!phi0 || !rho0) return fail(LBM_EINVAL, "phi0 and rho0 are required");
+    lbm_ctx *c = nullptr;
+    int rc = create(&c, p);
+    if (rc) return rc;
+    const size_t n = (size_t)c->box.n, bytes = sizeof(float) * n;
+    float *mom = c->st.mom;
+    float *ghost = nullptr;
+    auto bail = [&](cudaError_t e, const char *what) {
+        if (ghost) cudaFree(ghost);
+        lbm_destroy(c);
+        return cuda_fail(e, what);
+    };
+    cudaError_t e = cudaMemcpyAsync(mom, phi0, bytes, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(mom + n, rho0, bytes, cudaMemcpyHostToDevice, c->stream);
+    const float *u[3] = {ux0, uy0, uz0};
+    for (int a = 0; a < 3 && e == cudaSuccess; a++) {
+        if (u[a]) e = cudaMemcpyAsync(mom + (2 + a) * n, u[a], bytes, cudaMemcpyHostToDevice, c->stream);
+        else e = cudaMemsetAsync(mom + (2 + a) * n, 0, bytes, c->stream);
+    }
+    if (e == cudaSuccess && phi_ghost) {
+        e = cudaMalloc(&ghost, sizeof(float) * 2 * c->box.nxy);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(ghost, phi_ghost, sizeof(float) * 2 * c->box.nxy, cudaMemcpyHostToDevice, c->stream);
+    }
+    if (e == cudaSuccess)
+        e = lbm::launch_equilibrium(c->box, c->d, c->p.Gamma, mom, mom + n, ghost, ghost ? ghost + c->box.nxy : nullptr,
+                                    f_half(c, 0), c->st.g, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return bail(e, "lbm_init");
+    if (ghost) cudaFree(ghost);
+    rc = finish_init(c);
+    if (rc) {
+        lbm_destroy(c);
+        return rc;
+    }
+    *out = c;
+    return LBM_OK;
+}
+
+extern "C" int lbm_init_bubbles(lbm_ctx **out, const lbm_params *p, const float *bubbles, int nbubbles)
+{
+    if (nbubbles < 0 || (nbubbles > 0 && !bubbles)) return fail(LBM_EINVAL, "bad bubble list");
+    lbm_ctx *c = nullptr;
+    int rc = create(&c, p);
+    if (rc) return rc;
+    const size_t n = (size_t)c->box.n, nxy = (size_t)c->box.nxy;
+    float *phig = nullptr, *bub = nullptr;
+    float *mom = c->st.mom;
+    cudaError_t e = cudaMalloc(&phig, sizeof(float) * nxy * (c->box.nz + 2));
+    if (e == cudaSuccess && nbubbles > 0) e = cudaMalloc(&bub, sizeof(float) * 4 * nbubbles);
+    if (e == cudaSuccess && nbubbles > 0)
+        e = cudaMemcpyAsync(bub, bubbles, sizeof(float) * 4 * nbubbles, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess)
+        e = lbm::launch_bubble_phi(c->box, bub, nbubbles, c->d.phiStar, c->p.width, phig, c->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(mom, phig + nxy, sizeof(float) * n, cudaMemcpyDeviceToDevice, c->stream);
+    if (e == cudaSuccess) e = lbm::launch_fill(mom + n, (long long)n, 0.5f * (c->p.rhoH + c->p.rhoL), c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(mom + 2 * n, 0, sizeof(float) * 3 * n, c->stream);
+    if (e == cudaSuccess)
+        e = lbm::launch_equilibrium(c->box, c->d, c->p.Gamma, mom, mom + n, phig, phig + nxy * (c->box.nz + 1),
+                                    f_half(c, 0), c->st.g, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (phig) cudaFree(phig);
+    if (bub) cudaFree(bub);
+    if (e != cudaSuccess) {
+        lbm_destroy(c);
+        return cuda_fail(e, "lbm_init_bubbles");
+    }
+    rc = finish_init(c);
+    if (rc) {
+        lbm_destroy(c);
+        return rc;
+    }
+    *out = c;
+    return LBM_OK;
+}
+
+extern "C" int lbm_step(lbm_ctx *c, int nsteps, float grav)
+{
+    if (!c) return fail(LBM_EINVAL, "context is NULL");
+    if (nsteps < 0) return fail(LBM_EINVAL, "nsteps < 0");
+    if (!std::isfinite(grav)) return fail(LBM_EINVAL, "grav is not finite");
+    const lbm::StepConst k = lbm::step_const(c->d, c->p, grav);
+    for (int s = 0; s < nsteps; s++) {
+        const int in = c->st.f_cur, outh = 1 - in;
+        cudaError_t e = lbm::launch_step(c->box, k, f_half(c, in), f_half(c, outh), c->st.g, c->st.mom,
+                                         c->st.f_streamed, c->g_odd_next, s == nsteps - 1, c->stream);
+        if (e != cudaSuccess) return cuda_fail(e, "step kernel launch");
+        c->st.f_cur = outh;
+        c->st.f_streamed = false;
+        c->g_odd_next = !c->g_odd_next;
+        c->st.steps++;
+    }
+    return LBM_OK;
+}
+
+extern "C" int lbm_stats(lbm_ctx *c, lbm_stats_out *s, float *phi, float *rho, float *ux, float *uy, float *uz)
+{
+    if (!c) return fail(LBM_EINVAL, "context is NULL");
+    const size_t n = (size_t)c->box.n, bytes = sizeof(float) * n;
+    if (s) {
+        cudaError_t e = lbm::launch_stats(c->box, c->d, c->st.mom, c->partials, c->partial_count, c->result,
+                                          nullptr, c->stream);
+        if (e != cudaSuccess) return cuda_fail(e, "stats kernel launch");
+        LBM_CUDA(cudaMemcpyAsync(c->result_host, c->result, sizeof(double) * lbm::kStatsValues,
+                                 cudaMemcpyDeviceToHost, c->stream),
+                 "stats copy");
+    }
+    float *dst[5] = {phi, rho, ux, uy, uz};
+    for (int a = 0; a < 5; a++)
+        if (dst[a])
+            LBM_CUDA(cudaMemcpyAsync(dst[a], c->st.mom + a * n, bytes, cudaMemcpyDeviceToHost, c->stream),
+                     "field copy");
+    LBM_CUDA(cudaStreamSynchronize(c->stream), "lbm_stats");
+    if (!s) return LBM_OK;
+    const double *r = c->result_host;
+    std::memset(s, 0, sizeof(*s));
+    s->step = c->st.steps;
+    s->umax = std::sqrt(r[0]);
+    s->vol = r[1];
+    s->ux_av = r[1] > 0 ? r[2] / r[1] : 0.0;
+    s->uy_av = r[1] > 0 ? r[3] / r[1] : 0.0;
+    s->uz_av = r[1] > 0 ? r[4] / r[1] : 0.0;
+    s->ref = std::pow(r[1] * 0.75 / M_PI, 1.0 / 3.0);
+    const double vol_out = (double)c->box.n - r[1];
+    s->p_in = r[1] > 0 ? r[5] / r[1] : 0.0;
+    s->p_out = vol_out > 0 ? r[6] / vol_out : 0.0;
+    s->p_dif = s->p_in - s->p_out;
+    s->p_err = c->p.rc0 > 0.f ? 0.5 * (2.0 * c->p.sigma / c->p.rc0 - s->p_dif) * c->p.rc0 / c->p.sigma : 0.0;
+    s->phi_sum = r[7];
+    s->rho_sum = r[8];
+    s->mom_x = r[9];
+    s->mom_y = r[10];
+    s->mom_z = r[11];
+    s->vol_full = r[12];
+    s->umax_full = std::sqrt(r[13]);
+    s->nonfinite = (long long)r[14];
+    if (s->nonfinite > 0) return fail(LBM_ENAN, std::to_string(s->nonfinite) + " non-finite nodes");
+    return LBM_OK;
+}
+
+extern "C" int lbm_get_dist(lbm_ctx *c, float *f, float *g)
+{
+    if (!c) return fail(LBM_EINVAL, "context is NULL");
+    if (!f && !g) return LBM_OK;
+    const size_t n = (size_t)c->box.n;
+    float *tmp = nullptr;
+    const size_t count = (f ? lbm::kQf : 0) + (g ? lbm::kQg : 0);
+    LBM_CUDA(cudaMalloc(&tmp, sizeof(float) * count * n), "lbm_get_dist scratch");
+    float *tf = f ? tmp : nullptr;
+    float *tg = g ? tmp + (f ? lbm::kQf * n : 0) : nullptr;
+    cudaError_t e = lbm::launch_stream_out(c->box, c->d.eta, f_half(c, c->st.f_cur), c->st.f_streamed, c->st.g,
+                                           c->g_odd_next, tf, tg, c->stream);
+    if (e == cudaSuccess && f)
+        e = cudaMemcpyAsync(f, tf, sizeof(float) * lbm::kQf * n, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess && g)
+        e = cudaMemcpyAsync(g, tg, sizeof(float) * lbm::kQg * n, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cudaFree(tmp);
+    if (e != cudaSuccess) return cuda_fail(e, "lbm_get_dist");
+    return LBM_OK;
+}
+
+extern "C" int lbm_set_dist(lbm_ctx *c, const float *f, const float *g)
+{
+    if (!c || !f || !g) return fail(LBM_EINVAL, "NULL argument");
+    const size_t n = (size_t)c->box.n;
+    LBM_CUDA(cudaStreamSynchronize(c->stream), "lbm_set_dist");
+    LBM_CUDA(cudaMemcpyAsync(f_half(c, 0), f, sizeof(float) * lbm::kQf * n, cudaMemcpyHostToDevice, c->stream),
+             "lbm_set_dist f");
+    LBM_CUDA(cudaMemcpyAsync(c->st.g, g, sizeof(float) * lbm::kQg * n, cudaMemcpyHostToDevice, c->stream),
+             "lbm_set_dist g");
+    LBM_CUDA(lbm::launch_moments(c->box, f_half(c, 0), c->st.g, c->st.mom, c->stream), "moments kernel");
+    LBM_CUDA(cudaStreamSynchronize(c->stream), "lbm_set_dist");
+    c->st.f_cur = 0;
+    c->st.f_streamed = true;
+    c->g_odd_next = false;
+    return LBM_OK;
+}
+
+extern "C" long long lbm_steps_done(const lbm_ctx *c) { return c ? c->st.steps : -1; }
+
+extern "C" void *lbm_stream(const lbm_ctx *c) { return c ? (void *)c->stream : nullptr; }
+
+extern "C" int lbm_sync(lbm_ctx *c)
+{
+    if (!c) return fail(LBM_EINVAL, "context is NULL");
+    LBM_CUDA(cudaStreamSynchronize(c->stream), "lbm_sync");
+    return LBM_OK;
+}
+
+extern "C" void lbm_destroy(lbm_ctx *c)
+{
+    if (!c) return;
+    cudaSetDevice(c->p.device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    cudaFree(c->st.f);
+    cudaFree(c->st.g);
+    cudaFree(c->st.mom);
+    cudaFree(c->partials);
+    cudaFree(c->result);
+    if (c->result_host) cudaFreeHost(c->result_host);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}

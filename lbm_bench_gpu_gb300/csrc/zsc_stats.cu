@@ -1,0 +1,165 @@
+// zsc_stats.cu -- statistics of the phi, rho, u arrays in FP64.
+//
+// Replaces the host loops of src/stats.c:39-58 and the pressure part of
+// src/logsave.c:63-150.  One pass over the five arrays: per-thread FP64
+// accumulators, warp-shuffle reductions per block into a partials array, then
+// one block folds the partials in a fixed order (deterministic for a given box).
+//
+// Partial / result layout (doubles):
+//   0 max |u|^2 (compat)    1 #phi>=0 (compat)   2..4 sum u over phi>=0 (compat)
+//   5 sum p over phi>=0     6 sum p over phi<0 (compat)
+//   7 sum phi   8 sum rho   9..11 sum rho u   12 #phi>=0   13 max |u|^2
+//   14 #non-finite nodes    15 unused
+// "compat" skips the planes x = 0, nx-1 and y = 0, ny-1 like the reference.
+#include "lbm_internal.h"
+
+namespace lbm {
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kMaxBlocks = 152 * 8;
+constexpr float kInv6 = 0.16666666666666666667f;
+constexpr float kInv12 = 0.08333333333333333333f;
+
+struct StatsConst {
+    float alpha, kappa, phiStarSq;
+};
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ double warp_max(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// Block-wide reduction of acc[0..kStatsValues) (entries 0 and 13 by max, the
+// rest by sum); thread 0 writes the result to out.
+__device__ void block_reduce(double (&acc)[kStatsValues], double *out)
+{
+    __shared__ double red[kThreads / 32][kStatsValues];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int v = 0; v < kStatsValues; v++) {
+        const double r = (v == 0 || v == 13) ? warp_max(acc[v]) : warp_sum(acc[v]);
+        if (lane == 0) red[warp][v] = r;
+    }
+    __syncthreads();
+    if (threadIdx.x < kStatsValues) {
+        const int v = threadIdx.x;
+        double r = red[0][v];
+        for (int w = 1; w < kThreads / 32; w++) r = (v == 0 || v == 13) ? fmax(r, red[w][v]) : r + red[w][v];
+        out[v] = r;
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) stats_kernel(Box b, StatsConst c, const float *__restrict__ phi,
+                                                         const float *__restrict__ rho, const float *__restrict__ ux,
+                                                         const float *__restrict__ uy, const float *__restrict__ uz,
+                                                         double *__restrict__ partials)
+{
+    double acc[kStatsValues];
+#pragma unroll
+    for (int v = 0; v < kStatsValues; v++) acc[v] = 0.0;
+
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < b.n;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(t % b.nx);
+        const int j = (int)((t / b.nx) % b.ny);
+        const int k = (int)(t / b.nxy);
+        const float ph = phi[t], rh = rho[t], vx = ux[t], vy = uy[t], vz = uz[t];
+        if (!(isfinite(ph) && isfinite(rh) && isfinite(vx) && isfinite(vy) && isfinite(vz))) {
+            acc[14] += 1.0;
+            continue;
+        }
+        const double u2 = (double)vx * vx + (double)vy * vy + (double)vz * vz;
+        acc[7] += ph;
+        acc[8] += rh;
+        acc[9] += (double)rh * vx;
+        acc[10] += (double)rh * vy;
+        acc[11] += (double)rh * vz;
+        if (ph >= 0.f) acc[12] += 1.0;
+        acc[13] = fmax(acc[13], u2);
+        if (i < 1 || i > b.nx - 2 || j < 1 || j > b.ny - 2) continue;
+        acc[0] = fmax(acc[0], u2);
+
+        // pressure, src/logsave.c:94-137 (periodic neighbours)
+        const int ie = i == b.nx - 1 ? 0 : i + 1, iw = i == 0 ? b.nx - 1 : i - 1;
+        const int jn = j == b.ny - 1 ? 0 : j + 1, js = j == 0 ? b.ny - 1 : j - 1;
+        const int kt = k == b.nz - 1 ? 0 : k + 1, kb = k == 0 ? b.nz - 1 : k - 1;
+        auto P = [&](int x, int y, int z) -> float { return phi[x + b.nx * (y + (long long)b.ny * z)]; };
+        const float p01 = P(ie, j, k), p02 = P(iw, j, k), p03 = P(i, jn, k), p04 = P(i, js, k);
+        const float p05 = P(i, j, kt), p06 = P(i, j, kb), p07 = P(ie, jn, k), p08 = P(iw, js, k);
+        const float p09 = P(ie, js, k), p10 = P(iw, jn, k), p11 = P(ie, j, kt), p12 = P(iw, j, kb);
+        const float p13 = P(ie, j, kb), p14 = P(iw, j, kt), p15 = P(i, jn, kt), p16 = P(i, js, kb);
+        const float p17 = P(i, jn, kb), p18 = P(i, js, kt);
+        const double lap = ((double)p07 + p08 + p09 + p10 + p11 + p12 + p13 + p14 + p15 + p16 + p17 + p18
+                            + 2.0 * ((double)p01 + p02 + p03 + p04 + p05 + p06 - 12.0 * ph)) * kInv6;
+        const double gx = (2.0 * ((double)p01 - p02) + p07 - p08 + p09 - p10 + p11 - p12 + p13 - p14) * kInv12;
+        const double gy = (2.0 * ((double)p03 - p04) + p07 - p08 + p10 - p09 + p15 - p16 + p17 - p18) * kInv12;
+        const double gz = (2.0 * ((double)p05 - p06) + p11 - p12 + p14 - p13 + p15 - p16 + p18 - p17) * kInv12;
+        const double ph2 = (double)ph * ph;
+        const double pss = c.phiStarSq;
+        const double pres = c.alpha * (ph2 * (3.0 * ph2 - 2.0 * pss) - pss * pss)
+                            - c.kappa * (ph * lap - 0.5 * (gx * gx + gy * gy + gz * gz)) + rh / 3.0;
+        if (ph >= 0.f) {
+            acc[1] += 1.0;
+            acc[2] += vx;
+            acc[3] += vy;
+            acc[4] += vz;
+            acc[5] += pres;
+        } else {
+            acc[6] += pres;
+        }
+    }
+    block_reduce(acc, partials + (size_t)blockIdx.x * kStatsValues);
+}
+
+__global__ void __launch_bounds__(kThreads) fold_kernel(const double *__restrict__ partials, int nparts,
+                                                        double *__restrict__ out)
+{
+    double acc[kStatsValues];
+#pragma unroll
+    for (int v = 0; v < kStatsValues; v++) acc[v] = 0.0;
+    for (int p = threadIdx.x; p < nparts; p += blockDim.x) {
+#pragma unroll
+        for (int v = 0; v < kStatsValues; v++) {
+            const double x = partials[(size_t)p * kStatsValues + v];
+            acc[v] = (v == 0 || v == 13) ? fmax(acc[v], x) : acc[v] + x;
+        }
+    }
+    block_reduce(acc, out);
+}
+
+unsigned stats_blocks(const Box &b)
+{
+    long long blocks = (b.n + kThreads - 1) / kThreads;
+    if (blocks > kMaxBlocks) blocks = kMaxBlocks;
+    return (unsigned)(blocks < 1 ? 1 : blocks);
+}
+
+}  // namespace
+
+size_t stats_partial_count(const Box &b) { return stats_blocks(b); }
+
+cudaError_t launch_stats(const Box &b, const lbm_derived &d, const float *mom, double *partials,
+                         size_t partial_count, double *result, unsigned long long *, cudaStream_t s)
+{
+    const unsigned blocks = stats_blocks(b);
+    if (partial_count < blocks) return cudaErrorInvalidValue;
+    StatsConst c{d.alpha, d.kappa, d.phiStarSq};
+    stats_kernel<<<blocks, kThreads, 0, s>>>(b, c, mom, mom + b.n, mom + 2 * b.n, mom + 3 * b.n, mom + 4 * b.n,
+                                             partials);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    fold_kernel<<<1, kThreads, 0, s>>>(partials, (int)blocks, result);
+    return cudaGetLastError();
+}
+
+}  // namespace lbm

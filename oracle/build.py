@@ -1,0 +1,118 @@
+"""Build recipe for the test oracles (test infrastructure only).
+
+* ``build_oracle()`` compiles ``oracle/zsc_oracle.c`` (the FP64 restatement)
+  into ``oracle/_build/libzsc_oracle.so``.
+* ``build_reference()`` compiles the reference's own step kernels for the host
+  CPU (``oracle/ref_harness/zsc_ref_cpu.cpp`` + the reference sources, through
+  the CUDA/MPI emulation shim) into ``oracle/_ref/libzsc_ref.so``.
+
+The reference sources are read from ``$LBM_REFERENCE_SRC`` (default: the
+reference checkout's ``src/`` directory at /root/reference/src).  Where that
+directory exists the recipe first stages an unmodified copy of the files it
+needs into ``oracle/_ref/src`` (ignored by git; a machine without the
+checkout, such as the GPU host, builds from that staged copy).  Nothing is
+patched: inputs with more bubbles than the reference's MAX_BUBBLES are fed in
+as a phi field instead (see ``zr_init``).
+
+Usage: ``python oracle/build.py [oracle|reference|all]``.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+BUILD_DIR = HERE / "_build"
+REF_DIR = HERE / "_ref"
+REF_STAGE = REF_DIR / "src"
+ORACLE_SO = BUILD_DIR / "libzsc_oracle.so"
+REF_SO = REF_DIR / "libzsc_ref.so"
+
+DEFAULT_REFERENCE_SRC = "/root/reference/src"
+
+# Files of the reference that zsc_ref_cpu.cpp includes (src/main.cu:44-74 minus
+# the VTK writer).
+REFERENCE_FILES = [
+    "constants.h", "gridid.c", "init.c", "paramread.c", "logsave.c", "stats.c",
+    "mpiupdate.c", "mpiupdate_f.c", "mpiupdate_phi.c", "vgrid.c",
+    "init_f.cu", "init_g.cu", "update_phi.cu", "update_rho.cu", "update_velocity.cu",
+    "collision_f.cu", "collision_g.cu", "pack_mpi.cu", "pack_mpi_f.cu", "pack_mpi_phi.cu",
+    "stream_f.cu", "stream_g.cu", "unpack_mpi.cu", "unpack_mpi_f.cu", "unpack_mpi_phi.cu",
+]
+
+# Deterministic IEEE float arithmetic on x86-64 and aarch64 alike: no
+# contraction into fused multiply-adds, no fast-math.
+COMMON_FLAGS = ["-O2", "-fopenmp", "-fPIC", "-shared", "-ffp-contract=off"]
+
+
+def _newer(target: Path, sources: list[Path]) -> bool:
+    if not target.exists():
+        return False
+    t = target.stat().st_mtime
+    return all(s.exists() and s.stat().st_mtime <= t for s in sources)
+
+
+def build_oracle(force: bool = False) -> Path:
+    src = HERE / "zsc_oracle.c"
+    BUILD_DIR.mkdir(exist_ok=True)
+    if force or not _newer(ORACLE_SO, [src]):
+        cmd = ["gcc", *COMMON_FLAGS, "-std=c11", "-D_DEFAULT_SOURCE", str(src), "-o", str(ORACLE_SO), "-lm"]
+        subprocess.run(cmd, check=True)
+    return ORACLE_SO
+
+
+def reference_src_dir() -> Path | None:
+    """Directory holding the reference sources: the checkout, else the staged copy."""
+    env = os.environ.get("LBM_REFERENCE_SRC", DEFAULT_REFERENCE_SRC)
+    p = Path(env)
+    if all((p / f).exists() for f in REFERENCE_FILES):
+        return p
+    if all((REF_STAGE / f).exists() for f in REFERENCE_FILES):
+        return REF_STAGE
+    return None
+
+
+def stage_reference() -> Path | None:
+    """Copy the needed reference files, unmodified, into oracle/_ref/src."""
+    p = Path(os.environ.get("LBM_REFERENCE_SRC", DEFAULT_REFERENCE_SRC))
+    if not all((p / f).exists() for f in REFERENCE_FILES):
+        return REF_STAGE if all((REF_STAGE / f).exists() for f in REFERENCE_FILES) else None
+    REF_STAGE.mkdir(parents=True, exist_ok=True)
+    for f in REFERENCE_FILES:
+        dst = REF_STAGE / f
+        if not dst.exists() or dst.read_bytes() != (p / f).read_bytes():
+            shutil.copyfile(p / f, dst)
+    return REF_STAGE
+
+
+def build_reference(force: bool = False) -> Path | None:
+    """Compile the reference's kernels for the CPU; None if its sources are absent."""
+    stage_reference()
+    src_dir = reference_src_dir()
+    if src_dir is None:
+        return None
+    harness = HERE / "ref_harness" / "zsc_ref_cpu.cpp"
+    shim = HERE / "ref_harness" / "ref_shim.h"
+    deps = [harness, shim] + [src_dir / f for f in REFERENCE_FILES]
+    REF_DIR.mkdir(exist_ok=True)
+    if force or not _newer(REF_SO, deps):
+        cmd = ["g++", *COMMON_FLAGS, "-std=c++17", "-w", "-fvisibility=hidden", "-include", str(shim),
+               "-I", str(src_dir), "-I", str(shim.parent), str(harness), "-o", str(REF_SO), "-lm"]
+        subprocess.run(cmd, check=True)
+    return REF_SO
+
+
+def main(argv: list[str]) -> int:
+    what = argv[1] if len(argv) > 1 else "all"
+    if what in ("oracle", "all"):
+        print(build_oracle(force=True))
+    if what in ("reference", "all"):
+        print(build_reference(force=True) or "reference sources not found")
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main(sys.argv))

@@ -1,0 +1,242 @@
+"""ctypes front-ends of the two CPU checkers (test infrastructure only).
+
+* ``Oracle``  -- the FP64 restatement in zsc_oracle.c.
+* ``RefCPU``  -- the reference's own kernels compiled for the host CPU
+  (oracle/_ref/libzsc_ref.so, see oracle/build.py).
+
+Only tests, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline and
+reference legs use this module, and only as the checker or the timed CPU
+baseline -- never as the thing measured on the GPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+from . import build as _build
+
+_D = C.POINTER(C.c_double)
+_Fp = C.POINTER(C.c_float)
+
+
+def _dptr(a):
+    if a is None:
+        return None
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(_D)
+
+
+def _fptr(a):
+    if a is None:
+        return None
+    assert a.dtype == np.float32 and a.flags.c_contiguous
+    return a.ctypes.data_as(_Fp)
+
+
+_oracle_lib = None
+_ref_lib = None
+
+
+def oracle_lib() -> C.CDLL:
+    global _oracle_lib
+    if _oracle_lib is None:
+        lib = C.CDLL(str(_build.build_oracle()))
+        lib.zo_create.argtypes = [C.c_int, C.c_int, C.c_int, _D]
+        lib.zo_create.restype = C.c_void_p
+        lib.zo_destroy.argtypes = [C.c_void_p]
+        lib.zo_constants.argtypes = [C.c_void_p, _D]
+        lib.zo_bubble_phi.argtypes = [C.c_void_p, _Fp, C.c_int, _D]
+        lib.zo_init.argtypes = [C.c_void_p, _D, _D, _D, _D, _D, _D]
+        lib.zo_step.argtypes = [C.c_void_p, C.c_int, C.c_double]
+        lib.zo_moments.argtypes = [C.c_void_p, _D, _D, _D, _D, _D]
+        lib.zo_dist.argtypes = [C.c_void_p, _D, _D]
+        lib.zo_set_dist.argtypes = [C.c_void_p, _D, _D]
+        lib.zo_stats.argtypes = [C.c_void_p, _D]
+        lib.zo_steps.argtypes = [C.c_void_p]
+        lib.zo_steps.restype = C.c_long
+        lib.zo_threads.restype = C.c_int
+        _oracle_lib = lib
+    return _oracle_lib
+
+
+CONSTANT_NAMES = ["phiStar", "phiStarSq", "invTauRho", "invTauRhoOne", "invTauRhoHalf", "eta", "eta2",
+                  "invEta2", "invTauPhi", "invTauPhiOne", "alpha", "alpha4", "kappa", "gravity", "grav",
+                  "K0", "K1", "K2", "KC0", "KC1", "KC2"]
+STATS_NAMES = ["umax", "vol", "ux_av", "uy_av", "uz_av", "ref", "p_in", "p_out", "p_dif", "p_err",
+               "phi_sum", "rho_sum", "mom_x", "mom_y", "mom_z", "vol_full", "umax_full"]
+
+
+class Oracle:
+    """FP64 periodic-box ZSC step; arrays are (nz, ny, nx) float64."""
+
+    def __init__(self, nx: int, ny: int, nz: int, *, rhoL, rhoH, tauRho, tauPhi, width, sigma, Gamma,
+                 Eo=0.0, rc0=0.0):
+        self.lib = oracle_lib()
+        # the GPU reads these as float32: promote the same float32 values
+        prm = np.array([np.float32(v) for v in (rhoL, rhoH, tauRho, tauPhi, width, sigma, Gamma, Eo, rc0)],
+                       np.float64)
+        self.h = self.lib.zo_create(nx, ny, nz, _dptr(prm))
+        if not self.h:
+            raise MemoryError("zo_create failed")
+        self.shape = (nz, ny, nx)
+        self.nx, self.ny, self.nz = nx, ny, nz
+        self.rhoL, self.rhoH = float(prm[0]), float(prm[1])
+
+    @classmethod
+    def from_params(cls, p) -> "Oracle":
+        return cls(p.nx, p.ny, p.nz, rhoL=p.rhoL, rhoH=p.rhoH, tauRho=p.tauRho, tauPhi=p.tauPhi, width=p.width,
+                   sigma=p.sigma, Gamma=p.Gamma, Eo=p.Eo, rc0=p.rc0)
+
+    def constants(self) -> dict:
+        out = np.zeros(len(CONSTANT_NAMES), np.float64)
+        self.lib.zo_constants(self.h, _dptr(out))
+        return dict(zip(CONSTANT_NAMES, out))
+
+    def bubble_phi(self, bubbles) -> np.ndarray:
+        """phi with ghost planes, shape (nz + 2, ny, nx): plane k = reference z."""
+        b = np.ascontiguousarray(bubbles, np.float32).reshape(-1, 4)
+        out = np.empty((self.nz + 2, self.ny, self.nx), np.float64)
+        self.lib.zo_bubble_phi(self.h, _fptr(b) if len(b) else None, len(b), _dptr(out))
+        return out
+
+    def init(self, phi, rho, ux=None, uy=None, uz=None, ghost=None) -> None:
+        z = np.zeros(self.shape, np.float64)
+        arrs = [np.ascontiguousarray(a if a is not None else z, np.float64) for a in (phi, rho, ux, uy, uz)]
+        g = None if ghost is None else np.ascontiguousarray(ghost, np.float64)
+        self.lib.zo_init(self.h, *[_dptr(a) for a in arrs], _dptr(g))
+
+    def init_bubbles(self, bubbles) -> None:
+        """src/init.c + init_f/init_g: phi from bubbles (ghost planes from the
+        geometry, src/init.c:41-59), rho = (rhoH + rhoL) / 2, u = 0."""
+        pg = self.bubble_phi(bubbles)
+        rho = np.full(self.shape, 0.5 * (self.rhoH + self.rhoL), np.float64)
+        self.init(pg[1:-1], rho, ghost=np.stack([pg[0], pg[-1]]))
+
+    def step(self, n: int, grav: float = 0.0) -> None:
+        self.lib.zo_step(self.h, int(n), float(grav))
+
+    def moments(self) -> dict:
+        arrs = [np.empty(self.shape, np.float64) for _ in range(5)]
+        self.lib.zo_moments(self.h, *[_dptr(a) for a in arrs])
+        return dict(zip(("phi", "rho", "ux", "uy", "uz"), arrs))
+
+    def dist(self):
+        f = np.empty((7,) + self.shape, np.float64)
+        g = np.empty((19,) + self.shape, np.float64)
+        self.lib.zo_dist(self.h, _dptr(f), _dptr(g))
+        return f, g
+
+    def set_dist(self, f, g) -> None:
+        self.lib.zo_set_dist(self.h, _dptr(np.ascontiguousarray(f, np.float64)),
+                             _dptr(np.ascontiguousarray(g, np.float64)))
+
+    def stats(self) -> dict:
+        out = np.zeros(17, np.float64)
+        self.lib.zo_stats(self.h, _dptr(out))
+        return dict(zip(STATS_NAMES, out))
+
+    @property
+    def steps(self) -> int:
+        return int(self.lib.zo_steps(self.h))
+
+    @staticmethod
+    def threads() -> int:
+        return int(oracle_lib().zo_threads())
+
+    def close(self) -> None:
+        if self.h:
+            self.lib.zo_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def oracle_from_inputs(p, bubbles=None) -> Oracle:
+    """Oracle for library Params p, initialised from bubbles like lbm_init_bubbles."""
+    o = Oracle.from_params(p)
+    if bubbles is not None:
+        o.init_bubbles(bubbles)
+    return o
+
+
+def ref_lib() -> C.CDLL | None:
+    """The reference's kernels on the CPU, or None when the sources are unavailable."""
+    global _ref_lib
+    if _ref_lib is None:
+        path = _build.build_reference()
+        if path is None:
+            return None
+        lib = C.CDLL(str(path))
+        lib.zr_init.argtypes = [C.c_char_p, _Fp]
+        lib.zr_step.argtypes = [C.c_int, C.c_float]
+        lib.zr_fields.argtypes = [_Fp] * 5
+        lib.zr_dist.argtypes = [_Fp, _Fp]
+        lib.zr_dims.argtypes = [C.POINTER(C.c_int)]
+        lib.zr_consts.argtypes = [_Fp]
+        lib.zr_write_stats.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int]
+        lib.zr_threads.restype = C.c_int
+        _ref_lib = lib
+    return _ref_lib
+
+
+REF_CONSTANT_NAMES = ["phiStar", "phiStarSq", "invTauRhoOne", "eta", "eta2", "invEta2", "invTauPhi",
+                      "invTauPhiOne", "alpha", "alpha4", "kappa", "gravity", "grav", "K0", "K1", "K2",
+                      "KC0", "KC1", "KC2"]
+
+
+class RefCPU:
+    """The reference's own step (FP32, its nine kernels and three halo
+    exchanges) run on the CPU.  One instance at a time (the reference keeps
+    its state in globals)."""
+
+    def __init__(self, directory: str | os.PathLike, phi_override: np.ndarray | None = None):
+        self.lib = ref_lib()
+        if self.lib is None:
+            raise FileNotFoundError("reference sources not available")
+        po = None if phi_override is None else np.ascontiguousarray(phi_override, np.float32)
+        rc = self.lib.zr_init(str(directory).encode(), _fptr(po))
+        if rc != 0:
+            raise RuntimeError(f"zr_init failed with {rc}")
+        d = (C.c_int * 11)()
+        self.lib.zr_dims(d)
+        self.nx, self.ny, self.nz = d[0], d[1], d[2]
+        self.nbubbles, self.max_step, self.relax_step = d[4], d[5], d[6]
+        self.shape = (self.nz, self.ny, self.nx)
+
+    def constants(self) -> dict:
+        out = np.zeros(len(REF_CONSTANT_NAMES), np.float32)
+        self.lib.zr_consts(_fptr(out))
+        return dict(zip(REF_CONSTANT_NAMES, out))
+
+    def step(self, n: int, grav: float = 0.0) -> None:
+        rc = self.lib.zr_step(int(n), float(grav))
+        if rc != 0:
+            raise RuntimeError(f"zr_step failed with {rc}")
+
+    def fields(self) -> dict:
+        arrs = [np.empty(self.shape, np.float32) for _ in range(5)]
+        self.lib.zr_fields(*[_fptr(a) for a in arrs])
+        return dict(zip(("phi", "rho", "ux", "uy", "uz"), arrs))
+
+    def dist(self):
+        f = np.empty((7,) + self.shape, np.float32)
+        g = np.empty((19,) + self.shape, np.float32)
+        self.lib.zr_dist(_fptr(f), _fptr(g))
+        return f, g
+
+    def write_stats(self, directory, relax: int, step_no: int, with_log: bool = False) -> None:
+        rc = self.lib.zr_write_stats(str(directory).encode(), relax, step_no, int(with_log))
+        if rc != 0:
+            raise RuntimeError(f"zr_write_stats failed with {rc}")
+
+    @staticmethod
+    def threads() -> int:
+        lib = ref_lib()
+        return int(lib.zr_threads()) if lib else 0

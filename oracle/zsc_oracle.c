@@ -1,0 +1,517 @@
+/*
+ * zsc_oracle.c -- FP64 CPU oracle for the Zheng-Shu-Chew (ZSC) free-energy
+ * multiphase lattice Boltzmann step (D3Q7 order parameter f + D3Q19 momentum g).
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the checker: the parity tests, the
+ * smoke check and the CPU-baseline leg of bench.py call it; the product path
+ * (liblbm_gb300.so) never links or calls it.
+ *
+ * It restates, in double precision and on a fully periodic box, the update that
+ * carlosrosales/lbm_bench_gpu performs with nine kernels and three host-staged
+ * halo exchanges per step.  Every function cites the reference lines it follows
+ * (paths relative to the reference project root).  Naming follows the
+ * reference: f = D3Q7 order-parameter distribution (relaxed with tauPhi),
+ * g = D3Q19 momentum distribution (relaxed with tauRho), rho = ZSC mean
+ * density n.
+ *
+ * Layout: idx = x + nx*(y + ny*z), x fastest, z in [0, nz).  The reference
+ * stores the same interior node at plane k = z + 1 between two ghost planes
+ * (src/vgrid.c:38-52 with one rank: zl = 1, zu = zmax, NZ = zmax + 2).  With one
+ * rank the three halo exchanges (src/mpiupdate*.c:34-41 with top = bot = self)
+ * are exactly periodic wrap in z, which is what this file does with index
+ * arithmetic.  The only place the ghost planes are not periodic copies is the
+ * initial equilibrium (src/init.c:39-59 fills them from the bubble geometry and
+ * src/init_f.cu, src/init_g.cu read them through the Laplacian); zo_init takes
+ * those two planes as an optional argument.
+ *
+ * Build: cc -O2 -fopenmp -fPIC -shared zsc_oracle.c -o libzsc_oracle.so -lm
+ */
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#include <stdint.h>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* Lattice weights and forcing weights, src/constants.h:52-59. */
+#define ZO_W0 (1.0 / 3.0)
+#define ZO_W1 (1.0 / 18.0)
+#define ZO_W2 (1.0 / 36.0)
+#define ZO_WC0 1.0
+#define ZO_WC1 (1.0 / 6.0)
+#define ZO_WC2 (1.0 / 12.0)
+
+typedef struct {
+    /* inputs (properties.in values, promoted from float) */
+    double rhoL, rhoH, tauRho, tauPhi, width, sigma, Gamma, Eo, rc0;
+    /* derived, src/paramread.c:141-170 */
+    double phiStar, phiStarSq, invTauRho, invTauRhoOne, invTauRhoHalf;
+    double eta, eta2, invEta2, invTauPhi, invTauPhiOne;
+    double alpha, alpha4, kappa, gravity, grav;
+    double K0, K1, K2, KC0, KC1, KC2;
+} zo_const;
+
+typedef struct zo_ctx {
+    int nx, ny, nz;
+    long n;
+    zo_const c;
+    long steps;
+    double *f[7], *fp[7];     /* streamed / post-collision (reference lower / upper half) */
+    double *g[19], *gp[19];
+    double *phi, *rho, *ux, *uy, *uz;   /* moment arrays as the reference holds them */
+} zo_ctx;
+
+static inline long zo_idx(const zo_ctx *s, int x, int y, int z)
+{
+    return (long)x + (long)s->nx * ((long)y + (long)s->ny * (long)z);
+}
+
+static inline int wrap(int a, int n) { return a < 0 ? a + n : (a >= n ? a - n : a); }
+
+/* Derived constants: src/paramread.c:141-170 (same formulas, in double). */
+static void zo_derive(zo_const *c)
+{
+    c->phiStar = 0.5 * (c->rhoH - c->rhoL);
+    c->phiStarSq = c->phiStar * c->phiStar;
+    c->invTauRho = 1.0 / c->tauRho;
+    c->invTauRhoOne = 1.0 - c->invTauRho;
+    c->invTauRhoHalf = 1.0 - 0.5 * c->invTauRho;
+    c->eta = 1.0 / (c->tauPhi + 0.5);
+    c->eta2 = 1.0 - c->eta;
+    c->invEta2 = 0.5 / (1.0 - c->eta);
+    c->invTauPhi = 1.0 / c->tauPhi;
+    c->invTauPhiOne = 1.0 - c->invTauPhi;
+    c->alpha = 0.75 * c->sigma / (c->width * c->phiStarSq * c->phiStarSq);
+    c->alpha4 = 4.0 * c->alpha;
+    c->kappa = (c->width * c->phiStar) * (c->width * c->phiStar) * c->alpha * 0.5;
+    c->gravity = 0.25 * c->Eo * c->sigma / ((c->rhoH - c->rhoL) * c->rc0 * c->rc0);
+    c->grav = 2.0 * c->phiStar * c->gravity;
+    c->K0 = c->invTauRho * ZO_W0;
+    c->K1 = c->invTauRho * ZO_W1;
+    c->K2 = c->invTauRho * ZO_W2;
+    c->KC0 = c->invTauRhoHalf * ZO_WC0;
+    c->KC1 = c->invTauRhoHalf * ZO_WC1;
+    c->KC2 = c->invTauRhoHalf * ZO_WC2;
+}
+
+/* prm = {rhoL, rhoH, tauRho, tauPhi, width, sigma, Gamma, Eo, rc0} */
+zo_ctx *zo_create(int nx, int ny, int nz, const double *prm)
+{
+    if (nx < 3 || ny < 3 || nz < 3) return NULL;
+    zo_ctx *s = (zo_ctx *)calloc(1, sizeof(zo_ctx));
+    if (!s) return NULL;
+    s->nx = nx; s->ny = ny; s->nz = nz;
+    s->n = (long)nx * ny * nz;
+    s->c.rhoL = prm[0]; s->c.rhoH = prm[1]; s->c.tauRho = prm[2]; s->c.tauPhi = prm[3];
+    s->c.width = prm[4]; s->c.sigma = prm[5]; s->c.Gamma = prm[6]; s->c.Eo = prm[7];
+    s->c.rc0 = prm[8];
+    zo_derive(&s->c);
+    int ok = 1;
+    for (int i = 0; i < 7; i++) {
+        s->f[i] = (double *)malloc(sizeof(double) * s->n);
+        s->fp[i] = (double *)malloc(sizeof(double) * s->n);
+        ok &= s->f[i] && s->fp[i];
+    }
+    for (int i = 0; i < 19; i++) {
+        s->g[i] = (double *)malloc(sizeof(double) * s->n);
+        s->gp[i] = (double *)malloc(sizeof(double) * s->n);
+        ok &= s->g[i] && s->gp[i];
+    }
+    s->phi = (double *)malloc(sizeof(double) * s->n);
+    s->rho = (double *)malloc(sizeof(double) * s->n);
+    s->ux = (double *)malloc(sizeof(double) * s->n);
+    s->uy = (double *)malloc(sizeof(double) * s->n);
+    s->uz = (double *)malloc(sizeof(double) * s->n);
+    ok &= s->phi && s->rho && s->ux && s->uy && s->uz;
+    if (!ok) {
+        extern void zo_destroy(zo_ctx *);
+        zo_destroy(s);
+        return NULL;
+    }
+    return s;
+}
+
+void zo_destroy(zo_ctx *s)
+{
+    if (!s) return;
+    for (int i = 0; i < 7; i++) { free(s->f[i]); free(s->fp[i]); }
+    for (int i = 0; i < 19; i++) { free(s->g[i]); free(s->gp[i]); }
+    free(s->phi); free(s->rho); free(s->ux); free(s->uy); free(s->uz);
+    free(s);
+}
+
+/* out = {phiStar, phiStarSq, invTauRho, invTauRhoOne, invTauRhoHalf, eta, eta2,
+ *        invEta2, invTauPhi, invTauPhiOne, alpha, alpha4, kappa, gravity, grav,
+ *        K0, K1, K2, KC0, KC1, KC2} */
+void zo_constants(const zo_ctx *s, double *out)
+{
+    const zo_const *c = &s->c;
+    double v[21] = {c->phiStar, c->phiStarSq, c->invTauRho, c->invTauRhoOne, c->invTauRhoHalf,
+                    c->eta, c->eta2, c->invEta2, c->invTauPhi, c->invTauPhiOne,
+                    c->alpha, c->alpha4, c->kappa, c->gravity, c->grav,
+                    c->K0, c->K1, c->K2, c->KC0, c->KC1, c->KC2};
+    memcpy(out, v, sizeof(v));
+}
+
+long zo_steps(const zo_ctx *s) { return s->steps; }
+
+/*
+ * Bubble initial condition, src/init.c:39-59: phi = -phiStar everywhere, then
+ * for each bubble in file order, nodes with R <= Rc + width take
+ * phi = phiStar * tanh(2 (Rc - R) / width) (last writer wins, no minimum image).
+ * x, y are 0-based, the reference z coordinate is 1-based; the output holds the
+ * two ghost planes too: plane kk in [0, nz+1] is reference z = kk.
+ * Membership (R <= Rc + width) is decided in float arithmetic, as the reference
+ * does, so that nodes on the shell boundary fall on the same side; the value
+ * is then evaluated in double.
+ */
+void zo_bubble_phi(const zo_ctx *s, const float *bubbles, int nb, double *phi_g)
+{
+    const int nx = s->nx, ny = s->ny, nzg = s->nz + 2;
+    const double phiStar = s->c.phiStar, width = s->c.width;
+    const float widthf = (float)width;
+#pragma omp parallel for schedule(static)
+    for (int kk = 0; kk < nzg; kk++) {
+        for (int j = 0; j < ny; j++) {
+            for (int i = 0; i < nx; i++) {
+                double v = -phiStar;
+                for (int m = 0; m < nb; m++) {
+                    const float xc = bubbles[4 * m + 0], yc = bubbles[4 * m + 1];
+                    const float zc = bubbles[4 * m + 2], rc = bubbles[4 * m + 3];
+                    volatile float dxf = (float)i - xc;
+                    volatile float dyf = (float)j - yc;
+                    volatile float dzf = (float)kk - zc;
+                    volatile float sx = dxf * dxf, sy = dyf * dyf, sz = dzf * dzf;
+                    volatile float ssum = sx + sy;
+                    ssum = ssum + sz;
+                    const float Rf = sqrtf(ssum);
+                    if (Rf <= rc + widthf) {
+                        const double dx = (double)i - xc, dy = (double)j - yc, dz = (double)kk - zc;
+                        const double R = sqrt(dx * dx + dy * dy + dz * dz);
+                        v = phiStar * tanh(2.0 * ((double)rc - R) / width);
+                    }
+                }
+                phi_g[(long)i + (long)nx * ((long)j + (long)ny * kk)] = v;
+            }
+        }
+    }
+}
+
+/* phi at (x, y, z) with periodic x, y and, in z, either periodic wrap or the
+ * supplied ghost planes (ghost[0..nx*ny) = plane below z = 0, ghost[nx*ny..) =
+ * plane above z = nz-1). */
+static inline double phi_at(const zo_ctx *s, const double *phi, const double *ghost, int x, int y, int z)
+{
+    x = wrap(x, s->nx);
+    y = wrap(y, s->ny);
+    if (z < 0 || z >= s->nz) {
+        if (ghost) {
+            const long p = (long)x + (long)s->nx * y;
+            return z < 0 ? ghost[p] : ghost[(long)s->nx * s->ny + p];
+        }
+        z = wrap(z, s->nz);
+    }
+    return phi[zo_idx(s, x, y, z)];
+}
+
+/* The 19-point isotropic stencil of the reference: Laplacian
+ * (src/collision_f.cu:61-70) and gradient (src/collision_f.cu:78-94). */
+static inline void stencil(const zo_ctx *s, const double *phi, const double *ghost, int x, int y, int z,
+                           double *lap, double *gx, double *gy, double *gz)
+{
+#define P(dx, dy, dz) phi_at(s, phi, ghost, x + (dx), y + (dy), z + (dz))
+    const double c = P(0, 0, 0);
+    const double e = P(1, 0, 0), w = P(-1, 0, 0), n = P(0, 1, 0), so = P(0, -1, 0);
+    const double t = P(0, 0, 1), b = P(0, 0, -1);
+    const double en = P(1, 1, 0), ws = P(-1, -1, 0), es = P(1, -1, 0), wn = P(-1, 1, 0);
+    const double et = P(1, 0, 1), wb = P(-1, 0, -1), eb = P(1, 0, -1), wt = P(-1, 0, 1);
+    const double nt = P(0, 1, 1), sb = P(0, -1, -1), nb = P(0, 1, -1), st = P(0, -1, 1);
+#undef P
+    *lap = (en + ws + es + wn + et + wb + eb + wt + nt + sb + nb + st
+            + 2.0 * (e + w + n + so + t + b - 12.0 * c)) / 6.0;
+    *gx = (2.0 * (e - w) + en - ws + es - wn + et - wb + eb - wt) / 12.0;
+    *gy = (2.0 * (n - so) + en - ws + wn - es + nt - sb + nb - st) / 12.0;
+    *gz = (2.0 * (t - b) + et - wb + wt - eb + nt - sb + st - nb) / 12.0;
+}
+
+/*
+ * Initial equilibrium at rest: src/init_f.cu:42-79 and src/init_g.cu:46-93.
+ * Also fills the moment arrays with the given fields (src/main.cu copies the
+ * host phi, rho, ux, uy, uz to the device before init_f/init_g).  The initial
+ * velocity does not enter the distributions (both kernels build the at-rest
+ * equilibrium).  ghost: NULL for periodic z, else the two planes (see phi_at).
+ */
+void zo_init(zo_ctx *s, const double *phi, const double *rho, const double *ux, const double *uy,
+             const double *uz, const double *ghost)
+{
+    const zo_const *c = &s->c;
+    memcpy(s->phi, phi, sizeof(double) * s->n);
+    memcpy(s->rho, rho, sizeof(double) * s->n);
+    memcpy(s->ux, ux, sizeof(double) * s->n);
+    memcpy(s->uy, uy, sizeof(double) * s->n);
+    memcpy(s->uz, uz, sizeof(double) * s->n);
+#pragma omp parallel for schedule(static)
+    for (int z = 0; z < s->nz; z++) {
+        for (int y = 0; y < s->ny; y++) {
+            for (int x = 0; x < s->nx; x++) {
+                const long id = zo_idx(s, x, y, z);
+                double lap, gx, gy, gz;
+                stencil(s, s->phi, ghost, x, y, z, &lap, &gx, &gy, &gz);
+                const double ph = s->phi[id], rh = s->rho[id];
+                const double mu = c->alpha4 * ph * (ph * ph - c->phiStarSq) - c->kappa * lap;
+                const double Af = 0.5 * c->Gamma * mu;
+                s->f[0][id] = ph - 3.0 * c->Gamma * mu;
+                for (int i = 1; i < 7; i++) s->f[i][id] = Af;
+                const double Ag1 = ZO_W1 * (3.0 * ph * mu + rh);
+                const double Ag2 = ZO_W2 * (3.0 * ph * mu + rh);
+                s->g[0][id] = ZO_W0 * (rh - 6.0 * ph * mu);
+                for (int i = 1; i < 7; i++) s->g[i][id] = Ag1;
+                for (int i = 7; i < 19; i++) s->g[i][id] = Ag2;
+            }
+        }
+    }
+    s->steps = 0;
+}
+
+/* update_phi, update_rho, update_velocity: src/update_phi.cu:40-44,
+ * src/update_rho.cu:44-51, src/update_velocity.cu:45-61. */
+static void zo_moments_update(zo_ctx *s)
+{
+    double **f = s->f, **g = s->g;
+#pragma omp parallel for schedule(static)
+    for (long id = 0; id < s->n; id++) {
+        s->phi[id] = f[0][id] + f[1][id] + f[2][id] + f[3][id] + f[4][id] + f[5][id] + f[6][id];
+        double r = 0.0;
+        for (int i = 0; i < 19; i++) r += g[i][id];
+        s->rho[id] = r;
+        const double inv = 1.0 / r;
+        s->ux[id] = (g[1][id] - g[2][id] + g[7][id] - g[8][id] + g[9][id] - g[10][id]
+                     + g[11][id] - g[12][id] + g[13][id] - g[14][id]) * inv;
+        s->uy[id] = (g[3][id] - g[4][id] + g[7][id] - g[8][id] - g[9][id] + g[10][id]
+                     + g[15][id] - g[16][id] + g[17][id] - g[18][id]) * inv;
+        s->uz[id] = (g[5][id] - g[6][id] + g[11][id] - g[12][id] - g[13][id] + g[14][id]
+                     + g[15][id] - g[16][id] - g[17][id] + g[18][id]) * inv;
+    }
+}
+
+/* collision_f (src/collision_f.cu:44-116) and collision_g
+ * (src/collision_g.cu:49-196), both on every node, into fp / gp. */
+static void zo_collide(zo_ctx *s, double grav)
+{
+    const zo_const *c = &s->c;
+#pragma omp parallel for schedule(static)
+    for (int z = 0; z < s->nz; z++) {
+        for (int y = 0; y < s->ny; y++) {
+            for (int x = 0; x < s->nx; x++) {
+                const long id = zo_idx(s, x, y, z);
+                double lap, gx, gy, gz;
+                stencil(s, s->phi, NULL, x, y, z, &lap, &gx, &gy, &gz);
+                const double ph = s->phi[id], rh = s->rho[id];
+                const double mu = c->alpha4 * ph * (ph * ph - c->phiStarSq) - c->kappa * lap;
+                const double Fx = mu * gx, Fy = mu * gy;
+                double Fz = mu * gz;
+                if (ph > 0.0) Fz += grav;
+                const double ux = s->ux[id] + 0.5 * Fx / rh;
+                const double uy = s->uy[id] + 0.5 * Fy / rh;
+                const double uz = s->uz[id] + 0.5 * Fz / rh;
+
+                /* D3Q7, order parameter */
+                const double Af = 0.5 * c->Gamma * c->invTauPhi * mu;
+                const double Cf = c->invTauPhi * c->invEta2 * ph;
+                const double a = c->invTauPhiOne;
+                s->fp[0][id] = a * s->f[0][id] - 6.0 * Af + c->invTauPhi * ph;
+                s->fp[1][id] = a * s->f[1][id] + Af + Cf * ux;
+                s->fp[2][id] = a * s->f[2][id] + Af - Cf * ux;
+                s->fp[3][id] = a * s->f[3][id] + Af + Cf * uy;
+                s->fp[4][id] = a * s->f[4][id] + Af - Cf * uy;
+                s->fp[5][id] = a * s->f[5][id] + Af + Cf * uz;
+                s->fp[6][id] = a * s->f[6][id] + Af - Cf * uz;
+
+                /* D3Q19, momentum with forcing */
+                const double b = c->invTauRhoOne;
+                const double UF = ux * Fx + uy * Fy + uz * Fz;
+                const double usq = ux * ux + uy * uy + uz * uz;
+                const double temp1 = c->K1 * (3.0 * ph * mu + rh * (1.0 - 1.5 * usq));
+                const double vx = 3.0 * ux, vy = 3.0 * uy, vz = 3.0 * uz;
+                const double vsq = vx * vx + vy * vy + vz * vz;
+                double **g = s->g, **gp = s->gp;
+                gp[0][id] = b * g[0][id] + c->K0 * (rh - 6.0 * ph * mu - rh * vsq / 6.0) - c->KC0 * UF;
+                {
+                    const double va[3] = {vx, vy, vz}, Fa[3] = {Fx, Fy, Fz};
+                    for (int d = 0; d < 3; d++) {
+                        const double eq1 = temp1 + c->K1 * rh * va[d] * va[d] * 0.5 + c->KC1 * (va[d] * Fa[d] - UF);
+                        const double eq2 = va[d] * (c->K1 * rh + c->KC1 * Fa[d]);
+                        gp[1 + 2 * d][id] = b * g[1 + 2 * d][id] + eq1 + eq2;
+                        gp[2 + 2 * d][id] = b * g[2 + 2 * d][id] + eq1 - eq2;
+                    }
+                }
+                {
+                    const double temp2 = c->K2 * (3.0 * ph * mu + rh * (1.0 - vsq / 6.0));
+                    /* pairs (7,8) x+y, (9,10) x-y, (11,12) x+z, (13,14) x-z, (15,16) y+z, (17,18) y-z */
+                    const double wv[6] = {vx + vy, vx - vy, vx + vz, vx - vz, vy + vz, vy - vz};
+                    const double wF[6] = {Fx + Fy, Fx - Fy, Fx + Fz, Fx - Fz, Fy + Fz, Fy - Fz};
+                    for (int p = 0; p < 6; p++) {
+                        const double eq1 = temp2 + c->K2 * rh * wv[p] * 0.5 * wv[p] + c->KC2 * (wv[p] * wF[p] - UF);
+                        const double eq2 = c->K2 * rh * wv[p] + c->KC2 * wF[p];
+                        gp[7 + 2 * p][id] = b * g[7 + 2 * p][id] + eq1 + eq2;
+                        gp[8 + 2 * p][id] = b * g[8 + 2 * p][id] + eq1 - eq2;
+                    }
+                }
+            }
+        }
+    }
+}
+
+/* D3Q7 and D3Q19 lattice vectors in the reference order
+ * (src/stream_f.cu:52-59, src/stream_g.cu:56-76). */
+static const int CF[7][3] = {{0, 0, 0}, {1, 0, 0}, {-1, 0, 0}, {0, 1, 0}, {0, -1, 0}, {0, 0, 1}, {0, 0, -1}};
+static const int CG[19][3] = {{0, 0, 0},  {1, 0, 0},  {-1, 0, 0}, {0, 1, 0},  {0, -1, 0}, {0, 0, 1},  {0, 0, -1},
+                              {1, 1, 0},  {-1, -1, 0}, {1, -1, 0}, {-1, 1, 0}, {1, 0, 1},  {-1, 0, -1}, {1, 0, -1},
+                              {-1, 0, 1}, {0, 1, 1},  {0, -1, -1}, {0, 1, -1}, {0, -1, 1}};
+
+/* stream_f (src/stream_f.cu:52-59): ZSC eta-interpolated push,
+ * f_i(x + c_i) = eta * P_i(x) + (1 - eta) * P_i(x + c_i), f_0(x) = P_0(x).
+ * stream_g (src/stream_g.cu:122-142): g_i(x + c_i) = P_i(x).
+ * Periodic wrap replaces the ghost exchanges (src/pack_mpi_f.cu, src/pack_mpi.cu
+ * and their unpack twins with one rank). */
+static void zo_stream(zo_ctx *s)
+{
+    const double eta = s->c.eta, eta2 = s->c.eta2;
+#pragma omp parallel for schedule(static)
+    for (int z = 0; z < s->nz; z++) {
+        for (int y = 0; y < s->ny; y++) {
+            for (int x = 0; x < s->nx; x++) {
+                const long id = zo_idx(s, x, y, z);
+                s->f[0][id] = s->fp[0][id];
+                for (int i = 1; i < 7; i++) {
+                    const long d = zo_idx(s, wrap(x + CF[i][0], s->nx), wrap(y + CF[i][1], s->ny),
+                                          wrap(z + CF[i][2], s->nz));
+                    s->f[i][d] = eta * s->fp[i][id] + eta2 * s->fp[i][d];
+                }
+                s->g[0][id] = s->gp[0][id];
+                for (int i = 1; i < 19; i++) {
+                    const long d = zo_idx(s, wrap(x + CG[i][0], s->nx), wrap(y + CG[i][1], s->ny),
+                                          wrap(z + CG[i][2], s->nz));
+                    s->g[i][d] = s->gp[i][id];
+                }
+            }
+        }
+    }
+}
+
+/* One or more steps in the order of src/main.cu:283-373 (relaxation loop) and
+ * src/main.cu:416-507 (evolution loop); grav is grav_d (0 while relaxing). */
+void zo_step(zo_ctx *s, int nsteps, double grav)
+{
+    for (int t = 0; t < nsteps; t++) {
+        zo_moments_update(s);
+        zo_collide(s, grav);
+        zo_stream(s);
+        s->steps++;
+    }
+}
+
+void zo_moments(const zo_ctx *s, double *phi, double *rho, double *ux, double *uy, double *uz)
+{
+    if (phi) memcpy(phi, s->phi, sizeof(double) * s->n);
+    if (rho) memcpy(rho, s->rho, sizeof(double) * s->n);
+    if (ux) memcpy(ux, s->ux, sizeof(double) * s->n);
+    if (uy) memcpy(uy, s->uy, sizeof(double) * s->n);
+    if (uz) memcpy(uz, s->uz, sizeof(double) * s->n);
+}
+
+/* Streamed distributions after the last step (reference lower halves). */
+void zo_dist(const zo_ctx *s, double *f, double *g)
+{
+    for (int i = 0; i < 7; i++) if (f) memcpy(f + (long)i * s->n, s->f[i], sizeof(double) * s->n);
+    for (int i = 0; i < 19; i++) if (g) memcpy(g + (long)i * s->n, s->g[i], sizeof(double) * s->n);
+}
+
+/* Overwrite the streamed distributions (resume from a snapshot). */
+void zo_set_dist(zo_ctx *s, const double *f, const double *g)
+{
+    for (int i = 0; i < 7; i++) memcpy(s->f[i], f + (long)i * s->n, sizeof(double) * s->n);
+    for (int i = 0; i < 19; i++) memcpy(s->g[i], g + (long)i * s->n, sizeof(double) * s->n);
+}
+
+/*
+ * Statistics over the moment arrays.
+ *  compat (reference region: x in [1, nx-2], y in [1, ny-2], all z;
+ *  src/stats.c:39-55, src/logsave.c:63-147):
+ *   out[0] umax = sqrt(max |u|^2)       out[1] vol = #(phi >= 0)
+ *   out[2..4] mean u over phi >= 0      out[5] Ref = (0.75 vol / pi)^(1/3)
+ *   out[6] Pin  out[7] Pout  out[8] Pin - Pout  out[9] Laplace error
+ *   (src/logsave.c:135-162; Pout divides by nx*ny*nz - vol as the reference does)
+ *  full domain:
+ *   out[10] sum phi  out[11] sum rho  out[12..14] sum rho*u
+ *   out[15] #(phi >= 0)  out[16] sqrt(max |u|^2)
+ */
+void zo_stats(const zo_ctx *s, double *out)
+{
+    const zo_const *c = &s->c;
+    double umax2 = 0, vol = 0, sux = 0, suy = 0, suz = 0, pin = 0, pout = 0;
+    double sphi = 0, srho = 0, mx = 0, my = 0, mz = 0, hv = 0, umax2f = 0;
+#pragma omp parallel for schedule(static) reduction(max : umax2, umax2f) \
+    reduction(+ : vol, sux, suy, suz, pin, pout, sphi, srho, mx, my, mz, hv)
+    for (int z = 0; z < s->nz; z++) {
+        for (int y = 0; y < s->ny; y++) {
+            for (int x = 0; x < s->nx; x++) {
+                const long id = zo_idx(s, x, y, z);
+                const double ph = s->phi[id], rh = s->rho[id];
+                const double u2 = s->ux[id] * s->ux[id] + s->uy[id] * s->uy[id] + s->uz[id] * s->uz[id];
+                sphi += ph;
+                srho += rh;
+                mx += rh * s->ux[id];
+                my += rh * s->uy[id];
+                mz += rh * s->uz[id];
+                if (ph >= 0.0) hv += 1.0;
+                if (u2 > umax2f) umax2f = u2;
+                if (x < 1 || x > s->nx - 2 || y < 1 || y > s->ny - 2) continue;
+                if (u2 > umax2) umax2 = u2;
+                double lap, gx, gy, gz;
+                stencil(s, s->phi, NULL, x, y, z, &lap, &gx, &gy, &gz);
+                const double ph2 = ph * ph;
+                const double p = c->alpha * (ph2 * (3.0 * ph2 - 2.0 * c->phiStarSq) - c->phiStarSq * c->phiStarSq)
+                                 - c->kappa * (ph * lap - 0.5 * (gx * gx + gy * gy + gz * gz)) + rh / 3.0;
+                if (ph >= 0.0) {
+                    vol += 1.0;
+                    sux += s->ux[id];
+                    suy += s->uy[id];
+                    suz += s->uz[id];
+                    pin += p;
+                } else {
+                    pout += p;
+                }
+            }
+        }
+    }
+    const double volOut = (double)s->nx * s->ny * s->nz - vol;
+    out[0] = sqrt(umax2);
+    out[1] = vol;
+    out[2] = vol > 0 ? sux / vol : 0.0;
+    out[3] = vol > 0 ? suy / vol : 0.0;
+    out[4] = vol > 0 ? suz / vol : 0.0;
+    out[5] = pow(vol * 0.75 / M_PI, 1.0 / 3.0);
+    out[6] = vol > 0 ? pin / vol : 0.0;
+    out[7] = volOut > 0 ? pout / volOut : 0.0;
+    out[8] = out[6] - out[7];
+    out[9] = c->rc0 > 0.0 ? 0.5 * (2.0 * c->sigma / c->rc0 - out[8]) * c->rc0 / c->sigma : 0.0;
+    out[10] = sphi;
+    out[11] = srho;
+    out[12] = mx;
+    out[13] = my;
+    out[14] = mz;
+    out[15] = hv;
+    out[16] = sqrt(umax2f);
+}
+
+int zo_threads(void)
+{
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}

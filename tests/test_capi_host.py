@@ -1,0 +1,142 @@
+"""Host-side checks of liblbm_gb300.so that need no GPU: the library loads and
+exports every entry point of include/lbm_gb300.h, parses the reference's input
+format like src/paramread.c, derives the same constants, and rejects bad input
+with a status code before touching the device."""
+from __future__ import annotations
+
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+HEADER = ROOT / "include" / "lbm_gb300.h"
+
+
+def declared_functions() -> list[str]:
+    text = HEADER.read_text()
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?[\w\s\*]+?\b(lbm_\w+)\s*\(", text, re.M)))
+
+
+def test_header_declares_core_entry_points():
+    names = declared_functions()
+    for n in ("lbm_init", "lbm_step", "lbm_stats", "lbm_destroy", "lbm_strerror", "lbm_read_inputs"):
+        assert n in names
+
+
+def test_library_exports_every_declared_symbol(lib):
+    for name in declared_functions():
+        assert hasattr(lib, name), f"{name} declared in lbm_gb300.h but not exported"
+    from lbm_bench_gpu_gb300 import capi
+    assert set(capi.EXPORTS) == set(declared_functions())
+
+
+def test_read_inputs_matches_reference_parser(golden_manifest, tmp_path):
+    from lbm_bench_gpu_gb300 import capi
+    case = golden_manifest["sample_ratio"]
+    (tmp_path / "properties.in").write_text(case["properties.in"])
+    (tmp_path / "discrete.in").write_text(case["discrete.in"])
+    p, run, bub = capi.read_inputs(tmp_path)
+    assert (p.nx, p.ny, p.nz, p.block_x, p.block_y) == (64, 32, 16, 32, 8)
+    assert (p.rhoL, p.rhoH, p.tauRho) == (1.0, 1000.0, 1.0)
+    assert p.tauPhi == np.float32(0.7) and p.sigma == np.float32(0.01) and p.Gamma == 400.0 and p.Eo == 10.0
+    assert bub.shape == (1, 4) and p.rc0 == 5.0
+    d = capi.derive(p)
+    for k, v in case["ref_constants"].items():
+        mine = getattr(d, {"Wn0": "K0"}.get(k, k))
+        assert mine == pytest.approx(v, rel=5e-7, abs=1e-30), k
+
+
+def test_read_inputs_reference_sample():
+    """The reference's own Input/ directory, where the checkout is present."""
+    src = Path("/root/reference/Input")
+    if not (src / "properties.in").exists():
+        pytest.skip("reference checkout not present")
+    from lbm_bench_gpu_gb300 import capi
+    p, run, bub = capi.read_inputs(src)
+    assert (run.max_step, run.relax_step, run.save, run.stat) == (1000, 1000, 2000, 100)
+    assert (p.nx, p.ny, p.nz) == (128, 128, 128)
+    assert p.rhoH == 1000.0 and p.Gamma == 400.0 and p.Eo == 10.0
+    assert bub.tolist() == [[64.0, 64.0, 64.0, 10.0]]
+
+
+def test_missing_and_malformed_inputs(tmp_path):
+    from lbm_bench_gpu_gb300 import capi
+    with pytest.raises(capi.LbmError) as e:
+        capi.read_inputs(tmp_path)
+    assert e.value.code == capi.LBM_EIO
+    (tmp_path / "properties.in").write_text("maxStep relaxStep save stat\n10 0 1 1\nxmax ymax zmax\n32 32\n")
+    (tmp_path / "discrete.in").write_text("nBubbles\n0\nxc yc zc Rc\n")
+    with pytest.raises(capi.LbmError) as e:
+        capi.read_inputs(tmp_path)
+    assert e.value.code == capi.LBM_EIO
+
+
+def test_discrete_with_missing_rows(tmp_path):
+    from lbm_bench_gpu_gb300 import capi, inputs
+    inputs.write_inputs(tmp_path, inputs.Inputs(nx=32, ny=32, nz=32,
+                                                bubbles=np.array([[1, 2, 3, 4]], np.float32)))
+    (tmp_path / "discrete.in").write_text("nBubbles\n3\nxc yc zc Rc\n1 2 3 4\n")
+    with pytest.raises(capi.LbmError) as e:
+        capi.read_inputs(tmp_path)
+    assert e.value.code == capi.LBM_EIO
+
+
+@pytest.mark.parametrize("change,code", [
+    (dict(nx=48), 1),                      # nx not a multiple of 32
+    (dict(ny=12), 1),                      # ny not a multiple of 8
+    (dict(ny=40, compat=True), 1),         # compat: NY % 32 (src/main.cu:168)
+    (dict(block_x=64, block_y=16, compat=True), 1),  # compat: BLOCK_SIZE_X*Y > 512 (src/main.cu:171)
+    (dict(tauRho=0.0), 1),
+    (dict(rhoH=0.1), 1),                   # rhoH == rhoL: phiStar = 0
+    (dict(storage="bf16", nx=32), 1),
+    (dict(nz=2), 1),
+])
+def test_init_rejects_bad_params_without_touching_the_gpu(change, code):
+    from lbm_bench_gpu_gb300 import capi
+    kw = dict(rhoL=0.1, rhoH=1.0, tauRho=0.7, tauPhi=1.0, width=4.0, sigma=1e-3, Gamma=1.0)
+    dims = dict(nx=32, ny=32, nz=32)
+    for k in ("nx", "ny", "nz"):
+        if k in change:
+            dims[k] = change.pop(k)
+    kw.update(change)
+    p = capi.make_params(dims["nx"], dims["ny"], dims["nz"], **kw)
+    phi = np.zeros(p.nx * p.ny * p.nz, np.float32)
+    with pytest.raises(capi.LbmError) as e:
+        capi.Lattice.from_fields(p, phi, phi + 0.55)
+    assert e.value.code == code
+
+
+def test_strerror_covers_codes(lib):
+    from lbm_bench_gpu_gb300 import capi
+    for code in range(8):
+        assert lib.lbm_strerror(code).decode()
+    assert lib.lbm_strerror(99).decode() == "unknown status"
+
+
+def test_null_context_is_rejected(lib):
+    from lbm_bench_gpu_gb300 import capi
+    assert lib.lbm_step(None, 1, C.c_float(0.0)) == capi.LBM_EINVAL
+    assert lib.lbm_sync(None) == capi.LBM_EINVAL
+    assert lib.lbm_steps_done(None) == -1
+    lib.lbm_destroy(None)
+
+
+def test_bubble_placement_rules():
+    from lbm_bench_gpu_gb300 import inputs
+    b = inputs.place_bubbles(64, (256, 256, 256), (6.0, 10.0))
+    assert b.shape == (64, 4)
+    assert np.array_equal(b, inputs.place_bubbles(64, (256, 256, 256), (6.0, 10.0)))  # seeded
+    r = b[:, 3]
+    assert r.min() >= 6.0 and r.max() <= 10.0
+    c = b[:, :3].astype(np.float64)
+    d = np.linalg.norm(c[:, None] - c[None], axis=-1)
+    gap = d - (r[:, None] + r[None])
+    np.fill_diagonal(gap, np.inf)
+    assert gap.min() >= 3.0 - 1e-3
+    m = r + 4.0 + 1.0
+    assert np.all(c[:, 0] >= m) and np.all(c[:, 0] <= 255 - m)
+    assert np.all(c[:, 2] >= 1 + m) and np.all(c[:, 2] <= 256 - m)
