@@ -145,6 +145,41 @@ int lbm_get_dist(lbm_ctx *c, float *f, float *g);
  * their moments.  Synchronises. */
 int lbm_set_dist(lbm_ctx *c, const float *f, const float *g);
 
+/* Largest box lbm_stats_noalloc accepts: 512^3 nodes. */
+#define LBM_NOALLOC_MAX_NODES 134217728LL
+/* Number of doubles lbm_stats_noalloc writes. */
+#define LBM_STATS_RAW_VALUES 16
+
+/* lbm_stats for callers that cannot allocate device memory.  No counterpart
+ * in the reference (its statistics run on host copies of the fields).
+ *
+ * Meant for in-situ analysis and monitoring code that runs inside another
+ * program's time loop: there the device memory belongs to the host
+ * application's own pool allocator, and cudaMalloc / cudaFree are not allowed
+ * (they take memory outside that budget and synchronise the whole device).
+ * The caller passes what it already owns: the five fields on the device
+ * (nx*ny*nz floats each, x fastest; only nx, ny, nz, device and the physical
+ * parameters of p are used) and raw_out, a device buffer of
+ * LBM_STATS_RAW_VALUES doubles.  The call allocates nothing; it queues two
+ * kernels on `stream` (a cudaStream_t, NULL for the legacy default stream)
+ * and returns.  raw_out then receives, in this order:
+ *   0 max |u|^2 and 1 the number of nodes with phi >= 0, over the reference's
+ *   region (planes x = 0, nx-1 and y = 0, ny-1 skipped); 2..4 sum of u over
+ *   those phi >= 0 nodes; 5, 6 sum of the pressure over phi >= 0 / phi < 0
+ *   nodes of that region; 7 sum phi; 8 sum rho; 9..11 sum rho u;
+ *   12 number of nodes with phi >= 0; 13 max |u|^2; 14 number of nodes with a
+ *   non-finite value (full domain for 7..14); 15 zero.
+ * The per-block partial sums use a 1 MiB array in the library's static device
+ * memory, which every GPU that loads the library keeps until the process
+ * exits.  That array bounds the box: more than LBM_NOALLOC_MAX_NODES nodes is
+ * rejected with LBM_EINVAL.  The first call on a device looks up the array's
+ * device address (cudaGetSymbolAddress); make that first call before any
+ * stream capture.  All calls share the array: calls whose kernels can overlap
+ * on the GPU (other streams, other host threads) race and must be ordered by
+ * the caller.  Nothing in the array needs clearing between calls. */
+int lbm_stats_noalloc(const lbm_params *p, const float *phi, const float *rho, const float *ux,
+                      const float *uy, const float *uz, double *raw_out, void *stream);
+
 /* Steps taken since lbm_init. */
 long long lbm_steps_done(const lbm_ctx *c);
 

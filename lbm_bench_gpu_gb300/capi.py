@@ -22,7 +22,7 @@ STORAGE = {"fp32": 0, "fp16": 1, "bf16": 2}
 EXPORTS = [
     "lbm_read_inputs", "lbm_derive", "lbm_init", "lbm_init_bubbles", "lbm_step", "lbm_stats",
     "lbm_get_dist", "lbm_set_dist", "lbm_steps_done", "lbm_stream", "lbm_sync", "lbm_destroy",
-    "lbm_strerror", "lbm_last_error",
+    "lbm_strerror", "lbm_last_error", "lbm_stats_noalloc",
 ]
 
 
@@ -92,6 +92,8 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.lbm_stats.argtypes = [C.c_void_p, C.POINTER(StatsOut), _F, _F, _F, _F, _F]
     lib.lbm_get_dist.argtypes = [C.c_void_p, _F, _F]
     lib.lbm_set_dist.argtypes = [C.c_void_p, _F, _F]
+    lib.lbm_stats_noalloc.argtypes = [C.POINTER(Params), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                      C.c_void_p, C.c_void_p, C.c_void_p]
     lib.lbm_steps_done.argtypes = [C.c_void_p]
     lib.lbm_steps_done.restype = C.c_longlong
     lib.lbm_stream.argtypes = [C.c_void_p]

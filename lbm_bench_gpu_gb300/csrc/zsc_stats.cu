@@ -163,3 +163,112 @@ cudaError_t launch_stats(const Box &b, const lbm_derived &d, const float *mom, d
 }
 
 }  // namespace lbm
+
+// ---------------------------------------------------------------------------
+// lbm_stats_noalloc: the same reduction for callers that must not allocate
+// device memory.
+//
+// Who needs it: code that inspects the fields of a simulation it does not own
+// -- an in-situ analysis or monitoring hook called from inside another
+// program's time loop.  There the device memory usually belongs to the host
+// application's own pool allocator, and cudaMalloc / cudaFree are off limits:
+// they would take memory outside the application's budget and they
+// synchronise the whole device, stalling the work already queued.  Such a
+// caller hands over the five field arrays and a 16-double output buffer it
+// already owns; this entry point adds nothing to them.
+//
+// The per-block partial sums live in a fixed array in the library's static
+// device memory (1 MiB, reserved on every GPU that loads the library until the
+// process exits).  One block reduces 16384 nodes, so the array holds the
+// partials of at most 512^3 nodes; larger boxes are rejected.  Every row the
+// final fold reads is written earlier in the same call, so no part of the
+// array has to be cleared between calls.  All calls share the array: two calls
+// whose kernels overlap on the GPU (different streams, or different host
+// threads on one device) race on it and must be ordered by the caller.
+// ---------------------------------------------------------------------------
+#include <mutex>
+
+namespace lbm {
+namespace {
+
+constexpr int kNoAllocNodesPerBlock = kThreads * 64;
+constexpr long long kNoAllocMaxNodes = LBM_NOALLOC_MAX_NODES;
+constexpr int kNoAllocRows = (int)(kNoAllocMaxNodes / kNoAllocNodesPerBlock);
+static_assert(kNoAllocMaxNodes % kNoAllocNodesPerBlock == 0, "whole rows");
+
+static __device__ __align__(256) double g_noalloc_partials[kNoAllocRows * kStatsValues];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+double *g_noalloc_ptr[kMaxDevices] = {};
+
+// Device address of the scratch array on `device` (which must be current).
+// Looked up on the first call per device; later calls reuse it.
+cudaError_t noalloc_scratch(int device, double **out)
+{
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[device]) {
+        void *p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_partials);
+        if (e != cudaSuccess) return e;
+        g_noalloc_ptr[device] = static_cast<double *>(p);
+    }
+    *out = g_noalloc_ptr[device];
+    return cudaSuccess;
+}
+
+}  // namespace
+}  // namespace lbm
+
+extern "C" int lbm_stats_noalloc(const lbm_params *p, const float *phi, const float *rho, const float *ux,
+                                 const float *uy, const float *uz, double *raw_out, void *stream)
+{
+    if (!p || !phi || !rho || !ux || !uy || !uz || !raw_out) {
+        lbm::set_error("lbm_stats_noalloc: NULL argument");
+        return LBM_EINVAL;
+    }
+    if (p->nx < 3 || p->ny < 3 || p->nz < 3) {
+        lbm::set_error("lbm_stats_noalloc: box must be at least 3 nodes in each direction");
+        return LBM_EINVAL;
+    }
+    const long long n = (long long)p->nx * p->ny * p->nz;
+    if (n > lbm::kNoAllocMaxNodes) {
+        lbm::set_error("lbm_stats_noalloc: box of " + std::to_string(n) +
+                       " nodes exceeds the no-allocation limit of LBM_NOALLOC_MAX_NODES = 512^3 nodes");
+        return LBM_EINVAL;
+    }
+    if (p->device < 0 || p->device >= lbm::kMaxDevices) {
+        lbm::set_error("lbm_stats_noalloc: device ordinal out of range");
+        return LBM_EINVAL;
+    }
+    int prev = 0;
+    cudaError_t e = cudaGetDevice(&prev);
+    if (e == cudaSuccess && prev != p->device) e = cudaSetDevice(p->device);
+    double *scratch = nullptr;
+    if (e == cudaSuccess) e = lbm::noalloc_scratch(p->device, &scratch);
+    if (e == cudaSuccess) {
+        lbm_derived d;
+        lbm::derive(*p, d);
+        lbm::Box b;
+        b.nx = p->nx;
+        b.ny = p->ny;
+        b.nz = p->nz;
+        b.nxy = (long long)p->nx * p->ny;
+        b.n = n;
+        const unsigned blocks = (unsigned)((n + lbm::kNoAllocNodesPerBlock - 1) / lbm::kNoAllocNodesPerBlock);
+        const cudaStream_t s = static_cast<cudaStream_t>(stream);
+        lbm::StatsConst c{d.alpha, d.kappa, d.phiStarSq};
+        lbm::stats_kernel<<<blocks, lbm::kThreads, 0, s>>>(b, c, phi, rho, ux, uy, uz, scratch);
+        e = cudaGetLastError();
+        if (e == cudaSuccess) {
+            lbm::fold_kernel<<<1, lbm::kThreads, 0, s>>>(scratch, (int)blocks, raw_out);
+            e = cudaGetLastError();
+        }
+    }
+    if (prev != p->device) cudaSetDevice(prev);
+    if (e != cudaSuccess) {
+        lbm::set_error(std::string("lbm_stats_noalloc: ") + cudaGetErrorString(e));
+        return LBM_ECUDA;
+    }
+    return LBM_OK;
+}
