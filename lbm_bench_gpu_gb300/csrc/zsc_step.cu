@@ -17,29 +17,79 @@
 //    neighbours' natural slots.  Each thread reads and writes the same 19
 //    locations, so the update is race-free in one buffer.
 //
-// The phi stencil (19-point Laplacian and gradient, src/collision_f.cu:61-94)
-// needs phi on a one-node halo, and phi = sum f needs P^{n-1} one node further
-// out.  Each block owns a TX x TY column tile and marches a chunk of TZ planes
-// in z; phi of the tile plus a one-node ring is rebuilt per plane into a
-// four-plane shared-memory ring buffer, so DRAM sees each distribution once
-// per step (read + write = 26 x 8 B = 208 B per node in FP32) and the halo
-// re-reads are served by L1/L2.
+// Work decomposition: a block owns a TX x TY column tile and marches a chunk
+// of TZ planes in z.  The phi stencil (19-point Laplacian and gradient,
+// src/collision_f.cu:61-94) needs phi on a one-node ring around the tile, and
+// phi = sum f needs P^{n-1} one node further out, so each plane of P^{n-1} is
+// staged in shared memory on the tile plus two halo rows and four halo columns.
+//
+// Memory pipeline: every global read goes through cp.async (16-byte chunks,
+// L2-cached, no registers held while in flight) into shared-memory stages:
+//   - the 19 g rows of the next plane (2 stages; odd steps stage 36-wide rows
+//     so the +-x shifted reads stay 16-byte aligned),
+//   - the 7 P_f planes three planes ahead (4 stages),
+// so a block always has about one plane of the step's input in flight while it
+// computes the current plane.  Periodic wrap is applied per 16-byte chunk: with
+// nx a multiple of 32 no chunk straddles the seam.  DRAM sees each
+// distribution once per step (26 x 8 B = 208 B per node in FP32); the halo
+// re-reads of neighbouring tiles are served by L2.
 #include "lbm_internal.h"
 
 namespace lbm {
 namespace {
 
-constexpr int TX = 32;            // tile width in x (one warp per row)
-constexpr int TY = 8;             // tile height in y
-constexpr int TZ = 32;            // planes per block
-constexpr int NT = TX * TY;       // threads per block
-constexpr int RW = TX + 2;        // phi ring buffer row width (tile + 1 halo)
+#ifndef ZSC_TILE_Y
+#define ZSC_TILE_Y 8
+#endif
+#ifndef ZSC_TILE_Z
+#define ZSC_TILE_Z 32
+#endif
+#ifndef ZSC_MIN_BLOCKS
+#define ZSC_MIN_BLOCKS 2
+#endif
+constexpr int TX = 32;              // tile width in x (one warp per row)
+constexpr int TY = ZSC_TILE_Y;      // tile height in y
+constexpr int TZ = ZSC_TILE_Z;      // planes per block
+constexpr int NT = TX * TY;         // threads per block
+constexpr int GW = 40;              // staged row width: x in [x0 - 4, x0 + 36)
+constexpr int FR = TY + 4;          // staged P_f rows: y in [y0 - 2, y0 + TY + 2)
+constexpr int RW = TX + 2;          // phi ring width (tile + one-node ring)
 constexpr int RH = TY + 2;
-constexpr int RING = 2 * RW + 2 * TY;  // halo nodes around the tile
-static_assert(RING <= NT, "one halo node per thread at most");
+constexpr int RING = 2 * RW + 2 * TY;
+constexpr int NG = 2;               // g stages
+constexpr int NF = 4;               // P_f stages
+constexpr int NPHI = 4;             // phi planes
+constexpr int G_STAGE = kQg * TY * GW;
+constexpr int F_STAGE = kQf * FR * GW;
+constexpr int PHI_STAGE = RH * RW;
+constexpr size_t kSmemBytes = sizeof(float) * (NG * G_STAGE + NF * F_STAGE + NPHI * PHI_STAGE);
+static_assert(RING <= NT, "one ring node per thread at most");
 
 constexpr float kInv6 = 0.16666666666666666667f;
 constexpr float kInv12 = 0.08333333333333333333f;
+
+// D3Q19 lattice vectors and opposite directions (reference order).
+// (compile-time forms for unrolled loops, table forms for runtime indices)
+__host__ __device__ constexpr int kCx(int i)
+{
+    return (i == 1 || i == 7 || i == 9 || i == 11 || i == 13) ? 1
+           : (i == 2 || i == 8 || i == 10 || i == 12 || i == 14) ? -1 : 0;
+}
+__host__ __device__ constexpr int kCy(int i)
+{
+    return (i == 3 || i == 7 || i == 10 || i == 15 || i == 17) ? 1
+           : (i == 4 || i == 8 || i == 9 || i == 16 || i == 18) ? -1 : 0;
+}
+__host__ __device__ constexpr int kCz(int i)
+{
+    return (i == 5 || i == 11 || i == 14 || i == 15 || i == 18) ? 1
+           : (i == 6 || i == 12 || i == 13 || i == 16 || i == 17) ? -1 : 0;
+}
+__host__ __device__ constexpr int kOpp(int i) { return i == 0 ? 0 : ((i & 1) ? i + 1 : i - 1); }
+__constant__ int cCx[kQg] = {0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1, 0, 0, 0, 0};
+__constant__ int cCy[kQg] = {0, 0, 0, 1, -1, 0, 0, 1, -1, -1, 1, 0, 0, 0, 0, 1, -1, 1, -1};
+__constant__ int cCz[kQg] = {0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, -1, -1, 1, 1, -1, -1, 1};
+__constant__ int cOpp[kQg] = {0, 2, 1, 4, 3, 6, 5, 8, 7, 10, 9, 12, 11, 14, 13, 16, 15, 18, 17};
 
 struct StepPtrs {
     const float *fin[kQf];
@@ -72,39 +122,25 @@ __device__ __forceinline__ unsigned node_index(const Box &b, int x, int y, int z
     return (unsigned)x + (unsigned)b.nx * ((unsigned)y + (unsigned)b.ny * (unsigned)z);
 }
 
-__device__ __forceinline__ float ldg(const float *p) { return __ldg(p); }
+__device__ __forceinline__ int wrap(int a, int n) { return a < 0 ? a + n : (a >= n ? a - n : a); }
 
-// Streamed D3Q7 values at node (x, y, z) and their sum phi
-// (src/update_phi.cu:42-43).  STREAMED: f holds streamed values (initial
-// state).  Otherwise f holds P^{n-1} and the ZSC interpolated streaming
-// (src/stream_f.cu:52-59) is applied while reading.
-template <bool STREAMED>
-__device__ __forceinline__ float phi_at(const StepPtrs &P, const Box &b, const StepConst &c, int x, int y, int z,
-                                        float (&f)[kQf])
+// 16-byte global -> shared copy, cached in L2 only; completes asynchronously.
+__device__ __forceinline__ void cp_async16(float *smem, const float *gmem)
 {
-    const unsigned id = node_index(b, x, y, z);
-    if (STREAMED) {
-#pragma unroll
-        for (int i = 0; i < kQf; i++) f[i] = ldg(P.fin[i] + id);
-    } else {
-        const Nbr o = neighbours(b, x, y, z);
-        const float eta = c.eta, eta2 = c.eta2;
-        f[0] = ldg(P.fin[0] + id);
-        f[1] = eta * ldg(P.fin[1] + (id + o.xm)) + eta2 * ldg(P.fin[1] + id);
-        f[2] = eta * ldg(P.fin[2] + (id + o.xp)) + eta2 * ldg(P.fin[2] + id);
-        f[3] = eta * ldg(P.fin[3] + (id + o.ym)) + eta2 * ldg(P.fin[3] + id);
-        f[4] = eta * ldg(P.fin[4] + (id + o.yp)) + eta2 * ldg(P.fin[4] + id);
-        f[5] = eta * ldg(P.fin[5] + (id + o.zm)) + eta2 * ldg(P.fin[5] + id);
-        f[6] = eta * ldg(P.fin[6] + (id + o.zp)) + eta2 * ldg(P.fin[6] + id);
-    }
-    return f[0] + f[1] + f[2] + f[3] + f[4] + f[5] + f[6];
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
 }
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
 template <bool STREAMED, bool ODD>
-__global__ void __launch_bounds__(NT, 2)
+__global__ void __launch_bounds__(NT, ZSC_MIN_BLOCKS)
 zsc_step_kernel(const StepPtrs P, const Box b, const StepConst c, const int write_moments)
 {
-    __shared__ float sphi[4][RH][RW];
+    extern __shared__ __align__(16) float smem[];
+    float *const G = smem;                    // [NG][19][TY][GW]
+    float *const F = G + NG * G_STAGE;        // [NF][7][FR][GW]
+    float *const PHI = F + NF * F_STAGE;      // [NPHI][RH][RW]
 
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int tid = ty * TX + tx;
@@ -115,8 +151,7 @@ zsc_step_kernel(const StepPtrs P, const Box b, const StepConst c, const int writ
     const int by = bid % nty;
     bid /= nty;
     const int z0 = bid * TZ;
-    const int zend = min(z0 + TZ, b.nz);
-
+    const int nzc = min(TZ, b.nz - z0);       // planes of this chunk
     const int x0 = bx * TX, y0 = by * TY;
     const int x = x0 + tx, y = y0 + ty;
 
@@ -137,52 +172,135 @@ zsc_step_kernel(const StepPtrs P, const Box b, const StepConst c, const int writ
         rlx = TX + 1;
         rly = tid - 2 * RW - TY + 1;
     }
-    int rx = x0 + rlx - 1, ry = y0 + rly - 1;
-    rx = rx < 0 ? rx + b.nx : (rx >= b.nx ? rx - b.nx : rx);
-    ry = ry < 0 ? ry + b.ny : (ry >= b.ny ? ry - b.ny : ry);
 
-    auto wrapz = [&](int z) { return z < 0 ? z + b.nz : (z >= b.nz ? z - b.nz : z); };
+    // P_f stage of plane p (p >= z0 - 2)
+    auto fslot = [&](int p) { return F + ((p - z0 + 4) & (NF - 1)) * F_STAGE; };
 
-    float fcur[kQf], fnext[kQf];
-
-    // phi of plane z on the tile + ring into ring-buffer slot s; the streamed
-    // f of the thread's own node is returned in fo.
-    auto build_plane = [&](int z, int s, float (&fo)[kQf]) {
-        sphi[s][ty + 1][tx + 1] = phi_at<STREAMED>(P, b, c, x, y, z, fo);
-        if (has_ring) {
-            float tmp[kQf];
-            sphi[s][rly][rlx] = phi_at<STREAMED>(P, b, c, rx, ry, z, tmp);
+    // Queue the 7 P_f planes of plane p (tile + halo) into its stage.
+    auto issue_f = [&](int p) {
+        const int pw = wrap(p, b.nz);
+        float *dst = fslot(p);
+        constexpr int kChunks = kQf * FR * (GW / 4);
+        for (int ch = tid; ch < kChunks; ch += NT) {
+            const int arr = ch / (FR * (GW / 4));
+            const int rem = ch - arr * (FR * (GW / 4));
+            const int r = rem / (GW / 4), k = rem - r * (GW / 4);
+            const int yy = wrap(y0 - 2 + r, b.ny), xx = wrap(x0 - 4 + 4 * k, b.nx);
+            cp_async16(dst + (arr * FR + r) * GW + 4 * k, P.fin[arr] + node_index(b, xx, yy, pw));
         }
     };
 
+    // Queue the 19 g rows the nodes of plane z read, into g stage s.
+    auto issue_g = [&](int z, int s) {
+        float *dst = G + s * G_STAGE;
+        if (!ODD) {
+            constexpr int kChunks = kQg * TY * (TX / 4);
+            for (int ch = tid; ch < kChunks; ch += NT) {
+                const int i = ch / (TY * (TX / 4));
+                const int r = (ch / (TX / 4)) % TY, k = ch % (TX / 4);
+                cp_async16(dst + (i * TY + r) * GW + 4 + 4 * k, P.g[i] + node_index(b, x0 + 4 * k, y0 + r, z));
+            }
+        } else {
+            // direction i of node x sits in the reversed slot of x - c_i
+            constexpr int kRowChunks = TX / 4 + 1;
+            constexpr int kChunks = kQg * TY * kRowChunks;
+            for (int ch = tid; ch < kChunks; ch += NT) {
+                const int i = ch / (TY * kRowChunks);
+                const int rem = ch - i * (TY * kRowChunks);
+                const int r = rem / kRowChunks, k = rem - r * kRowChunks;
+                const int cx = cCx[i];
+                const int yy = wrap(y0 + r - cCy[i], b.ny), zz = wrap(z - cCz[i], b.nz);
+                const int xs = cx < 0 ? x0 + 4 * k : x0 - 4 + 4 * k;
+                const int col = cx < 0 ? 4 + 4 * k : 4 * k;
+                cp_async16(dst + (i * TY + r) * GW + col, P.g[cOpp[i]] + node_index(b, wrap(xs, b.nx), yy, zz));
+            }
+        }
+    };
+
+    // Streamed D3Q7 values at ring-tile position (lx, ly) of plane p and their
+    // sum phi (src/update_phi.cu:42-43), from the staged planes.
+    auto phi_at = [&](int p, int lx, int ly, float(&f)[kQf]) -> float {
+        const int col = lx + 3, row = ly + 1;
+        const float *S1 = fslot(p);
+        auto at = [&](const float *S, int arr, int rr, int cc) { return S[(arr * FR + rr) * GW + cc]; };
+        if (STREAMED) {
+#pragma unroll
+            for (int i = 0; i < kQf; i++) f[i] = at(S1, i, row, col);
+        } else {
+            const float *S0 = fslot(p - 1), *S2 = fslot(p + 1);
+            const float eta = c.eta, eta2 = c.eta2;
+            f[0] = at(S1, 0, row, col);
+            f[1] = eta * at(S1, 1, row, col - 1) + eta2 * at(S1, 1, row, col);
+            f[2] = eta * at(S1, 2, row, col + 1) + eta2 * at(S1, 2, row, col);
+            f[3] = eta * at(S1, 3, row - 1, col) + eta2 * at(S1, 3, row, col);
+            f[4] = eta * at(S1, 4, row + 1, col) + eta2 * at(S1, 4, row, col);
+            f[5] = eta * at(S0, 5, row, col) + eta2 * at(S1, 5, row, col);
+            f[6] = eta * at(S2, 6, row, col) + eta2 * at(S1, 6, row, col);
+        }
+        return f[0] + f[1] + f[2] + f[3] + f[4] + f[5] + f[6];
+    };
+
+    // phi of plane p on the tile + ring into phi slot s; the streamed f of the
+    // thread's own node is returned in fo.
+    auto build_plane = [&](int p, int s, float(&fo)[kQf]) {
+        float *ph = PHI + s * PHI_STAGE;
+        ph[(ty + 1) * RW + tx + 1] = phi_at(p, tx + 1, ty + 1, fo);
+        if (has_ring) {
+            float tmp[kQf];
+            ph[rly * RW + rlx] = phi_at(p, rlx, rly, tmp);
+        }
+    };
+
+    float fcur[kQf], fnext[kQf];
+
+    // prologue: P_f planes z0-2 .. z0+1, g of plane z0; phi of z0-1 and z0
+    issue_f(z0 - 2);
+    issue_f(z0 - 1);
+    issue_f(z0);
+    issue_f(z0 + 1);
+    issue_g(z0, 0);
+    cp_async_commit();
+    cp_async_wait_all();
+    __syncthreads();
     {
         float tmp[kQf];
-        build_plane(wrapz(z0 - 1), 0, tmp);
+        build_plane(z0 - 1, 0, tmp);
     }
     build_plane(z0, 1, fcur);
+    __syncthreads();
+    issue_f(z0 + 2);
+    cp_async_commit();
 
-    for (int z = z0; z < zend; ++z) {
-        const int j = z - z0;
-        build_plane(wrapz(z + 1), (j + 2) & 3, fnext);
+    for (int j = 0; j < nzc; ++j) {
+        const int z = z0 + j;
+        cp_async_wait_all();
+        __syncthreads();
+        if (j + 1 < nzc) {
+            issue_g(z + 1, (j + 1) & 1);
+            issue_f(z + 3);
+        }
+        cp_async_commit();
+        build_plane(z + 1, (j + 2) & 3, fnext);
         __syncthreads();
 
-        const float(*S0)[RW] = sphi[j & 3];        // plane z - 1
-        const float(*S1)[RW] = sphi[(j + 1) & 3];  // plane z
-        const float(*S2)[RW] = sphi[(j + 2) & 3];  // plane z + 1
+        const float *S0 = PHI + (j & 3) * PHI_STAGE;        // plane z - 1
+        const float *S1 = PHI + ((j + 1) & 3) * PHI_STAGE;  // plane z
+        const float *S2 = PHI + ((j + 2) & 3) * PHI_STAGE;  // plane z + 1
         const int lx = tx + 1, ly = ty + 1;
+        auto at = [&](const float *S, int yy, int xx) { return S[yy * RW + xx]; };
 
         // 19-point stencil, src/collision_f.cu:61-94 (e/w = x+-1, n/s = y+-1,
         // t/b = z+-1)
-        const float pc = S1[ly][lx];
-        const float pe = S1[ly][lx + 1], pw = S1[ly][lx - 1];
-        const float pn = S1[ly + 1][lx], ps = S1[ly - 1][lx];
-        const float pt = S2[ly][lx], pb = S0[ly][lx];
-        const float pen = S1[ly + 1][lx + 1], pws = S1[ly - 1][lx - 1];
-        const float pes = S1[ly - 1][lx + 1], pwn = S1[ly + 1][lx - 1];
-        const float pet = S2[ly][lx + 1], pwb = S0[ly][lx - 1];
-        const float peb = S0[ly][lx + 1], pwt = S2[ly][lx - 1];
-        const float pnt = S2[ly + 1][lx], psb = S0[ly - 1][lx];
-        const float pnb = S0[ly + 1][lx], pst = S2[ly - 1][lx];
+        const float pc = at(S1, ly, lx);
+        const float pe = at(S1, ly, lx + 1), pw = at(S1, ly, lx - 1);
+        const float pn = at(S1, ly + 1, lx), ps = at(S1, ly - 1, lx);
+        const float pt = at(S2, ly, lx), pb = at(S0, ly, lx);
+        const float pen = at(S1, ly + 1, lx + 1), pws = at(S1, ly - 1, lx - 1);
+        const float pes = at(S1, ly - 1, lx + 1), pwn = at(S1, ly + 1, lx - 1);
+        const float pet = at(S2, ly, lx + 1), pwb = at(S0, ly, lx - 1);
+        const float peb = at(S0, ly, lx + 1), pwt = at(S2, ly, lx - 1);
+        const float pnt = at(S2, ly + 1, lx), psb = at(S0, ly - 1, lx);
+        const float pnb = at(S0, ly + 1, lx), pst = at(S2, ly - 1, lx);
 
         const float lap = (pen + pws + pes + pwn + pet + pwb + peb + pwt + pnt + psb + pnb + pst
                            + 2.f * (pe + pw + pn + ps + pt + pb - 12.f * pc)) * kInv6;
@@ -192,34 +310,11 @@ zsc_step_kernel(const StepPtrs P, const Box b, const StepConst c, const int writ
         float Fz = mu * (2.f * (pt - pb) + pet - pwb + pwt - peb + pnt - psb + pst - pnb) * kInv12;
         if (pc > 0.f) Fz += c.grav;
 
-        // D3Q19 values of this node (AA pattern)
-        const unsigned id = node_index(b, x, y, z);
-        const Nbr o = neighbours(b, x, y, z);
+        // D3Q19 values of this node from the staged rows (AA pattern)
+        const float *Gs = G + (j & 1) * G_STAGE;
         float g[kQg];
-        if (!ODD) {
 #pragma unroll
-            for (int i = 0; i < kQg; i++) g[i] = P.g[i][id];
-        } else {
-            g[0] = P.g[0][id];
-            g[1] = P.g[2][id + o.xm];
-            g[2] = P.g[1][id + o.xp];
-            g[3] = P.g[4][id + o.ym];
-            g[4] = P.g[3][id + o.yp];
-            g[5] = P.g[6][id + o.zm];
-            g[6] = P.g[5][id + o.zp];
-            g[7] = P.g[8][id + o.xm + o.ym];
-            g[8] = P.g[7][id + o.xp + o.yp];
-            g[9] = P.g[10][id + o.xm + o.yp];
-            g[10] = P.g[9][id + o.xp + o.ym];
-            g[11] = P.g[12][id + o.xm + o.zm];
-            g[12] = P.g[11][id + o.xp + o.zp];
-            g[13] = P.g[14][id + o.xm + o.zp];
-            g[14] = P.g[13][id + o.xp + o.zm];
-            g[15] = P.g[16][id + o.ym + o.zm];
-            g[16] = P.g[15][id + o.yp + o.zp];
-            g[17] = P.g[18][id + o.ym + o.zp];
-            g[18] = P.g[17][id + o.yp + o.zm];
-        }
+        for (int i = 0; i < kQg; i++) g[i] = Gs[(i * TY + ty) * GW + 4 + tx - (ODD ? kCx(i) : 0)];
 
         // moments: src/update_rho.cu:46-50, src/update_velocity.cu:47-59
         float rho = g[0];
@@ -229,6 +324,7 @@ zsc_step_kernel(const StepPtrs P, const Box b, const StepConst c, const int writ
         const float ux = (g[1] - g[2] + g[7] - g[8] + g[9] - g[10] + g[11] - g[12] + g[13] - g[14]) * invRho;
         const float uy = (g[3] - g[4] + g[7] - g[8] - g[9] + g[10] + g[15] - g[16] + g[17] - g[18]) * invRho;
         const float uz = (g[5] - g[6] + g[11] - g[12] - g[13] + g[14] + g[15] - g[16] - g[17] + g[18]) * invRho;
+        const unsigned id = node_index(b, x, y, z);
         if (write_moments) {
             P.mom[0][id] = pc;
             P.mom[1][id] = rho;
@@ -285,9 +381,9 @@ zsc_step_kernel(const StepPtrs P, const Box b, const StepConst c, const int writ
             {
                 const float K2r = K2 * rho;
                 const float temp2 = K2 * (phimu3 + rho * (1.f - vsq6));
-                auto pair = [&](float w, float G, int ip, int im) {
-                    const float eq1 = temp2 + K2r * w * 0.5f * w + KC2 * (w * G - UF);
-                    const float eq2 = K2r * w + KC2 * G;
+                auto pair = [&](float w, float Gf, int ip, int im) {
+                    const float eq1 = temp2 + K2r * w * 0.5f * w + KC2 * (w * Gf - UF);
+                    const float eq2 = K2r * w + KC2 * Gf;
                     q[ip] = bb * g[ip] + eq1 + eq2;
                     q[im] = bb * g[im] + eq1 - eq2;
                 };
@@ -300,52 +396,38 @@ zsc_step_kernel(const StepPtrs P, const Box b, const StepConst c, const int writ
             }
             if (!ODD) {
                 // even: own node, reversed slots
-                P.g[0][id] = q[0];
-                P.g[2][id] = q[1];
-                P.g[1][id] = q[2];
-                P.g[4][id] = q[3];
-                P.g[3][id] = q[4];
-                P.g[6][id] = q[5];
-                P.g[5][id] = q[6];
-                P.g[8][id] = q[7];
-                P.g[7][id] = q[8];
-                P.g[10][id] = q[9];
-                P.g[9][id] = q[10];
-                P.g[12][id] = q[11];
-                P.g[11][id] = q[12];
-                P.g[14][id] = q[13];
-                P.g[13][id] = q[14];
-                P.g[16][id] = q[15];
-                P.g[15][id] = q[16];
-                P.g[18][id] = q[17];
-                P.g[17][id] = q[18];
+#pragma unroll
+                for (int i = 0; i < kQg; i++) P.g[kOpp(i)][id] = q[i];
             } else {
                 // odd: downstream neighbour x + c_i, natural slot i
-                P.g[0][id] = q[0];
-                P.g[1][id + o.xp] = q[1];
-                P.g[2][id + o.xm] = q[2];
-                P.g[3][id + o.yp] = q[3];
-                P.g[4][id + o.ym] = q[4];
-                P.g[5][id + o.zp] = q[5];
-                P.g[6][id + o.zm] = q[6];
-                P.g[7][id + o.xp + o.yp] = q[7];
-                P.g[8][id + o.xm + o.ym] = q[8];
-                P.g[9][id + o.xp + o.ym] = q[9];
-                P.g[10][id + o.xm + o.yp] = q[10];
-                P.g[11][id + o.xp + o.zp] = q[11];
-                P.g[12][id + o.xm + o.zm] = q[12];
-                P.g[13][id + o.xp + o.zm] = q[13];
-                P.g[14][id + o.xm + o.zp] = q[14];
-                P.g[15][id + o.yp + o.zp] = q[15];
-                P.g[16][id + o.ym + o.zm] = q[16];
-                P.g[17][id + o.yp + o.zm] = q[17];
-                P.g[18][id + o.ym + o.zp] = q[18];
+                const Nbr o = neighbours(b, x, y, z);
+                auto off = [&](int i) {
+                    return (kCx(i) > 0 ? o.xp : kCx(i) < 0 ? o.xm : 0) + (kCy(i) > 0 ? o.yp : kCy(i) < 0 ? o.ym : 0)
+                           + (kCz(i) > 0 ? o.zp : kCz(i) < 0 ? o.zm : 0);
+                };
+#pragma unroll
+                for (int i = 0; i < kQg; i++) P.g[i][id + off(i)] = q[i];
             }
         }
 
 #pragma unroll
         for (int i = 0; i < kQf; i++) fcur[i] = fnext[i];
     }
+}
+
+template <bool S, bool O>
+cudaError_t launch_variant(unsigned nblocks, const StepPtrs &P, const Box &b, const StepConst &c, int wm,
+                           cudaStream_t s)
+{
+    static bool configured = false;   // per template instance, per process
+    if (!configured) {
+        const cudaError_t e = cudaFuncSetAttribute(zsc_step_kernel<S, O>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                   (int)kSmemBytes);
+        if (e != cudaSuccess) return e;
+        configured = true;
+    }
+    zsc_step_kernel<S, O><<<nblocks, dim3(TX, TY, 1), kSmemBytes, s>>>(P, b, c, wm);
+    return cudaGetLastError();
 }
 
 }  // namespace
@@ -363,17 +445,13 @@ cudaError_t launch_step(const Box &b, const StepConst &c, const float *f_in, flo
     for (int i = 0; i < 5; i++) P.mom[i] = mom + (size_t)i * b.n;
     const int nchunks = (b.nz + TZ - 1) / TZ;
     const unsigned nblocks = (unsigned)((b.nx / TX) * (b.ny / TY) * nchunks);
-    const dim3 block(TX, TY, 1);
     const int wm = write_moments ? 1 : 0;
     if (f_streamed) {
         if (odd) return cudaErrorInvalidValue;  // the streamed initial state is always read by an even step
-        zsc_step_kernel<true, false><<<nblocks, block, 0, s>>>(P, b, c, wm);
-    } else if (odd) {
-        zsc_step_kernel<false, true><<<nblocks, block, 0, s>>>(P, b, c, wm);
-    } else {
-        zsc_step_kernel<false, false><<<nblocks, block, 0, s>>>(P, b, c, wm);
+        return launch_variant<true, false>(nblocks, P, b, c, wm, s);
     }
-    return cudaGetLastError();
+    if (odd) return launch_variant<false, true>(nblocks, P, b, c, wm, s);
+    return launch_variant<false, false>(nblocks, P, b, c, wm, s);
 }
 
 }  // namespace lbm
