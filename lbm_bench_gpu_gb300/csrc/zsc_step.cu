@@ -69,7 +69,6 @@ constexpr float kInv6 = 0.16666666666666666667f;
 constexpr float kInv12 = 0.08333333333333333333f;
 
 // D3Q19 lattice vectors and opposite directions (reference order).
-// (compile-time forms for unrolled loops, table forms for runtime indices)
 __host__ __device__ constexpr int kCx(int i)
 {
     return (i == 1 || i == 7 || i == 9 || i == 11 || i == 13) ? 1
@@ -86,10 +85,11 @@ __host__ __device__ constexpr int kCz(int i)
            : (i == 6 || i == 12 || i == 13 || i == 16 || i == 17) ? -1 : 0;
 }
 __host__ __device__ constexpr int kOpp(int i) { return i == 0 ? 0 : ((i & 1) ? i + 1 : i - 1); }
-__constant__ int cCx[kQg] = {0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1, 0, 0, 0, 0};
-__constant__ int cCy[kQg] = {0, 0, 0, 1, -1, 0, 0, 1, -1, -1, 1, 0, 0, 0, 0, 1, -1, 1, -1};
-__constant__ int cCz[kQg] = {0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, -1, -1, 1, 1, -1, -1, 1};
-__constant__ int cOpp[kQg] = {0, 2, 1, 4, 3, 6, 5, 8, 7, 10, 9, 12, 11, 14, 13, 16, 15, 18, 17};
+
+template <int I>
+struct Dir {
+    static constexpr int value = I;
+};
 
 struct StepPtrs {
     const float *fin[kQf];
@@ -176,44 +176,87 @@ zsc_step_kernel(const StepPtrs P, const Box b, const StepConst c, const int writ
     // P_f stage of plane p (p >= z0 - 2)
     auto fslot = [&](int p) { return F + ((p - z0 + 4) & (NF - 1)) * F_STAGE; };
 
+    // ---- staging roles, fixed per thread for the whole chunk ----
+    // Warps 0-3 queue the 7 P_f planes: thread t < FR * GW/4 owns staged row
+    // t / (GW/4), 16-byte chunk t % (GW/4), of every array.
+    constexpr int kFChunks = FR * (GW / 4);
+    static_assert(kFChunks <= NT / 2, "P_f issuers fit in the first half of the block");
+    const bool f_issuer = tid < kFChunks;
+    int f_xy = 0, f_dst = 0;
+    if (f_issuer) {
+        const int r = tid / (GW / 4), k = tid - r * (GW / 4);
+        f_xy = wrap(x0 - 4 + 4 * k, b.nx) + b.nx * wrap(y0 - 2 + r, b.ny);
+        f_dst = r * GW + 4 * k;
+    }
+    // Warps 4-7 queue the g rows: thread owns row g_r, chunk g_k of every
+    // second direction (g_hi: odd or even directions; uniform per warp).
+    static_assert(TX == 32 && TY == 8, "g issuer mapping: 8 rows x 8 chunks per direction, two halves");
+    const int gt = tid - NT / 2;
+    const bool g_issuer = gt >= 0;
+    const int g_hi = (gt >> 6) & 1;
+    const int g_r = (gt & 63) >> 3, g_k = gt & 7;
+    int g_row_0 = 0, g_row_p = 0, g_row_m = 0, g_x_lo = 0, g_x_hi = 0, g_x_wrap = 0;
+    if (g_issuer) {
+        g_row_0 = b.nx * (y0 + g_r);
+        g_row_p = b.nx * wrap(y0 + g_r - 1, b.ny);   // directions with c_y = +1 read row y - 1
+        g_row_m = b.nx * wrap(y0 + g_r + 1, b.ny);   // c_y = -1 reads row y + 1
+        g_x_lo = wrap(x0 - 4 + 4 * g_k, b.nx);        // c_x = +1 reads x - 1: chunks from x0 - 4
+        g_x_hi = x0 + 4 * g_k;                         // c_x <= 0: chunks from x0
+        g_x_wrap = wrap(x0 + TX, b.nx);                // c_x = -1 also needs x0 + 32
+    }
+
     // Queue the 7 P_f planes of plane p (tile + halo) into its stage.
     auto issue_f = [&](int p) {
-        const int pw = wrap(p, b.nz);
-        float *dst = fslot(p);
-        constexpr int kChunks = kQf * FR * (GW / 4);
-        for (int ch = tid; ch < kChunks; ch += NT) {
-            const int arr = ch / (FR * (GW / 4));
-            const int rem = ch - arr * (FR * (GW / 4));
-            const int r = rem / (GW / 4), k = rem - r * (GW / 4);
-            const int yy = wrap(y0 - 2 + r, b.ny), xx = wrap(x0 - 4 + 4 * k, b.nx);
-            cp_async16(dst + (arr * FR + r) * GW + 4 * k, P.fin[arr] + node_index(b, xx, yy, pw));
+        if (!f_issuer) return;
+        const unsigned base = (unsigned)wrap(p, b.nz) * (unsigned)b.nxy + (unsigned)f_xy;
+        float *dst = fslot(p) + f_dst;
+#pragma unroll
+        for (int arr = 0; arr < kQf; arr++) cp_async16(dst + arr * FR * GW, P.fin[arr] + base);
+    };
+
+    // Call f(direction) for the directions this g issuer owns (compile-time
+    // direction numbers; the branch is uniform per warp).
+    auto for_my_dirs = [&](auto &&f) {
+        if (g_hi == 0) {
+            f(Dir<0>{}); f(Dir<2>{}); f(Dir<4>{}); f(Dir<6>{}); f(Dir<8>{});
+            f(Dir<10>{}); f(Dir<12>{}); f(Dir<14>{}); f(Dir<16>{}); f(Dir<18>{});
+        } else {
+            f(Dir<1>{}); f(Dir<3>{}); f(Dir<5>{}); f(Dir<7>{}); f(Dir<9>{});
+            f(Dir<11>{}); f(Dir<13>{}); f(Dir<15>{}); f(Dir<17>{});
         }
     };
 
-    // Queue the 19 g rows the nodes of plane z read, into g stage s.
+    // Queue the 19 g rows the nodes of plane z read, into g stage s.  Even
+    // steps read the node's own slots; odd steps read direction i of node x
+    // from the reversed slot of x - c_i (AA pattern).
     auto issue_g = [&](int z, int s) {
-        float *dst = G + s * G_STAGE;
+        if (!g_issuer) return;
+        float *dst = G + s * G_STAGE + g_r * GW;
         if (!ODD) {
-            constexpr int kChunks = kQg * TY * (TX / 4);
-            for (int ch = tid; ch < kChunks; ch += NT) {
-                const int i = ch / (TY * (TX / 4));
-                const int r = (ch / (TX / 4)) % TY, k = ch % (TX / 4);
-                cp_async16(dst + (i * TY + r) * GW + 4 + 4 * k, P.g[i] + node_index(b, x0 + 4 * k, y0 + r, z));
-            }
+            const unsigned base = (unsigned)z * (unsigned)b.nxy + (unsigned)(g_row_0 + g_x_hi);
+            for_my_dirs([&](auto d) {
+                constexpr int i = decltype(d)::value;
+                cp_async16(dst + i * TY * GW + 4 + 4 * g_k, P.g[i] + base);
+            });
         } else {
-            // direction i of node x sits in the reversed slot of x - c_i
-            constexpr int kRowChunks = TX / 4 + 1;
-            constexpr int kChunks = kQg * TY * kRowChunks;
-            for (int ch = tid; ch < kChunks; ch += NT) {
-                const int i = ch / (TY * kRowChunks);
-                const int rem = ch - i * (TY * kRowChunks);
-                const int r = rem / kRowChunks, k = rem - r * kRowChunks;
-                const int cx = cCx[i];
-                const int yy = wrap(y0 + r - cCy[i], b.ny), zz = wrap(z - cCz[i], b.nz);
-                const int xs = cx < 0 ? x0 + 4 * k : x0 - 4 + 4 * k;
-                const int col = cx < 0 ? 4 + 4 * k : 4 * k;
-                cp_async16(dst + (i * TY + r) * GW + col, P.g[cOpp[i]] + node_index(b, wrap(xs, b.nx), yy, zz));
-            }
+            const unsigned zb0 = (unsigned)z * (unsigned)b.nxy;
+            const unsigned zbp = (unsigned)wrap(z - 1, b.nz) * (unsigned)b.nxy;   // c_z = +1 reads z - 1
+            const unsigned zbm = (unsigned)wrap(z + 1, b.nz) * (unsigned)b.nxy;   // c_z = -1 reads z + 1
+            for_my_dirs([&](auto d) {
+                constexpr int i = decltype(d)::value;
+                constexpr int cx = kCx(i), cy = kCy(i), cz = kCz(i);
+                const unsigned zb = cz > 0 ? zbp : (cz < 0 ? zbm : zb0);
+                const int row = cy > 0 ? g_row_p : (cy < 0 ? g_row_m : g_row_0);
+                const float *src = P.g[kOpp(i)] + (zb + (unsigned)row);
+                float *d_row = dst + i * TY * GW;
+                if (cx > 0) {
+                    cp_async16(d_row + 4 * g_k, src + g_x_lo);
+                    if (g_k == 0) cp_async16(d_row + 32, src + (x0 + 28));
+                } else {
+                    cp_async16(d_row + 4 + 4 * g_k, src + g_x_hi);
+                    if (cx < 0 && g_k == 0) cp_async16(d_row + 36, src + g_x_wrap);
+                }
+            });
         }
     };
 
