@@ -41,15 +41,11 @@ namespace {
 #ifndef ZSC_TILE_Y
 #define ZSC_TILE_Y 8
 #endif
-#ifndef ZSC_TILE_Z
-#define ZSC_TILE_Z 32
-#endif
 #ifndef ZSC_MIN_BLOCKS
 #define ZSC_MIN_BLOCKS 2
 #endif
 constexpr int TX = 32;              // tile width in x (one warp per row)
 constexpr int TY = ZSC_TILE_Y;      // tile height in y
-constexpr int TZ = ZSC_TILE_Z;      // planes per block
 constexpr int NT = TX * TY;         // threads per block
 constexpr int GW = 40;              // staged row width: x in [x0 - 4, x0 + 36)
 constexpr int FR = TY + 4;          // staged P_f rows: y in [y0 - 2, y0 + TY + 2)
@@ -135,7 +131,7 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 
 template <bool STREAMED, bool ODD>
 __global__ void __launch_bounds__(NT, ZSC_MIN_BLOCKS)
-zsc_step_kernel(const StepPtrs P, const Box b, const StepConst c, const int write_moments)
+zsc_step_kernel(const StepPtrs P, const Box b, const StepConst c, const int tz, const int write_moments)
 {
     extern __shared__ __align__(16) float smem[];
     float *const G = smem;                    // [NG][19][TY][GW]
@@ -150,8 +146,8 @@ zsc_step_kernel(const StepPtrs P, const Box b, const StepConst c, const int writ
     bid /= ntx;
     const int by = bid % nty;
     bid /= nty;
-    const int z0 = bid * TZ;
-    const int nzc = min(TZ, b.nz - z0);       // planes of this chunk
+    const int z0 = bid * tz;
+    const int nzc = min(tz, b.nz - z0);       // planes of this chunk
     const int x0 = bx * TX, y0 = by * TY;
     const int x = x0 + tx, y = y0 + ty;
 
@@ -459,18 +455,45 @@ zsc_step_kernel(const StepPtrs P, const Box b, const StepConst c, const int writ
 }
 
 template <bool S, bool O>
-cudaError_t launch_variant(unsigned nblocks, const StepPtrs &P, const Box &b, const StepConst &c, int wm,
-                           cudaStream_t s)
+cudaError_t configure()
 {
-    static bool configured = false;   // per template instance, per process
-    if (!configured) {
-        const cudaError_t e = cudaFuncSetAttribute(zsc_step_kernel<S, O>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                   (int)kSmemBytes);
-        if (e != cudaSuccess) return e;
-        configured = true;
+    static bool done = false;   // per template instance, per process
+    if (done) return cudaSuccess;
+    const cudaError_t e =
+        cudaFuncSetAttribute(zsc_step_kernel<S, O>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes);
+    if (e == cudaSuccess) done = true;
+    return e;
+}
+
+// Planes per block.  The blocks of one launch all march the same number of
+// planes, so the step takes about ceil(blocks / resident slots) "waves" of
+// (tz + prologue) planes; pick the chunk depth that minimises that product
+// (e.g. 256^3: 37 planes -> 1792 blocks = 5.9 waves of 304 slots, instead of
+// 32 planes -> 6.7 waves with a 74%-full last wave).
+int choose_tz(const Box &b)
+{
+    static int slots = 0;
+    if (slots == 0) {
+        int dev = 0, sms = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, zsc_step_kernel<false, false>, NT, kSmemBytes);
+        slots = sms * per_sm > 0 ? sms * per_sm : 1;
     }
-    zsc_step_kernel<S, O><<<nblocks, dim3(TX, TY, 1), kSmemBytes, s>>>(P, b, c, wm);
-    return cudaGetLastError();
+    const long long tiles = (long long)(b.nx / TX) * (b.ny / TY);
+    constexpr int kPrologue = 3;   // extra planes each block stages and rebuilds
+    int best = 32;
+    long long best_cost = -1;
+    for (int tz = 4; tz <= 64; tz++) {
+        const long long chunks = (b.nz + tz - 1) / tz;
+        const long long waves = (tiles * chunks + slots - 1) / slots;
+        const long long cost = waves * (tz + kPrologue);
+        if (best_cost < 0 || cost < best_cost) {
+            best_cost = cost;
+            best = tz;
+        }
+    }
+    return best;
 }
 
 }  // namespace
@@ -486,15 +509,24 @@ cudaError_t launch_step(const Box &b, const StepConst &c, const float *f_in, flo
     }
     for (int i = 0; i < kQg; i++) P.g[i] = g + (size_t)i * b.n;
     for (int i = 0; i < 5; i++) P.mom[i] = mom + (size_t)i * b.n;
-    const int nchunks = (b.nz + TZ - 1) / TZ;
+    cudaError_t e = configure<true, false>();
+    if (e == cudaSuccess) e = configure<false, true>();
+    if (e == cudaSuccess) e = configure<false, false>();
+    if (e != cudaSuccess) return e;
+    const int tz = choose_tz(b);
+    const int nchunks = (b.nz + tz - 1) / tz;
     const unsigned nblocks = (unsigned)((b.nx / TX) * (b.ny / TY) * nchunks);
+    const dim3 block(TX, TY, 1);
     const int wm = write_moments ? 1 : 0;
     if (f_streamed) {
         if (odd) return cudaErrorInvalidValue;  // the streamed initial state is always read by an even step
-        return launch_variant<true, false>(nblocks, P, b, c, wm, s);
+        zsc_step_kernel<true, false><<<nblocks, block, kSmemBytes, s>>>(P, b, c, tz, wm);
+    } else if (odd) {
+        zsc_step_kernel<false, true><<<nblocks, block, kSmemBytes, s>>>(P, b, c, tz, wm);
+    } else {
+        zsc_step_kernel<false, false><<<nblocks, block, kSmemBytes, s>>>(P, b, c, tz, wm);
     }
-    if (odd) return launch_variant<false, true>(nblocks, P, b, c, wm, s);
-    return launch_variant<false, false>(nblocks, P, b, c, wm, s);
+    return cudaGetLastError();
 }
 
 }  // namespace lbm
