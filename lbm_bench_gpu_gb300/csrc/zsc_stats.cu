@@ -21,9 +21,14 @@ constexpr int kMaxBlocks = 152 * 8;
 constexpr float kInv6 = 0.16666666666666666667f;
 constexpr float kInv12 = 0.08333333333333333333f;
 
+constexpr float kCsSq = 0.33333333333333333333f;   // src/constants.h:48
+
 struct StatsConst {
     float alpha, kappa, phiStarSq;
 };
+
+// row index of (y, z)
+__device__ __forceinline__ int kk_row(int y, int z, int ny) { return y + ny * z; }
 
 __device__ __forceinline__ double warp_sum(double v)
 {
@@ -59,6 +64,9 @@ __device__ void block_reduce(double (&acc)[kStatsValues], double *out)
     }
 }
 
+// One block works on whole x-rows (row r = y + ny z, grid-stride over rows);
+// the pressure is evaluated in float as the reference does
+// (src/logsave.c:94-137), every sum is accumulated in FP64.
 __global__ void __launch_bounds__(kThreads) stats_kernel(Box b, StatsConst c, const float *__restrict__ phi,
                                                          const float *__restrict__ rho, const float *__restrict__ ux,
                                                          const float *__restrict__ uy, const float *__restrict__ uz,
@@ -68,54 +76,59 @@ __global__ void __launch_bounds__(kThreads) stats_kernel(Box b, StatsConst c, co
 #pragma unroll
     for (int v = 0; v < kStatsValues; v++) acc[v] = 0.0;
 
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < b.n;
-         t += (long long)gridDim.x * blockDim.x) {
-        const int i = (int)(t % b.nx);
-        const int j = (int)((t / b.nx) % b.ny);
-        const int k = (int)(t / b.nxy);
-        const float ph = phi[t], rh = rho[t], vx = ux[t], vy = uy[t], vz = uz[t];
-        if (!(isfinite(ph) && isfinite(rh) && isfinite(vx) && isfinite(vy) && isfinite(vz))) {
-            acc[14] += 1.0;
-            continue;
-        }
-        const double u2 = (double)vx * vx + (double)vy * vy + (double)vz * vz;
-        acc[7] += ph;
-        acc[8] += rh;
-        acc[9] += (double)rh * vx;
-        acc[10] += (double)rh * vy;
-        acc[11] += (double)rh * vz;
-        if (ph >= 0.f) acc[12] += 1.0;
-        acc[13] = fmax(acc[13], u2);
-        if (i < 1 || i > b.nx - 2 || j < 1 || j > b.ny - 2) continue;
-        acc[0] = fmax(acc[0], u2);
+    const int nx = b.nx, ny = b.ny, nz = b.nz;
+    const int rows = ny * nz;
+    for (int r = blockIdx.x; r < rows; r += gridDim.x) {
+        const int k = r / ny, j = r - k * ny;
+        const bool row_in = j >= 1 && j <= ny - 2;   // reference region in y
+        const int jn = j == ny - 1 ? 0 : j + 1, js = j == 0 ? ny - 1 : j - 1;
+        const int kt = k == nz - 1 ? 0 : k + 1, kb = k == 0 ? nz - 1 : k - 1;
+        const size_t row_c = (size_t)r * nx;
+        const size_t row_n = ((size_t)kk_row(jn, k, ny)) * nx, row_s = ((size_t)kk_row(js, k, ny)) * nx;
+        const size_t row_t = ((size_t)kk_row(j, kt, ny)) * nx, row_b = ((size_t)kk_row(j, kb, ny)) * nx;
+        const size_t row_nt = ((size_t)kk_row(jn, kt, ny)) * nx, row_sb = ((size_t)kk_row(js, kb, ny)) * nx;
+        const size_t row_nb = ((size_t)kk_row(jn, kb, ny)) * nx, row_st = ((size_t)kk_row(js, kt, ny)) * nx;
+        for (int i = threadIdx.x; i < nx; i += blockDim.x) {
+            const size_t t = row_c + i;
+            const float ph = phi[t], rh = rho[t], vx = ux[t], vy = uy[t], vz = uz[t];
+            if (!(isfinite(ph) && isfinite(rh) && isfinite(vx) && isfinite(vy) && isfinite(vz))) {
+                acc[14] += 1.0;
+                continue;
+            }
+            const double u2 = (double)vx * vx + (double)vy * vy + (double)vz * vz;
+            acc[7] += ph;
+            acc[8] += rh;
+            acc[9] += (double)rh * vx;
+            acc[10] += (double)rh * vy;
+            acc[11] += (double)rh * vz;
+            if (ph >= 0.f) acc[12] += 1.0;
+            acc[13] = fmax(acc[13], u2);
+            if (!row_in || i < 1 || i > nx - 2) continue;
+            acc[0] = fmax(acc[0], u2);
 
-        // pressure, src/logsave.c:94-137 (periodic neighbours)
-        const int ie = i == b.nx - 1 ? 0 : i + 1, iw = i == 0 ? b.nx - 1 : i - 1;
-        const int jn = j == b.ny - 1 ? 0 : j + 1, js = j == 0 ? b.ny - 1 : j - 1;
-        const int kt = k == b.nz - 1 ? 0 : k + 1, kb = k == 0 ? b.nz - 1 : k - 1;
-        auto P = [&](int x, int y, int z) -> float { return phi[x + b.nx * (y + (long long)b.ny * z)]; };
-        const float p01 = P(ie, j, k), p02 = P(iw, j, k), p03 = P(i, jn, k), p04 = P(i, js, k);
-        const float p05 = P(i, j, kt), p06 = P(i, j, kb), p07 = P(ie, jn, k), p08 = P(iw, js, k);
-        const float p09 = P(ie, js, k), p10 = P(iw, jn, k), p11 = P(ie, j, kt), p12 = P(iw, j, kb);
-        const float p13 = P(ie, j, kb), p14 = P(iw, j, kt), p15 = P(i, jn, kt), p16 = P(i, js, kb);
-        const float p17 = P(i, jn, kb), p18 = P(i, js, kt);
-        const double lap = ((double)p07 + p08 + p09 + p10 + p11 + p12 + p13 + p14 + p15 + p16 + p17 + p18
-                            + 2.0 * ((double)p01 + p02 + p03 + p04 + p05 + p06 - 12.0 * ph)) * kInv6;
-        const double gx = (2.0 * ((double)p01 - p02) + p07 - p08 + p09 - p10 + p11 - p12 + p13 - p14) * kInv12;
-        const double gy = (2.0 * ((double)p03 - p04) + p07 - p08 + p10 - p09 + p15 - p16 + p17 - p18) * kInv12;
-        const double gz = (2.0 * ((double)p05 - p06) + p11 - p12 + p14 - p13 + p15 - p16 + p18 - p17) * kInv12;
-        const double ph2 = (double)ph * ph;
-        const double pss = c.phiStarSq;
-        const double pres = c.alpha * (ph2 * (3.0 * ph2 - 2.0 * pss) - pss * pss)
-                            - c.kappa * (ph * lap - 0.5 * (gx * gx + gy * gy + gz * gz)) + rh / 3.0;
-        if (ph >= 0.f) {
-            acc[1] += 1.0;
-            acc[2] += vx;
-            acc[3] += vy;
-            acc[4] += vz;
-            acc[5] += pres;
-        } else {
-            acc[6] += pres;
+            const int ie = i == nx - 1 ? 0 : i + 1, iw = i == 0 ? nx - 1 : i - 1;
+            const float p01 = phi[row_c + ie], p02 = phi[row_c + iw], p03 = phi[row_n + i], p04 = phi[row_s + i];
+            const float p05 = phi[row_t + i], p06 = phi[row_b + i], p07 = phi[row_n + ie], p08 = phi[row_s + iw];
+            const float p09 = phi[row_s + ie], p10 = phi[row_n + iw], p11 = phi[row_t + ie], p12 = phi[row_b + iw];
+            const float p13 = phi[row_b + ie], p14 = phi[row_t + iw], p15 = phi[row_nt + i], p16 = phi[row_sb + i];
+            const float p17 = phi[row_nb + i], p18 = phi[row_st + i];
+            const float lap = (p07 + p08 + p09 + p10 + p11 + p12 + p13 + p14 + p15 + p16 + p17 + p18
+                               + 2.f * (p01 + p02 + p03 + p04 + p05 + p06 - 12.f * ph)) * kInv6;
+            const float gx = (2.f * (p01 - p02) + p07 - p08 + p09 - p10 + p11 - p12 + p13 - p14) * kInv12;
+            const float gy = (2.f * (p03 - p04) + p07 - p08 + p10 - p09 + p15 - p16 + p17 - p18) * kInv12;
+            const float gz = (2.f * (p05 - p06) + p11 - p12 + p14 - p13 + p15 - p16 + p18 - p17) * kInv12;
+            const float ph2 = ph * ph;
+            const float pres = c.alpha * (ph2 * (3.f * ph2 - 2.f * c.phiStarSq) - c.phiStarSq * c.phiStarSq)
+                               - c.kappa * (ph * lap - 0.5f * (gx * gx + gy * gy + gz * gz)) + kCsSq * rh;
+            if (ph >= 0.f) {
+                acc[1] += 1.0;
+                acc[2] += vx;
+                acc[3] += vy;
+                acc[4] += vz;
+                acc[5] += pres;
+            } else {
+                acc[6] += pres;
+            }
         }
     }
     block_reduce(acc, partials + (size_t)blockIdx.x * kStatsValues);
@@ -139,7 +152,7 @@ __global__ void __launch_bounds__(kThreads) fold_kernel(const double *__restrict
 
 unsigned stats_blocks(const Box &b)
 {
-    long long blocks = (b.n + kThreads - 1) / kThreads;
+    long long blocks = (long long)b.ny * b.nz;   // one x-row per block and pass
     if (blocks > kMaxBlocks) blocks = kMaxBlocks;
     return (unsigned)(blocks < 1 ? 1 : blocks);
 }
