@@ -34,7 +34,9 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 METRIC = "MLUPS + HBM GB/s (FP32 vs FP16-storage) at 256^3; adjoint-to-forward time ratio"
-BYTES_PER_NODE = {"fp32": 26 * 2 * 4, "fp16": 26 * 2 * 2, "bf16": 26 * 2 * 2}
+# algorithmic bytes per lattice update: every distribution read and written once
+# (16-bit formats keep the D3Q7 rest population f_0 in FP32)
+BYTES_PER_NODE = {"fp32": 26 * 2 * 4, "fp16": 2 * 4 + 25 * 2 * 2, "bf16": 2 * 4 + 25 * 2 * 2}
 FALLBACK_HBM_GBS = 6800.0
 
 
@@ -49,6 +51,7 @@ def parse_args(argv=None):
     ap.add_argument("--storage", default="fp32")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-variants", action="store_true", help="time only --storage (not the other formats)")
     ap.add_argument("--stat-every", type=int, default=100, help="lbm_stats cadence inside the e2e run")
     return ap.parse_args(argv)
 
@@ -190,36 +193,29 @@ def cpu_baseline(inp, budget_s: float = 15.0):
                       f"({dt:.1f} s)"}
 
 
-def run_ours(args, rank, world, local):
+def time_storage(inp, storage, local, K, W, sampler=None):
+    """Device time (ms) of K fused steps on resident state, CUDA events on the
+    context's stream."""
     import torch
     from lbm_bench_gpu_gb300 import capi
-
-    torch.cuda.set_device(local)
-    inp = workload(args.size, args.bubbles)
-    p = params_for(inp, args.storage, local)
+    p = params_for(inp, storage, local)
     grav = float(capi.derive(p).grav)
-    nodes = inp.nx * inp.ny * inp.nz
-    K, W = args.steps, args.warmup
-
     lat = capi.Lattice.from_bubbles(p, inp.bubbles)
     stream = torch.cuda.ExternalStream(lat.stream, device=local)
     lat.step(W, grav)
     lat.sync()
-
+    world = int(os.environ.get("WORLD_SIZE", "1"))
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
-    sampler = ClockSampler(gpu_identity(local)) if rank == 0 else None
     if sampler:
         sampler.__enter__()
-    t_start = time.time()
     e0.record(stream)
     lat.step(K, grav)
     e1.record(stream)
     e1.synchronize()
-    t_end = time.time()
     if sampler:
         sampler.__exit__(None, None, None)
     torch.cuda.synchronize()
@@ -231,9 +227,25 @@ def run_ours(args, rank, world, local):
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms = float(t.item())
     s, _ = lat.stats()
-    if s["nonfinite"]:
-        raise RuntimeError("state went non-finite during the bench")
     lat.close()
+    if s["nonfinite"]:
+        raise RuntimeError(f"state went non-finite during the {storage} bench")
+    return ms
+
+
+def run_ours(args, rank, world, local):
+    import torch
+    from lbm_bench_gpu_gb300 import capi
+
+    torch.cuda.set_device(local)
+    inp = workload(args.size, args.bubbles)
+    p = params_for(inp, args.storage, local)
+    grav = float(capi.derive(p).grav)
+    nodes = inp.nx * inp.ny * inp.nz
+    K, W = args.steps, args.warmup
+
+    sampler = ClockSampler(gpu_identity(local)) if rank == 0 else None
+    ms = time_storage(inp, args.storage, local, K, W, sampler)
 
     ms_step = ms / K
     value = world * nodes * K / (ms / 1e3) / 1e6
@@ -251,7 +263,7 @@ def run_ours(args, rank, world, local):
                                "gravity -1e-6 along z",
                    "nx": inp.nx, "ny": inp.ny, "nz": inp.nz, "bubbles": args.bubbles, "storage": args.storage,
                    "seed": 20261203, "parallelism": f"replicas x{world}",
-                   "l2": "state 1.75 GB >> 129 MB L2: no flush needed"},
+                   "l2": "state >= 1.5 GB >> 129 MB L2: no flush needed"},
         "hbm_gbs": round(achieved, 1),
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic,
@@ -259,7 +271,20 @@ def run_ours(args, rank, world, local):
         "gpu_launches": K,
     }
     if sampler:
-        result["clocks"] = sampler.summary(t_start, t_end)
+        result["clocks"] = sampler.summary(0, 0)
+    if not args.no_variants:
+        variants = {}
+        for st in ("fp32", "fp16", "bf16"):
+            if st == args.storage:
+                continue
+            ms_v = time_storage(inp, st, local, K, W)
+            b_v = BYTES_PER_NODE[st]
+            mlups = world * nodes * K / (ms_v / 1e3) / 1e6
+            variants[st] = {"value": round(mlups, 1), "unit": "MLUPS", "ms_per_step": round(ms_v / K, 5),
+                            "hbm_gbs": round(b_v * nodes / (ms_v / K / 1e3) / 1e9, 1),
+                            "roofline_frac": round(b_v * nodes / (ms_v / K / 1e3) / 1e9 / peak, 4),
+                            "bytes_per_node": b_v, "speedup_vs_headline": round(mlups / value, 3)}
+        result["storage_variants"] = variants
     if rank == 0 and not args.no_e2e:
         result["e2e"] = run_e2e(args, inp, p, grav, local)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

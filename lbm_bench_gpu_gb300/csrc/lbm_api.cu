@@ -12,7 +12,8 @@ struct lbm_ctx {
     lbm::Box box;
     cudaStream_t stream = nullptr;
     lbm::State st;
-    bool g_odd_next = false;       // the next step reads g in the AA "odd" layout
+    lbm::Quant q;
+    size_t esz = 4;                // bytes per element of fq / g
     double *partials = nullptr;    // stats scratch: per-block partial sums
     size_t partial_count = 0;
     double *result = nullptr;      // stats result (device)
@@ -20,6 +21,10 @@ struct lbm_ctx {
 };
 
 namespace {
+
+constexpr double kW[lbm::kQg] = {1.0 / 3,  1.0 / 18, 1.0 / 18, 1.0 / 18, 1.0 / 18, 1.0 / 18, 1.0 / 18,
+                                 1.0 / 36, 1.0 / 36, 1.0 / 36, 1.0 / 36, 1.0 / 36, 1.0 / 36, 1.0 / 36,
+                                 1.0 / 36, 1.0 / 36, 1.0 / 36, 1.0 / 36, 1.0 / 36};   // src/constants.h:52-54
 
 int fail(int code, const std::string &msg)
 {
@@ -33,9 +38,9 @@ int cuda_fail(cudaError_t e, const char *what)
                 std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-#define LBM_CUDA(call, what)                          \
-    do {                                              \
-        cudaError_t e_ = (call);                      \
+#define LBM_CUDA(call, what)                               \
+    do {                                                   \
+        cudaError_t e_ = (call);                           \
         if (e_ != cudaSuccess) return cuda_fail(e_, what); \
     } while (0)
 
@@ -59,8 +64,18 @@ int validate(const lbm_params *p)
         return fail(LBM_EINVAL, "tauRho, tauPhi and width must be positive");
     if (!(p->rhoH != p->rhoL)) return fail(LBM_EINVAL, "rhoH must differ from rhoL");
     if (p->Eo != 0.f && !(p->rc0 > 0.f)) return fail(LBM_EINVAL, "rc0 must be positive when Eo is not zero");
-    if (p->storage != LBM_STORAGE_FP32) return fail(LBM_EINVAL, "storage format not supported");
+    if (p->storage != LBM_STORAGE_FP32 && p->storage != LBM_STORAGE_FP16 && p->storage != LBM_STORAGE_BF16)
+        return fail(LBM_EINVAL, "unknown storage format");
     return LBM_OK;
+}
+
+void identity_quant(lbm::Quant &q)
+{
+    for (int a = 0; a < lbm::kQf - 1; a++) q.f_scale[a] = q.f_inv[a] = 1.f;
+    for (int i = 0; i < lbm::kQg; i++) {
+        q.g_scale[i] = q.g_inv[i] = 1.f;
+        q.g_shift[i] = 0.f;
+    }
 }
 
 // Allocate a context and its buffers; the state is left uninitialised.
@@ -79,6 +94,8 @@ int create(lbm_ctx **out, const lbm_params *p)
         c->d.gravity = 0.f;
         c->d.grav = 0.f;
     }
+    identity_quant(c->q);
+    c->esz = lbm::storage_bytes(p->storage);
     c->box.nx = p->nx;
     c->box.ny = p->ny;
     c->box.nz = p->nz;
@@ -86,8 +103,9 @@ int create(lbm_ctx **out, const lbm_params *p)
     c->box.n = c->box.nxy * p->nz;
     const size_t n = (size_t)c->box.n;
     cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaMalloc(&c->st.f, sizeof(float) * 2 * lbm::kQf * n);
-    if (e == cudaSuccess) e = cudaMalloc(&c->st.g, sizeof(float) * lbm::kQg * n);
+    if (e == cudaSuccess) e = cudaMalloc(&c->st.f0, sizeof(float) * 2 * n);
+    if (e == cudaSuccess) e = cudaMalloc(&c->st.fq, c->esz * 2 * (lbm::kQf - 1) * n);
+    if (e == cudaSuccess) e = cudaMalloc(&c->st.g, c->esz * lbm::kQg * n);
     if (e == cudaSuccess) e = cudaMalloc(&c->st.mom, sizeof(float) * 5 * n);
     c->partial_count = lbm::stats_partial_count(c->box);
     if (e == cudaSuccess) e = cudaMalloc(&c->partials, sizeof(double) * lbm::kStatsValues * c->partial_count);
@@ -101,16 +119,112 @@ int create(lbm_ctx **out, const lbm_params *p)
     return LBM_OK;
 }
 
-float *f_half(lbm_ctx *c, int half) { return c->st.f + (size_t)half * lbm::kQf * c->box.n; }
-
-int finish_init(lbm_ctx *c)
+// The buffers of a step that reads half `in` of f.
+lbm::StepView view(lbm_ctx *c, int in)
 {
+    const size_t n = (size_t)c->box.n;
+    const int out = 1 - in;
+    unsigned char *fq = static_cast<unsigned char *>(c->st.fq);
+    lbm::StepView v;
+    v.storage = c->p.storage;
+    v.f0_in = c->st.f0 + (size_t)in * n;
+    v.f0_out = c->st.f0 + (size_t)out * n;
+    v.fq_in = fq + (size_t)in * (lbm::kQf - 1) * n * c->esz;
+    v.fq_out = fq + (size_t)out * (lbm::kQf - 1) * n * c->esz;
+    v.g = c->st.g;
+    v.mom = c->st.mom;
+    return v;
+}
+
+// Stats reduction of the mom arrays into c->result_host (synchronises).
+int reduce_stats(lbm_ctx *c)
+{
+    cudaError_t e = lbm::launch_stats(c->box, c->d, c->st.mom, c->partials, c->partial_count, c->result, nullptr,
+                                      c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "stats kernel launch");
+    LBM_CUDA(cudaMemcpyAsync(c->result_host, c->result, sizeof(double) * lbm::kStatsValues, cudaMemcpyDeviceToHost,
+                             c->stream),
+             "stats copy");
+    LBM_CUDA(cudaStreamSynchronize(c->stream), "stats");
+    return LBM_OK;
+}
+
+// Load streamed FP32 distributions tf (7 x n) and tg (19 x n) into the state
+// (half 0, natural g layout), choosing the 16-bit storage map from the data.
+// c->st.mom must already hold the fields (for the mean density).
+int load_state(lbm_ctx *c, const float *tf, const float *tg)
+{
+    identity_quant(c->q);
+    if (c->p.storage != LBM_STORAGE_FP32) {
+        int rc = reduce_stats(c);
+        if (rc) return rc;
+        const double rho_mean = c->result_host[8] / (double)c->box.n;
+        float shift[lbm::kQg];
+        for (int i = 0; i < lbm::kQg; i++) shift[i] = (float)(kW[i] * rho_mean);
+        float *shift_dev = nullptr;
+        unsigned *bits_dev = nullptr;
+        unsigned bits[lbm::kQf + lbm::kQg];
+        cudaError_t e = cudaMalloc(&shift_dev, sizeof(shift));
+        if (e == cudaSuccess) e = cudaMalloc(&bits_dev, sizeof(bits));
+        if (e == cudaSuccess) e = cudaMemcpyAsync(shift_dev, shift, sizeof(shift), cudaMemcpyHostToDevice, c->stream);
+        if (e == cudaSuccess) e = lbm::launch_field_maxabs(c->box, tf, tg, shift_dev, bits_dev, c->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(bits, bits_dev, sizeof(bits), cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        cudaFree(shift_dev);
+        cudaFree(bits_dev);
+        if (e != cudaSuccess) return cuda_fail(e, "storage map");
+        // Scales: powers of two that put a generous bound on each field at
+        // 2^12, leaving 16x headroom below the FP16 maximum (65504).  The bound
+        // covers the flow developing later: |u| up to 0.1 moves g_i by about
+        // 3 w_i rho |u| and f_i by about phiStar |u| / (tauPhi (1 - eta)).
+        // BF16 has the FP32 exponent range and keeps scale 1.
+        const bool fp16 = c->p.storage == LBM_STORAGE_FP16;
+        auto pick = [&](float maxabs, double bound) -> float {
+            double m = std::max((double)maxabs, bound);
+            if (!fp16 || !(m > 0.0) || !std::isfinite(m)) return 1.f;
+            int ex = (int)std::floor(std::log2(4096.0 / m));
+            ex = std::max(-60, std::min(60, ex));
+            return std::ldexp(1.f, ex);
+        };
+        const double fbound = 0.1 * std::fabs((double)c->d.phiStar) * c->d.invTauPhi * c->d.invEta2;
+        for (int a = 0; a < lbm::kQf - 1; a++) {
+            float m;
+            std::memcpy(&m, &bits[a + 1], sizeof(float));
+            c->q.f_scale[a] = pick(m, fbound);
+            c->q.f_inv[a] = 1.f / c->q.f_scale[a];
+        }
+        for (int i = 0; i < lbm::kQg; i++) {
+            float m;
+            std::memcpy(&m, &bits[lbm::kQf + i], sizeof(float));
+            c->q.g_shift[i] = shift[i];
+            c->q.g_scale[i] = pick(m, 0.3 * kW[i] * std::fabs(rho_mean));
+            c->q.g_inv[i] = 1.f / c->q.g_scale[i];
+        }
+    }
+    lbm::StepView v = view(c, 0);
+    LBM_CUDA(lbm::launch_quantize(c->box, c->q, c->p.storage, tf, tg, c->st.f0, const_cast<void *>(v.fq_in),
+                                  c->st.g, c->stream),
+             "quantize kernel");
+    LBM_CUDA(cudaStreamSynchronize(c->stream), "load state");
     c->st.f_cur = 0;
     c->st.f_streamed = true;
-    c->st.steps = 0;
-    c->g_odd_next = false;
-    LBM_CUDA(cudaStreamSynchronize(c->stream), "initialisation");
+    c->st.g_odd_next = false;
     return LBM_OK;
+}
+
+// Equilibrium from the fields in c->st.mom into the state.
+int init_from_mom(lbm_ctx *c, const float *ghost_lo, const float *ghost_hi)
+{
+    const size_t n = (size_t)c->box.n;
+    float *tmp = nullptr;
+    LBM_CUDA(cudaMalloc(&tmp, sizeof(float) * (lbm::kQf + lbm::kQg) * n), "init scratch");
+    cudaError_t e = lbm::launch_equilibrium(c->box, c->d, c->p.Gamma, c->st.mom, c->st.mom + n, ghost_lo, ghost_hi,
+                                            tmp, tmp + lbm::kQf * n, c->stream);
+    int rc = e == cudaSuccess ? load_state(c, tmp, tmp + lbm::kQf * n) : cuda_fail(e, "equilibrium kernel");
+    cudaStreamSynchronize(c->stream);
+    cudaFree(tmp);
+    c->st.steps = 0;
+    return rc;
 }
 
 }  // namespace
@@ -125,11 +239,6 @@ extern "C" int lbm_init(lbm_ctx **out, const lbm_params *p, const float *phi0, c
     const size_t n = (size_t)c->box.n, bytes = sizeof(float) * n;
     float *mom = c->st.mom;
     float *ghost = nullptr;
-    auto bail = [&](cudaError_t e, const char *what) {
-        if (ghost) cudaFree(ghost);
-        lbm_destroy(c);
-        return cuda_fail(e, what);
-    };
     cudaError_t e = cudaMemcpyAsync(mom, phi0, bytes, cudaMemcpyHostToDevice, c->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(mom + n, rho0, bytes, cudaMemcpyHostToDevice, c->stream);
     const float *u[3] = {ux0, uy0, uz0};
@@ -142,13 +251,14 @@ extern "C" int lbm_init(lbm_ctx **out, const lbm_params *p, const float *phi0, c
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(ghost, phi_ghost, sizeof(float) * 2 * c->box.nxy, cudaMemcpyHostToDevice, c->stream);
     }
-    if (e == cudaSuccess)
-        e = lbm::launch_equilibrium(c->box, c->d, c->p.Gamma, mom, mom + n, ghost, ghost ? ghost + c->box.nxy : nullptr,
-                                    f_half(c, 0), c->st.g, c->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-    if (e != cudaSuccess) return bail(e, "lbm_init");
+    if (e != cudaSuccess) {
+        cudaStreamSynchronize(c->stream);
+        if (ghost) cudaFree(ghost);
+        lbm_destroy(c);
+        return cuda_fail(e, "lbm_init");
+    }
+    rc = init_from_mom(c, ghost, ghost ? ghost + c->box.nxy : nullptr);
     if (ghost) cudaFree(ghost);
-    rc = finish_init(c);
     if (rc) {
         lbm_destroy(c);
         return rc;
@@ -176,17 +286,10 @@ extern "C" int lbm_init_bubbles(lbm_ctx **out, const lbm_params *p, const float 
         e = cudaMemcpyAsync(mom, phig + nxy, sizeof(float) * n, cudaMemcpyDeviceToDevice, c->stream);
     if (e == cudaSuccess) e = lbm::launch_fill(mom + n, (long long)n, 0.5f * (c->p.rhoH + c->p.rhoL), c->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(mom + 2 * n, 0, sizeof(float) * 3 * n, c->stream);
-    if (e == cudaSuccess)
-        e = lbm::launch_equilibrium(c->box, c->d, c->p.Gamma, mom, mom + n, phig, phig + nxy * (c->box.nz + 1),
-                                    f_half(c, 0), c->st.g, c->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    rc = e == cudaSuccess ? init_from_mom(c, phig, phig + nxy * (c->box.nz + 1)) : cuda_fail(e, "lbm_init_bubbles");
+    cudaStreamSynchronize(c->stream);
     if (phig) cudaFree(phig);
     if (bub) cudaFree(bub);
-    if (e != cudaSuccess) {
-        lbm_destroy(c);
-        return cuda_fail(e, "lbm_init_bubbles");
-    }
-    rc = finish_init(c);
     if (rc) {
         lbm_destroy(c);
         return rc;
@@ -202,13 +305,13 @@ extern "C" int lbm_step(lbm_ctx *c, int nsteps, float grav)
     if (!std::isfinite(grav)) return fail(LBM_EINVAL, "grav is not finite");
     const lbm::StepConst k = lbm::step_const(c->d, c->p, grav);
     for (int s = 0; s < nsteps; s++) {
-        const int in = c->st.f_cur, outh = 1 - in;
-        cudaError_t e = lbm::launch_step(c->box, k, f_half(c, in), f_half(c, outh), c->st.g, c->st.mom,
-                                         c->st.f_streamed, c->g_odd_next, s == nsteps - 1, c->stream);
+        const int in = c->st.f_cur;
+        cudaError_t e = lbm::launch_step(c->box, k, c->q, view(c, in), c->st.f_streamed, c->st.g_odd_next,
+                                         s == nsteps - 1, c->stream);
         if (e != cudaSuccess) return cuda_fail(e, "step kernel launch");
-        c->st.f_cur = outh;
+        c->st.f_cur = 1 - in;
         c->st.f_streamed = false;
-        c->g_odd_next = !c->g_odd_next;
+        c->st.g_odd_next = !c->st.g_odd_next;
         c->st.steps++;
     }
     return LBM_OK;
@@ -269,8 +372,8 @@ extern "C" int lbm_get_dist(lbm_ctx *c, float *f, float *g)
     LBM_CUDA(cudaMalloc(&tmp, sizeof(float) * count * n), "lbm_get_dist scratch");
     float *tf = f ? tmp : nullptr;
     float *tg = g ? tmp + (f ? lbm::kQf * n : 0) : nullptr;
-    cudaError_t e = lbm::launch_stream_out(c->box, c->d.eta, f_half(c, c->st.f_cur), c->st.f_streamed, c->st.g,
-                                           c->g_odd_next, tf, tg, c->stream);
+    cudaError_t e = lbm::launch_stream_out(c->box, c->d.eta, c->q, view(c, c->st.f_cur), c->st.f_streamed,
+                                           c->st.g_odd_next, tf, tg, c->stream);
     if (e == cudaSuccess && f)
         e = cudaMemcpyAsync(f, tf, sizeof(float) * lbm::kQf * n, cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess && g)
@@ -286,16 +389,16 @@ extern "C" int lbm_set_dist(lbm_ctx *c, const float *f, const float *g)
     if (!c || !f || !g) return fail(LBM_EINVAL, "NULL argument");
     const size_t n = (size_t)c->box.n;
     LBM_CUDA(cudaStreamSynchronize(c->stream), "lbm_set_dist");
-    LBM_CUDA(cudaMemcpyAsync(f_half(c, 0), f, sizeof(float) * lbm::kQf * n, cudaMemcpyHostToDevice, c->stream),
-             "lbm_set_dist f");
-    LBM_CUDA(cudaMemcpyAsync(c->st.g, g, sizeof(float) * lbm::kQg * n, cudaMemcpyHostToDevice, c->stream),
-             "lbm_set_dist g");
-    LBM_CUDA(lbm::launch_moments(c->box, f_half(c, 0), c->st.g, c->st.mom, c->stream), "moments kernel");
-    LBM_CUDA(cudaStreamSynchronize(c->stream), "lbm_set_dist");
-    c->st.f_cur = 0;
-    c->st.f_streamed = true;
-    c->g_odd_next = false;
-    return LBM_OK;
+    float *tmp = nullptr;
+    LBM_CUDA(cudaMalloc(&tmp, sizeof(float) * (lbm::kQf + lbm::kQg) * n), "lbm_set_dist scratch");
+    float *tf = tmp, *tg = tmp + lbm::kQf * n;
+    cudaError_t e = cudaMemcpyAsync(tf, f, sizeof(float) * lbm::kQf * n, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(tg, g, sizeof(float) * lbm::kQg * n, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = lbm::launch_moments(c->box, tf, tg, c->st.mom, c->stream);
+    const int rc = e == cudaSuccess ? load_state(c, tf, tg) : cuda_fail(e, "lbm_set_dist");
+    cudaStreamSynchronize(c->stream);
+    cudaFree(tmp);
+    return rc;
 }
 
 extern "C" long long lbm_steps_done(const lbm_ctx *c) { return c ? c->st.steps : -1; }
@@ -314,7 +417,8 @@ extern "C" void lbm_destroy(lbm_ctx *c)
     if (!c) return;
     cudaSetDevice(c->p.device);
     if (c->stream) cudaStreamSynchronize(c->stream);
-    cudaFree(c->st.f);
+    cudaFree(c->st.f0);
+    cudaFree(c->st.fq);
     cudaFree(c->st.g);
     cudaFree(c->st.mom);
     cudaFree(c->partials);

@@ -33,27 +33,46 @@ struct Box {
     long long nxy, n;
 };
 
-// Device buffers of one context.
-//  f      : 2 x 7 x n   post-collision D3Q7 values (A/B by step parity), or the
-//           streamed initial values while `f_streamed` is set
-//  g      : 19 x n      D3Q19 values in the in-place AA layout
-//  mom    : 5 x n       phi, rho, ux, uy, uz as the reference's arrays hold them
-struct State {
-    float *f = nullptr;
-    float *g = nullptr;
-    float *mom = nullptr;
-    int f_cur = 0;            // which half of f holds the current values
-    bool f_streamed = true;   // f holds streamed (not post-collision) values
-    long long steps = 0;      // steps since init; AA parity = steps & 1
+// Per-field affine map of the 16-bit storage formats:
+//   stored = (value - shift) * scale,   value = stored * inv + shift.
+// scale is a power of two (exact); shift is w_i * mean(rho) for g and 0 for f.
+// For FP32 storage the map is the identity and is not applied.
+struct Quant {
+    float f_scale[kQf - 1], f_inv[kQf - 1];          // f_1 .. f_6
+    float g_scale[kQg], g_inv[kQg], g_shift[kQg];
 };
 
-// Scratch for reductions (per-block partials), owned by the context.
-struct Scratch {
-    double *partials = nullptr;
-    size_t partial_count = 0;
-    double *result = nullptr;      // final reduced values
-    unsigned long long *counters = nullptr;
+// Device buffers of one context (element type of fq and g: the storage type,
+// float / __half / __nv_bfloat16):
+//  f0     : 2 x n floats        D3Q7 rest population, A/B
+//  fq     : 2 x 6 x n           D3Q7 f_1..f_6, A/B
+//  g      : 19 x n              D3Q19 in the in-place AA layout
+//  mom    : 5 x n floats        phi, rho, ux, uy, uz as the reference's arrays hold them
+// f holds post-collision values, except right after init / lbm_set_dist
+// (f_streamed), when it holds streamed values.
+struct State {
+    float *f0 = nullptr;
+    void *fq = nullptr;
+    void *g = nullptr;
+    float *mom = nullptr;
+    int f_cur = 0;            // which half of f0 / fq holds the current values
+    bool f_streamed = true;
+    bool g_odd_next = false;  // the next step reads g in the AA "odd" layout
+    long long steps = 0;
 };
+
+// The state buffers one step reads and writes.
+struct StepView {
+    int storage;              // LBM_STORAGE_*
+    const float *f0_in;
+    float *f0_out;
+    const void *fq_in;        // 6 arrays of n elements
+    void *fq_out;
+    void *g;                  // 19 arrays of n elements
+    float *mom;
+};
+
+size_t storage_bytes(int storage);   // bytes per element of fq / g
 
 void set_error(const std::string &msg);
 const std::string &last_error();
@@ -62,16 +81,24 @@ const std::string &last_error();
 void derive(const lbm_params &p, lbm_derived &d);
 StepConst step_const(const lbm_derived &d, const lbm_params &p, float grav);
 
-// Kernel launchers (defined in the .cu files); all return cudaError_t of the launch.
+// Kernel launchers (defined in the .cu files); all return the cudaError_t of the launch.
 cudaError_t launch_bubble_phi(const Box &b, const float *bubbles_dev, int nbubbles, float phiStar, float width,
                               float *phi_ghosted, cudaStream_t s);
+// At-rest equilibrium into FP32 arrays f (7 x n) and g (19 x n), streamed layout.
 cudaError_t launch_equilibrium(const Box &b, const lbm_derived &d, float Gamma, const float *phi, const float *rho,
                                const float *ghost_lo, const float *ghost_hi, float *f, float *g, cudaStream_t s);
 cudaError_t launch_fill(float *p, long long n, float v, cudaStream_t s);
-cudaError_t launch_step(const Box &b, const StepConst &c, const float *f_in, float *f_out, float *g, float *mom,
-                        bool f_streamed, bool odd, bool write_moments, cudaStream_t s);
-cudaError_t launch_stream_out(const Box &b, float eta, const float *f_state, bool f_streamed, const float *g,
-                              bool odd, float *f_out, float *g_out, cudaStream_t s);
+cudaError_t launch_step(const Box &b, const StepConst &c, const Quant &q, const StepView &v, bool f_streamed,
+                        bool odd, bool write_moments, cudaStream_t s);
+// State (post-collision / AA layout, any storage) -> streamed FP32 f (7 x n) and g (19 x n).
+cudaError_t launch_stream_out(const Box &b, float eta, const Quant &q, const StepView &v, bool f_streamed, bool odd,
+                              float *f_out, float *g_out, cudaStream_t s);
+// Streamed FP32 f, g -> state half 0 (natural layout), applying the storage map.
+cudaError_t launch_quantize(const Box &b, const Quant &q, int storage, const float *f, const float *g, float *f0,
+                            void *fq, void *gq, cudaStream_t s);
+// Per-field max |x - shift| of the 7 f and 19 g FP32 arrays (26 floats at out, device).
+cudaError_t launch_field_maxabs(const Box &b, const float *f, const float *g, const float *g_shift_dev,
+                                unsigned *out_bits, cudaStream_t s);
 cudaError_t launch_moments(const Box &b, const float *f, const float *g, float *mom, cudaStream_t s);
 cudaError_t launch_stats(const Box &b, const lbm_derived &d, const float *mom, double *partials,
                          size_t partial_count, double *result, unsigned long long *counters, cudaStream_t s);

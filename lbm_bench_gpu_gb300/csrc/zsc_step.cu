@@ -16,23 +16,30 @@
 //    the reversed slots of the upstream neighbours and write the downstream
 //    neighbours' natural slots.  Each thread reads and writes the same 19
 //    locations, so the update is race-free in one buffer.
+//  * Storage type ST of f_1..f_6 and g: float, or __half / __nv_bfloat16 with a
+//    per-field affine map (stored = (value - shift) * scale; shift = w_i mean(rho)
+//    for g).  f_0 ~ phi is bimodal (+-phiStar), so no shift centres it: it stays
+//    FP32 in every format.  Arithmetic is FP32 throughout.
 //
 // Work decomposition: a block owns a TX x TY column tile and marches a chunk
-// of TZ planes in z.  The phi stencil (19-point Laplacian and gradient,
+// of tz planes in z.  The phi stencil (19-point Laplacian and gradient,
 // src/collision_f.cu:61-94) needs phi on a one-node ring around the tile, and
 // phi = sum f needs P^{n-1} one node further out, so each plane of P^{n-1} is
-// staged in shared memory on the tile plus two halo rows and four halo columns.
+// staged in shared memory on the tile plus two halo rows and one 16-byte
+// chunk of halo columns on each side.
 //
 // Memory pipeline: every global read goes through cp.async (16-byte chunks,
 // L2-cached, no registers held while in flight) into shared-memory stages:
-//   - the 19 g rows of the next plane (2 stages; odd steps stage 36-wide rows
-//     so the +-x shifted reads stay 16-byte aligned),
+//   - the 19 g rows of the next plane (2 stages; odd steps stage one extra
+//     chunk per row so the +-x shifted reads stay 16-byte aligned),
 //   - the 7 P_f planes three planes ahead (4 stages),
 // so a block always has about one plane of the step's input in flight while it
-// computes the current plane.  Periodic wrap is applied per 16-byte chunk: with
-// nx a multiple of 32 no chunk straddles the seam.  DRAM sees each
-// distribution once per step (26 x 8 B = 208 B per node in FP32); the halo
-// re-reads of neighbouring tiles are served by L2.
+// computes the current plane.  Warps 0-3 queue P_f, warps 4-7 queue g, each
+// thread with chunk coordinates fixed for the whole block.  Periodic wrap is
+// applied per chunk: with nx a multiple of 32 no chunk straddles the seam.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
 #include "lbm_internal.h"
 
 namespace lbm {
@@ -47,19 +54,16 @@ namespace {
 constexpr int TX = 32;              // tile width in x (one warp per row)
 constexpr int TY = ZSC_TILE_Y;      // tile height in y
 constexpr int NT = TX * TY;         // threads per block
-constexpr int GW = 40;              // staged row width: x in [x0 - 4, x0 + 36)
 constexpr int FR = TY + 4;          // staged P_f rows: y in [y0 - 2, y0 + TY + 2)
+constexpr int W0 = TX + 8;          // staged f_0 row (floats): x in [x0 - 4, x0 + 36)
 constexpr int RW = TX + 2;          // phi ring width (tile + one-node ring)
 constexpr int RH = TY + 2;
 constexpr int RING = 2 * RW + 2 * TY;
 constexpr int NG = 2;               // g stages
 constexpr int NF = 4;               // P_f stages
 constexpr int NPHI = 4;             // phi planes
-constexpr int G_STAGE = kQg * TY * GW;
-constexpr int F_STAGE = kQf * FR * GW;
-constexpr int PHI_STAGE = RH * RW;
-constexpr size_t kSmemBytes = sizeof(float) * (NG * G_STAGE + NF * F_STAGE + NPHI * PHI_STAGE);
 static_assert(RING <= NT, "one ring node per thread at most");
+static_assert(TX == 32 && TY == 8, "issuer roles assume a 32 x 8 tile");
 
 constexpr float kInv6 = 0.16666666666666666667f;
 constexpr float kInv12 = 0.08333333333333333333f;
@@ -87,31 +91,59 @@ struct Dir {
     static constexpr int value = I;
 };
 
+// Storage formats: element conversions.
+template <typename ST>
+struct Fmt;
+template <>
+struct Fmt<float> {
+    static constexpr bool kMapped = false;
+    __device__ static float load(float v) { return v; }
+    __device__ static float store(float v) { return v; }
+};
+template <>
+struct Fmt<__half> {
+    static constexpr bool kMapped = true;
+    __device__ static float load(__half v) { return __half2float(v); }
+    __device__ static __half store(float v) { return __float2half_rn(v); }
+};
+template <>
+struct Fmt<__nv_bfloat16> {
+    static constexpr bool kMapped = true;
+    __device__ static float load(__nv_bfloat16 v) { return __bfloat162float(v); }
+    __device__ static __nv_bfloat16 store(float v) { return __float2bfloat16_rn(v); }
+};
+
+// Staging geometry implied by the element size.
+template <typename ST>
+struct Geo {
+    static constexpr int E = 16 / (int)sizeof(ST);   // elements per 16-byte chunk
+    static constexpr int W = TX + 2 * E;             // staged row: x in [x0 - E, x0 + TX + E)
+    static constexpr int CR = W / E;                 // chunks per staged row
+    static constexpr int CM = TX / E;                // chunks covering [x0, x0 + TX)
+    static constexpr int G_STAGE = kQg * TY * W * (int)sizeof(ST);            // bytes
+    static constexpr int F0_BYTES = FR * W0 * 4;
+    static constexpr int F_STAGE = F0_BYTES + (kQf - 1) * FR * W * (int)sizeof(ST);
+    static constexpr int PHI_STAGE = RH * RW * 4;
+    static constexpr int G_OFF = 0;
+    static constexpr int F_OFF = NG * G_STAGE;
+    static constexpr int PHI_OFF = F_OFF + NF * F_STAGE;
+    static constexpr int SMEM = PHI_OFF + NPHI * PHI_STAGE;
+    static constexpr int TPD = TY * CM;              // g issuer threads per direction
+    static constexpr int D = (NT / 2) / TPD;         // directions per pass of the g issuers
+    static_assert(G_STAGE % 16 == 0 && F_STAGE % 16 == 0 && F0_BYTES % 16 == 0, "16-byte aligned stages");
+    static_assert(FR * (W0 / 4) <= NT / 2 && FR * CR <= NT / 2, "P_f issuers fit in warps 0-3");
+    static_assert(D * TPD == NT / 2, "g issuers cover whole directions");
+};
+
+template <typename ST>
 struct StepPtrs {
-    const float *fin[kQf];
-    float *fout[kQf];
-    float *g[kQg];
+    const float *f0in;
+    float *f0out;
+    const ST *fin[kQf - 1];   // f_1 .. f_6
+    ST *fout[kQf - 1];
+    ST *g[kQg];
     float *mom[5];
 };
-
-// Offsets (in elements, within one array) from a node to its periodic
-// neighbours.
-struct Nbr {
-    int xm, xp, ym, yp, zm, zp;
-};
-
-__device__ __forceinline__ Nbr neighbours(const Box &b, int x, int y, int z)
-{
-    Nbr o;
-    o.xm = (x == 0) ? b.nx - 1 : -1;
-    o.xp = (x == b.nx - 1) ? -(b.nx - 1) : 1;
-    o.ym = (y == 0) ? (b.ny - 1) * b.nx : -b.nx;
-    o.yp = (y == b.ny - 1) ? -(b.ny - 1) * b.nx : b.nx;
-    const int nxy = (int)b.nxy;
-    o.zm = (z == 0) ? (b.nz - 1) * nxy : -nxy;
-    o.zp = (z == b.nz - 1) ? -(b.nz - 1) * nxy : nxy;
-    return o;
-}
 
 __device__ __forceinline__ unsigned node_index(const Box &b, int x, int y, int z)
 {
@@ -121,7 +153,7 @@ __device__ __forceinline__ unsigned node_index(const Box &b, int x, int y, int z
 __device__ __forceinline__ int wrap(int a, int n) { return a < 0 ? a + n : (a >= n ? a - n : a); }
 
 // 16-byte global -> shared copy, cached in L2 only; completes asynchronously.
-__device__ __forceinline__ void cp_async16(float *smem, const float *gmem)
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
 {
     const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
@@ -129,14 +161,29 @@ __device__ __forceinline__ void cp_async16(float *smem, const float *gmem)
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
-template <bool STREAMED, bool ODD>
-__global__ void __launch_bounds__(NT, ZSC_MIN_BLOCKS)
-zsc_step_kernel(const StepPtrs P, const Box b, const StepConst c, const int tz, const int write_moments)
+// f(Dir<i>) for i = I, I + D, I + 2D, ... < 19
+template <int I, int D, typename F>
+__device__ __forceinline__ void for_dirs_from(F &&f)
 {
-    extern __shared__ __align__(16) float smem[];
-    float *const G = smem;                    // [NG][19][TY][GW]
-    float *const F = G + NG * G_STAGE;        // [NF][7][FR][GW]
-    float *const PHI = F + NF * F_STAGE;      // [NPHI][RH][RW]
+    if constexpr (I < kQg) {
+        f(Dir<I>{});
+        for_dirs_from<I + D, D>(f);
+    }
+}
+
+template <typename ST, bool STREAMED, bool ODD>
+__global__ void __launch_bounds__(NT, ZSC_MIN_BLOCKS)
+zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Quant q, const int tz,
+                const int write_moments)
+{
+    using Gm = Geo<ST>;
+    using Fm = Fmt<ST>;
+    constexpr int E = Gm::E, W = Gm::W, CR = Gm::CR, CM = Gm::CM;
+    extern __shared__ __align__(16) unsigned char smem[];
+    ST *const G = reinterpret_cast<ST *>(smem + Gm::G_OFF);            // [NG][19][TY][W]
+    unsigned char *const F = smem + Gm::F_OFF;                          // [NF]{f0 [FR][W0]; fq [6][FR][W]}
+    float *const PHI = reinterpret_cast<float *>(smem + Gm::PHI_OFF);   // [NPHI][RH][RW]
+    constexpr int G_ELEMS = kQg * TY * W;                               // per stage
 
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int tid = ty * TX + tx;
@@ -169,56 +216,68 @@ zsc_step_kernel(const StepPtrs P, const Box b, const StepConst c, const int tz, 
         rly = tid - 2 * RW - TY + 1;
     }
 
-    // P_f stage of plane p (p >= z0 - 2)
-    auto fslot = [&](int p) { return F + ((p - z0 + 4) & (NF - 1)) * F_STAGE; };
+    // P_f stage of plane p (p >= z0 - 2): f_0 part and f_1..f_6 part
+    auto fstage = [&](int p) { return F + ((p - z0 + 4) & (NF - 1)) * Gm::F_STAGE; };
+    auto f0part = [&](unsigned char *st) { return reinterpret_cast<float *>(st); };
+    auto fqpart = [&](unsigned char *st) { return reinterpret_cast<ST *>(st + Gm::F0_BYTES); };
 
     // ---- staging roles, fixed per thread for the whole chunk ----
-    // Warps 0-3 queue the 7 P_f planes: thread t < FR * GW/4 owns staged row
-    // t / (GW/4), 16-byte chunk t % (GW/4), of every array.
-    constexpr int kFChunks = FR * (GW / 4);
-    static_assert(kFChunks <= NT / 2, "P_f issuers fit in the first half of the block");
-    const bool f_issuer = tid < kFChunks;
-    int f_xy = 0, f_dst = 0;
-    if (f_issuer) {
-        const int r = tid / (GW / 4), k = tid - r * (GW / 4);
-        f_xy = wrap(x0 - 4 + 4 * k, b.nx) + b.nx * wrap(y0 - 2 + r, b.ny);
-        f_dst = r * GW + 4 * k;
+    // Warps 0-3 queue P_f: thread t owns staged row t / (chunks per row), chunk
+    // t % (chunks per row), of f_0 (FP32 geometry) and of f_1..f_6 (ST geometry).
+    const bool f0_issuer = tid < FR * (W0 / 4);
+    const bool fq_issuer = tid < FR * CR;
+    int f0_xy = 0, f0_dst = 0, fq_xy = 0, fq_dst = 0;
+    if (f0_issuer) {
+        const int r = tid / (W0 / 4), k = tid - r * (W0 / 4);
+        f0_xy = wrap(x0 - 4 + 4 * k, b.nx) + b.nx * wrap(y0 - 2 + r, b.ny);
+        f0_dst = r * W0 + 4 * k;
     }
-    // Warps 4-7 queue the g rows: thread owns row g_r, chunk g_k of every
-    // second direction (g_hi: odd or even directions; uniform per warp).
-    static_assert(TX == 32 && TY == 8, "g issuer mapping: 8 rows x 8 chunks per direction, two halves");
+    if (fq_issuer) {
+        const int r = tid / CR, k = tid - r * CR;
+        fq_xy = wrap(x0 - E + E * k, b.nx) + b.nx * wrap(y0 - 2 + r, b.ny);
+        fq_dst = r * W + E * k;
+    }
+    // Warps 4-7 queue the g rows: thread owns row g_r, chunk g_k of every D-th
+    // direction starting at g_q (uniform per warp).
     const int gt = tid - NT / 2;
     const bool g_issuer = gt >= 0;
-    const int g_hi = (gt >> 6) & 1;
-    const int g_r = (gt & 63) >> 3, g_k = gt & 7;
+    const int g_q = gt / Gm::TPD;
+    const int g_r = (gt % Gm::TPD) / CM, g_k = gt % CM;
     int g_row_0 = 0, g_row_p = 0, g_row_m = 0, g_x_lo = 0, g_x_hi = 0, g_x_wrap = 0;
     if (g_issuer) {
         g_row_0 = b.nx * (y0 + g_r);
         g_row_p = b.nx * wrap(y0 + g_r - 1, b.ny);   // directions with c_y = +1 read row y - 1
         g_row_m = b.nx * wrap(y0 + g_r + 1, b.ny);   // c_y = -1 reads row y + 1
-        g_x_lo = wrap(x0 - 4 + 4 * g_k, b.nx);        // c_x = +1 reads x - 1: chunks from x0 - 4
-        g_x_hi = x0 + 4 * g_k;                         // c_x <= 0: chunks from x0
-        g_x_wrap = wrap(x0 + TX, b.nx);                // c_x = -1 also needs x0 + 32
+        g_x_lo = wrap(x0 - E + E * g_k, b.nx);        // c_x = +1 reads x - 1: chunks from x0 - E
+        g_x_hi = x0 + E * g_k;                         // c_x <= 0: chunks from x0
+        g_x_wrap = wrap(x0 + TX, b.nx);                // c_x = -1 also needs x0 + TX
     }
 
     // Queue the 7 P_f planes of plane p (tile + halo) into its stage.
     auto issue_f = [&](int p) {
-        if (!f_issuer) return;
-        const unsigned base = (unsigned)wrap(p, b.nz) * (unsigned)b.nxy + (unsigned)f_xy;
-        float *dst = fslot(p) + f_dst;
+        const unsigned zb = (unsigned)wrap(p, b.nz) * (unsigned)b.nxy;
+        unsigned char *st = fstage(p);
+        if (f0_issuer) cp_async16(f0part(st) + f0_dst, P.f0in + (zb + (unsigned)f0_xy));
+        if (fq_issuer) {
+            ST *dst = fqpart(st) + fq_dst;
+            const unsigned base = zb + (unsigned)fq_xy;
 #pragma unroll
-        for (int arr = 0; arr < kQf; arr++) cp_async16(dst + arr * FR * GW, P.fin[arr] + base);
+            for (int a = 0; a < kQf - 1; a++) cp_async16(dst + a * FR * W, P.fin[a] + base);
+        }
     };
 
-    // Call f(direction) for the directions this g issuer owns (compile-time
+    // Call f(Dir<i>) for the directions this g issuer owns (compile-time
     // direction numbers; the branch is uniform per warp).
     auto for_my_dirs = [&](auto &&f) {
-        if (g_hi == 0) {
-            f(Dir<0>{}); f(Dir<2>{}); f(Dir<4>{}); f(Dir<6>{}); f(Dir<8>{});
-            f(Dir<10>{}); f(Dir<12>{}); f(Dir<14>{}); f(Dir<16>{}); f(Dir<18>{});
+        if constexpr (Gm::D == 2) {
+            if (g_q == 0) for_dirs_from<0, 2>(f);
+            else for_dirs_from<1, 2>(f);
         } else {
-            f(Dir<1>{}); f(Dir<3>{}); f(Dir<5>{}); f(Dir<7>{}); f(Dir<9>{});
-            f(Dir<11>{}); f(Dir<13>{}); f(Dir<15>{}); f(Dir<17>{});
+            static_assert(Gm::D == 4, "two or four directions per pass");
+            if (g_q == 0) for_dirs_from<0, 4>(f);
+            else if (g_q == 1) for_dirs_from<1, 4>(f);
+            else if (g_q == 2) for_dirs_from<2, 4>(f);
+            else for_dirs_from<3, 4>(f);
         }
     };
 
@@ -227,12 +286,12 @@ zsc_step_kernel(const StepPtrs P, const Box b, const StepConst c, const int tz, 
     // from the reversed slot of x - c_i (AA pattern).
     auto issue_g = [&](int z, int s) {
         if (!g_issuer) return;
-        float *dst = G + s * G_STAGE + g_r * GW;
+        ST *dst = G + s * G_ELEMS + g_r * W;
         if (!ODD) {
             const unsigned base = (unsigned)z * (unsigned)b.nxy + (unsigned)(g_row_0 + g_x_hi);
             for_my_dirs([&](auto d) {
                 constexpr int i = decltype(d)::value;
-                cp_async16(dst + i * TY * GW + 4 + 4 * g_k, P.g[i] + base);
+                cp_async16(dst + i * TY * W + E + E * g_k, P.g[i] + base);
             });
         } else {
             const unsigned zb0 = (unsigned)z * (unsigned)b.nxy;
@@ -243,14 +302,14 @@ zsc_step_kernel(const StepPtrs P, const Box b, const StepConst c, const int tz, 
                 constexpr int cx = kCx(i), cy = kCy(i), cz = kCz(i);
                 const unsigned zb = cz > 0 ? zbp : (cz < 0 ? zbm : zb0);
                 const int row = cy > 0 ? g_row_p : (cy < 0 ? g_row_m : g_row_0);
-                const float *src = P.g[kOpp(i)] + (zb + (unsigned)row);
-                float *d_row = dst + i * TY * GW;
+                const ST *src = P.g[kOpp(i)] + (zb + (unsigned)row);
+                ST *d_row = dst + i * TY * W;
                 if (cx > 0) {
-                    cp_async16(d_row + 4 * g_k, src + g_x_lo);
-                    if (g_k == 0) cp_async16(d_row + 32, src + (x0 + 28));
+                    cp_async16(d_row + E * g_k, src + g_x_lo);
+                    if (g_k == 0) cp_async16(d_row + TX, src + (x0 + TX - E));
                 } else {
-                    cp_async16(d_row + 4 + 4 * g_k, src + g_x_hi);
-                    if (cx < 0 && g_k == 0) cp_async16(d_row + 36, src + g_x_wrap);
+                    cp_async16(d_row + E + E * g_k, src + g_x_hi);
+                    if (cx < 0 && g_k == 0) cp_async16(d_row + TX + E, src + g_x_wrap);
                 }
             });
         }
@@ -259,22 +318,27 @@ zsc_step_kernel(const StepPtrs P, const Box b, const StepConst c, const int tz, 
     // Streamed D3Q7 values at ring-tile position (lx, ly) of plane p and their
     // sum phi (src/update_phi.cu:42-43), from the staged planes.
     auto phi_at = [&](int p, int lx, int ly, float(&f)[kQf]) -> float {
-        const int col = lx + 3, row = ly + 1;
-        const float *S1 = fslot(p);
-        auto at = [&](const float *S, int arr, int rr, int cc) { return S[(arr * FR + rr) * GW + cc]; };
+        const int row = ly + 1;
+        const int c0 = lx + 3;          // f_0 column: x - (x0 - 4)
+        const int cq = lx - 1 + E;      // f_1..f_6 column: x - (x0 - E)
+        unsigned char *S1 = fstage(p);
+        auto fq = [&](unsigned char *S, int a, int rr, int cc) {
+            const float v = Fm::load(fqpart(S)[(a * FR + rr) * W + cc]);
+            if constexpr (Fm::kMapped) return v * q.f_inv[a]; else return v;
+        };
+        f[0] = f0part(S1)[row * W0 + c0];
         if (STREAMED) {
 #pragma unroll
-            for (int i = 0; i < kQf; i++) f[i] = at(S1, i, row, col);
+            for (int a = 0; a < kQf - 1; a++) f[a + 1] = fq(S1, a, row, cq);
         } else {
-            const float *S0 = fslot(p - 1), *S2 = fslot(p + 1);
+            unsigned char *S0 = fstage(p - 1), *S2 = fstage(p + 1);
             const float eta = c.eta, eta2 = c.eta2;
-            f[0] = at(S1, 0, row, col);
-            f[1] = eta * at(S1, 1, row, col - 1) + eta2 * at(S1, 1, row, col);
-            f[2] = eta * at(S1, 2, row, col + 1) + eta2 * at(S1, 2, row, col);
-            f[3] = eta * at(S1, 3, row - 1, col) + eta2 * at(S1, 3, row, col);
-            f[4] = eta * at(S1, 4, row + 1, col) + eta2 * at(S1, 4, row, col);
-            f[5] = eta * at(S0, 5, row, col) + eta2 * at(S1, 5, row, col);
-            f[6] = eta * at(S2, 6, row, col) + eta2 * at(S1, 6, row, col);
+            f[1] = eta * fq(S1, 0, row, cq - 1) + eta2 * fq(S1, 0, row, cq);
+            f[2] = eta * fq(S1, 1, row, cq + 1) + eta2 * fq(S1, 1, row, cq);
+            f[3] = eta * fq(S1, 2, row - 1, cq) + eta2 * fq(S1, 2, row, cq);
+            f[4] = eta * fq(S1, 3, row + 1, cq) + eta2 * fq(S1, 3, row, cq);
+            f[5] = eta * fq(S0, 4, row, cq) + eta2 * fq(S1, 4, row, cq);
+            f[6] = eta * fq(S2, 5, row, cq) + eta2 * fq(S1, 5, row, cq);
         }
         return f[0] + f[1] + f[2] + f[3] + f[4] + f[5] + f[6];
     };
@@ -282,13 +346,19 @@ zsc_step_kernel(const StepPtrs P, const Box b, const StepConst c, const int tz, 
     // phi of plane p on the tile + ring into phi slot s; the streamed f of the
     // thread's own node is returned in fo.
     auto build_plane = [&](int p, int s, float(&fo)[kQf]) {
-        float *ph = PHI + s * PHI_STAGE;
+        float *ph = PHI + s * (RH * RW);
         ph[(ty + 1) * RW + tx + 1] = phi_at(p, tx + 1, ty + 1, fo);
         if (has_ring) {
             float tmp[kQf];
             ph[rly * RW + rlx] = phi_at(p, rlx, rly, tmp);
         }
     };
+
+    // Neighbour offsets in x and y are fixed for the thread; z per plane.
+    const int o_xm = (x == 0) ? b.nx - 1 : -1;
+    const int o_xp = (x == b.nx - 1) ? -(b.nx - 1) : 1;
+    const int o_ym = (y == 0) ? (b.ny - 1) * b.nx : -b.nx;
+    const int o_yp = (y == b.ny - 1) ? -(b.ny - 1) * b.nx : b.nx;
 
     float fcur[kQf], fnext[kQf];
 
@@ -322,9 +392,9 @@ zsc_step_kernel(const StepPtrs P, const Box b, const StepConst c, const int tz, 
         build_plane(z + 1, (j + 2) & 3, fnext);
         __syncthreads();
 
-        const float *S0 = PHI + (j & 3) * PHI_STAGE;        // plane z - 1
-        const float *S1 = PHI + ((j + 1) & 3) * PHI_STAGE;  // plane z
-        const float *S2 = PHI + ((j + 2) & 3) * PHI_STAGE;  // plane z + 1
+        const float *S0 = PHI + (j & 3) * (RH * RW);        // plane z - 1
+        const float *S1 = PHI + ((j + 1) & 3) * (RH * RW);  // plane z
+        const float *S2 = PHI + ((j + 2) & 3) * (RH * RW);  // plane z + 1
         const int lx = tx + 1, ly = ty + 1;
         auto at = [&](const float *S, int yy, int xx) { return S[yy * RW + xx]; };
 
@@ -350,10 +420,13 @@ zsc_step_kernel(const StepPtrs P, const Box b, const StepConst c, const int tz, 
         if (pc > 0.f) Fz += c.grav;
 
         // D3Q19 values of this node from the staged rows (AA pattern)
-        const float *Gs = G + (j & 1) * G_STAGE;
+        const ST *Gs = G + (j & 1) * G_ELEMS;
         float g[kQg];
 #pragma unroll
-        for (int i = 0; i < kQg; i++) g[i] = Gs[(i * TY + ty) * GW + 4 + tx - (ODD ? kCx(i) : 0)];
+        for (int i = 0; i < kQg; i++) {
+            const float v = Fm::load(Gs[(i * TY + ty) * W + E + tx - (ODD ? kCx(i) : 0)]);
+            if constexpr (Fm::kMapped) g[i] = v * q.g_inv[i] + q.g_shift[i]; else g[i] = v;
+        }
 
         // moments: src/update_rho.cu:46-50, src/update_velocity.cu:47-59
         float rho = g[0];
@@ -382,13 +455,17 @@ zsc_step_kernel(const StepPtrs P, const Box b, const StepConst c, const int tz, 
             const float Af = 0.5f * c.Gamma * c.invTauPhi * mu;
             const float Cf = c.invTauPhi * c.invEta2 * pc;
             const float a = c.invTauPhiOne;
-            P.fout[0][id] = a * fcur[0] - 6.0f * Af + c.invTauPhi * pc;
-            P.fout[1][id] = a * fcur[1] + Af + Cf * usx;
-            P.fout[2][id] = a * fcur[2] + Af - Cf * usx;
-            P.fout[3][id] = a * fcur[3] + Af + Cf * usy;
-            P.fout[4][id] = a * fcur[4] + Af - Cf * usy;
-            P.fout[5][id] = a * fcur[5] + Af + Cf * usz;
-            P.fout[6][id] = a * fcur[6] + Af - Cf * usz;
+            auto put = [&](int k, float v) {
+                if constexpr (Fm::kMapped) P.fout[k][id] = Fm::store(v * q.f_scale[k]);
+                else P.fout[k][id] = v;
+            };
+            P.f0out[id] = a * fcur[0] - 6.0f * Af + c.invTauPhi * pc;
+            put(0, a * fcur[1] + Af + Cf * usx);
+            put(1, a * fcur[2] + Af - Cf * usx);
+            put(2, a * fcur[3] + Af + Cf * usy);
+            put(3, a * fcur[4] + Af - Cf * usy);
+            put(4, a * fcur[5] + Af + Cf * usz);
+            put(5, a * fcur[6] + Af - Cf * usz);
         }
 
         // D3Q19 collision with forcing, src/collision_g.cu:232-313
@@ -400,22 +477,22 @@ zsc_step_kernel(const StepPtrs P, const Box b, const StepConst c, const int tz, 
             const float UF = usx * Fx + usy * Fy + usz * Fz;
             const float vx = usx * 3.f, vy = usy * 3.f, vz = usz * 3.f;
             const float vsq6 = (vx * vx + vy * vy + vz * vz) * kInv6;
-            float q[kQg];
-            q[0] = bb * g[0] + c.K0 * (rho - 6.f * pc * mu - rho * vsq6) - c.KC0 * UF;
+            float qv[kQg];
+            qv[0] = bb * g[0] + c.K0 * (rho - 6.f * pc * mu - rho * vsq6) - c.KC0 * UF;
             {
                 const float K1r = K1 * rho;
                 float eq1 = temp1 + K1r * vx * vx * 0.5f + KC1 * (vx * Fx - UF);
                 float eq2 = vx * (K1r + KC1 * Fx);
-                q[1] = bb * g[1] + eq1 + eq2;
-                q[2] = bb * g[2] + eq1 - eq2;
+                qv[1] = bb * g[1] + eq1 + eq2;
+                qv[2] = bb * g[2] + eq1 - eq2;
                 eq1 = temp1 + K1r * vy * 0.5f * vy + KC1 * (vy * Fy - UF);
                 eq2 = vy * (K1r + KC1 * Fy);
-                q[3] = bb * g[3] + eq1 + eq2;
-                q[4] = bb * g[4] + eq1 - eq2;
+                qv[3] = bb * g[3] + eq1 + eq2;
+                qv[4] = bb * g[4] + eq1 - eq2;
                 eq1 = temp1 + K1r * vz * 0.5f * vz + KC1 * (vz * Fz - UF);
                 eq2 = vz * (K1r + KC1 * Fz);
-                q[5] = bb * g[5] + eq1 + eq2;
-                q[6] = bb * g[6] + eq1 - eq2;
+                qv[5] = bb * g[5] + eq1 + eq2;
+                qv[6] = bb * g[6] + eq1 - eq2;
             }
             {
                 const float K2r = K2 * rho;
@@ -423,8 +500,8 @@ zsc_step_kernel(const StepPtrs P, const Box b, const StepConst c, const int tz, 
                 auto pair = [&](float w, float Gf, int ip, int im) {
                     const float eq1 = temp2 + K2r * w * 0.5f * w + KC2 * (w * Gf - UF);
                     const float eq2 = K2r * w + KC2 * Gf;
-                    q[ip] = bb * g[ip] + eq1 + eq2;
-                    q[im] = bb * g[im] + eq1 - eq2;
+                    qv[ip] = bb * g[ip] + eq1 + eq2;
+                    qv[im] = bb * g[im] + eq1 - eq2;
                 };
                 pair(vx + vy, Fx + Fy, 7, 8);
                 pair(vx - vy, Fx - Fy, 9, 10);
@@ -433,19 +510,24 @@ zsc_step_kernel(const StepPtrs P, const Box b, const StepConst c, const int tz, 
                 pair(vy + vz, Fy + Fz, 15, 16);
                 pair(vy - vz, Fy - Fz, 17, 18);
             }
+            auto enc = [&](int i, float v) -> ST {
+                if constexpr (Fm::kMapped) return Fm::store((v - q.g_shift[i]) * q.g_scale[i]);
+                else return v;
+            };
             if (!ODD) {
                 // even: own node, reversed slots
 #pragma unroll
-                for (int i = 0; i < kQg; i++) P.g[kOpp(i)][id] = q[i];
+                for (int i = 0; i < kQg; i++) P.g[kOpp(i)][id] = enc(i, qv[i]);
             } else {
                 // odd: downstream neighbour x + c_i, natural slot i
-                const Nbr o = neighbours(b, x, y, z);
+                const int o_zm = (z == 0) ? (b.nz - 1) * (int)b.nxy : -(int)b.nxy;
+                const int o_zp = (z == b.nz - 1) ? -(b.nz - 1) * (int)b.nxy : (int)b.nxy;
                 auto off = [&](int i) {
-                    return (kCx(i) > 0 ? o.xp : kCx(i) < 0 ? o.xm : 0) + (kCy(i) > 0 ? o.yp : kCy(i) < 0 ? o.ym : 0)
-                           + (kCz(i) > 0 ? o.zp : kCz(i) < 0 ? o.zm : 0);
+                    return (kCx(i) > 0 ? o_xp : kCx(i) < 0 ? o_xm : 0) + (kCy(i) > 0 ? o_yp : kCy(i) < 0 ? o_ym : 0)
+                           + (kCz(i) > 0 ? o_zp : kCz(i) < 0 ? o_zm : 0);
                 };
 #pragma unroll
-                for (int i = 0; i < kQg; i++) P.g[i][id + off(i)] = q[i];
+                for (int i = 0; i < kQg; i++) P.g[i][id + off(i)] = enc(i, qv[i]);
             }
         }
 
@@ -454,13 +536,13 @@ zsc_step_kernel(const StepPtrs P, const Box b, const StepConst c, const int tz, 
     }
 }
 
-template <bool S, bool O>
+template <typename ST, bool S, bool O>
 cudaError_t configure()
 {
     static bool done = false;   // per template instance, per process
     if (done) return cudaSuccess;
-    const cudaError_t e =
-        cudaFuncSetAttribute(zsc_step_kernel<S, O>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes);
+    const cudaError_t e = cudaFuncSetAttribute(zsc_step_kernel<ST, S, O>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               Geo<ST>::SMEM);
     if (e == cudaSuccess) done = true;
     return e;
 }
@@ -468,16 +550,17 @@ cudaError_t configure()
 // Planes per block.  The blocks of one launch all march the same number of
 // planes, so the step takes about ceil(blocks / resident slots) "waves" of
 // (tz + prologue) planes; pick the chunk depth that minimises that product
-// (e.g. 256^3: 37 planes -> 1792 blocks = 5.9 waves of 304 slots, instead of
-// 32 planes -> 6.7 waves with a 74%-full last wave).
+// (e.g. 256^3 FP32: 37 planes -> 1792 blocks = 5.9 waves of 304 slots, instead
+// of 32 planes -> 6.7 waves with a 74%-full last wave).
+template <typename ST>
 int choose_tz(const Box &b)
 {
-    static int slots = 0;
+    static int slots = 0;   // per storage type, per process
     if (slots == 0) {
         int dev = 0, sms = 0, per_sm = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, zsc_step_kernel<false, false>, NT, kSmemBytes);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, zsc_step_kernel<ST, false, false>, NT, Geo<ST>::SMEM);
         slots = sms * per_sm > 0 ? sms * per_sm : 1;
     }
     const long long tiles = (long long)(b.nx / TX) * (b.ny / TY);
@@ -496,37 +579,55 @@ int choose_tz(const Box &b)
     return best;
 }
 
-}  // namespace
-
-cudaError_t launch_step(const Box &b, const StepConst &c, const float *f_in, float *f_out, float *g, float *mom,
-                        bool f_streamed, bool odd, bool write_moments, cudaStream_t s)
+template <typename ST>
+cudaError_t launch_typed(const Box &b, const StepConst &c, const Quant &q, const StepView &v, bool f_streamed,
+                         bool odd, bool write_moments, cudaStream_t s)
 {
-    if (b.nx % TX != 0 || b.ny % TY != 0) return cudaErrorInvalidValue;
-    StepPtrs P;
-    for (int i = 0; i < kQf; i++) {
-        P.fin[i] = f_in + (size_t)i * b.n;
-        P.fout[i] = f_out + (size_t)i * b.n;
+    StepPtrs<ST> P;
+    P.f0in = v.f0_in;
+    P.f0out = v.f0_out;
+    const ST *fin = static_cast<const ST *>(v.fq_in);
+    ST *fout = static_cast<ST *>(v.fq_out);
+    ST *g = static_cast<ST *>(v.g);
+    for (int a = 0; a < kQf - 1; a++) {
+        P.fin[a] = fin + (size_t)a * b.n;
+        P.fout[a] = fout + (size_t)a * b.n;
     }
     for (int i = 0; i < kQg; i++) P.g[i] = g + (size_t)i * b.n;
-    for (int i = 0; i < 5; i++) P.mom[i] = mom + (size_t)i * b.n;
-    cudaError_t e = configure<true, false>();
-    if (e == cudaSuccess) e = configure<false, true>();
-    if (e == cudaSuccess) e = configure<false, false>();
+    for (int i = 0; i < 5; i++) P.mom[i] = v.mom + (size_t)i * b.n;
+    cudaError_t e = configure<ST, true, false>();
+    if (e == cudaSuccess) e = configure<ST, false, true>();
+    if (e == cudaSuccess) e = configure<ST, false, false>();
     if (e != cudaSuccess) return e;
-    const int tz = choose_tz(b);
+    const int tz = choose_tz<ST>(b);
     const int nchunks = (b.nz + tz - 1) / tz;
     const unsigned nblocks = (unsigned)((b.nx / TX) * (b.ny / TY) * nchunks);
     const dim3 block(TX, TY, 1);
     const int wm = write_moments ? 1 : 0;
+    constexpr int smem = Geo<ST>::SMEM;
     if (f_streamed) {
         if (odd) return cudaErrorInvalidValue;  // the streamed initial state is always read by an even step
-        zsc_step_kernel<true, false><<<nblocks, block, kSmemBytes, s>>>(P, b, c, tz, wm);
+        zsc_step_kernel<ST, true, false><<<nblocks, block, smem, s>>>(P, b, c, q, tz, wm);
     } else if (odd) {
-        zsc_step_kernel<false, true><<<nblocks, block, kSmemBytes, s>>>(P, b, c, tz, wm);
+        zsc_step_kernel<ST, false, true><<<nblocks, block, smem, s>>>(P, b, c, q, tz, wm);
     } else {
-        zsc_step_kernel<false, false><<<nblocks, block, kSmemBytes, s>>>(P, b, c, tz, wm);
+        zsc_step_kernel<ST, false, false><<<nblocks, block, smem, s>>>(P, b, c, q, tz, wm);
     }
     return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_step(const Box &b, const StepConst &c, const Quant &q, const StepView &v, bool f_streamed,
+                        bool odd, bool write_moments, cudaStream_t s)
+{
+    if (b.nx % TX != 0 || b.ny % TY != 0) return cudaErrorInvalidValue;
+    switch (v.storage) {
+    case LBM_STORAGE_FP32: return launch_typed<float>(b, c, q, v, f_streamed, odd, write_moments, s);
+    case LBM_STORAGE_FP16: return launch_typed<__half>(b, c, q, v, f_streamed, odd, write_moments, s);
+    case LBM_STORAGE_BF16: return launch_typed<__nv_bfloat16>(b, c, q, v, f_streamed, odd, write_moments, s);
+    default: return cudaErrorInvalidValue;
+    }
 }
 
 }  // namespace lbm

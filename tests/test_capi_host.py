@@ -92,7 +92,7 @@ def test_discrete_with_missing_rows(tmp_path):
     (dict(block_x=64, block_y=16, compat=True), 1),  # compat: BLOCK_SIZE_X*Y > 512 (src/main.cu:171)
     (dict(tauRho=0.0), 1),
     (dict(rhoH=0.1), 1),                   # rhoH == rhoL: phiStar = 0
-    (dict(storage="bf16", nx=32), 1),
+    (dict(storage=7, nx=32), 1),           # unknown storage format
     (dict(nz=2), 1),
 ])
 def test_init_rejects_bad_params_without_touching_the_gpu(change, code):
@@ -103,7 +103,10 @@ def test_init_rejects_bad_params_without_touching_the_gpu(change, code):
         if k in change:
             dims[k] = change.pop(k)
     kw.update(change)
+    storage = kw.pop("storage", None)
     p = capi.make_params(dims["nx"], dims["ny"], dims["nz"], **kw)
+    if storage is not None:
+        p.storage = storage
     phi = np.zeros(p.nx * p.ny * p.nz, np.float32)
     with pytest.raises(capi.LbmError) as e:
         capi.Lattice.from_fields(p, phi, phi + 0.55)

@@ -17,7 +17,7 @@ def make(nx, ny, nz, **kw):
     from lbm_bench_gpu_gb300 import capi
     args = dict(PHYS)
     args.update(kw)
-    return capi.make_params(nx, ny, nz, **args)
+    return capi.make_params(nx, ny, nz, **args)   # storage= "fp32" (default), "fp16" or "bf16"
 
 
 def oracle_for(p, bubbles):
@@ -215,3 +215,51 @@ def test_full_size_conservation(lib):
     assert abs(s1["phi_sum"] - s0["phi_sum"]) <= 1e-6 * abs(s0["phi_sum"])
     assert abs(s1["rho_sum"] - s0["rho_sum"]) <= 1e-6 * abs(s0["rho_sum"])
     assert s1["vol"] == pytest.approx(s0["vol"], rel=2e-2)
+
+
+# 16-bit storage (f_1..f_6 and g in FP16 / BF16 with a shifted, power-of-two
+# scaled map; f_0 and all arithmetic FP32).  Tolerances against the FP64
+# oracle at 10 steps: FP16 5e-5 relative (phi, rho, distributions) and
+# 5e-5 c_s on u; BF16 (8-bit mantissa) 5e-4 and 5e-4 c_s.
+STORAGE_TOL = {"fp16": 5e-5, "bf16": 5e-4}
+
+
+@pytest.mark.parametrize("storage", ["fp16", "bf16"])
+def test_storage_roundtrip_error_bound(lib, storage):
+    """lbm_set_dist -> lbm_get_dist: every value within half a unit in the last
+    place of its shifted, scaled 16-bit encoding."""
+    from lbm_bench_gpu_gb300 import capi
+    p = make(32, 16, 24, tauRho=0.65, tauPhi=0.75, storage=storage)
+    f, g = random_state((24, 16, 32), 5, make(32, 16, 24, tauRho=0.65, tauPhi=0.75))
+    f32, g32 = f.astype(np.float32), g.astype(np.float32)
+    with capi.Lattice.from_fields(p, np.zeros((24, 16, 32), np.float32), np.full((24, 16, 32), 0.55, np.float32)) as lat:
+        lat.set_dist(f32, g32)
+        fb, gb = lat.dist()
+    assert np.array_equal(fb[0], f32[0])                      # f_0 stays FP32
+    ulp = 2.0 ** -11 if storage == "fp16" else 2.0 ** -8
+    rho_mean = g32.sum(axis=0).mean()
+    w = np.array([1 / 3] + [1 / 18] * 6 + [1 / 36] * 12)
+    for i in range(19):
+        dev = np.abs(g32[i] - w[i] * rho_mean).max()
+        assert np.abs(gb[i] - g32[i]).max() <= ulp * dev * 1.01 + 1e-9, f"g{i}"
+    for i in range(1, 7):
+        assert np.abs(fb[i] - f32[i]).max() <= ulp * np.abs(f32[i]).max() * 1.01 + 1e-12, f"f{i}"
+
+
+@pytest.mark.parametrize("storage", ["fp16", "bf16"])
+@pytest.mark.parametrize("steps", [1, 2, 10])
+def test_storage_steps_match_oracle(lib, storage, steps):
+    from lbm_bench_gpu_gb300 import capi
+    shape = (64, 32, 48)
+    nx, ny, nz = shape
+    b = np.array([[nx / 2 - 0.3, ny / 2 + 0.2, nz / 2 + 0.4, 10.0], [16, 8, 13, 6.0]], np.float32)
+    p = make(nx, ny, nz, tauRho=0.8, tauPhi=0.9, storage=storage)
+    tol = STORAGE_TOL[storage]
+    with capi.Lattice.from_bubbles(p, b) as lat:
+        o = oracle_for(make(nx, ny, nz, tauRho=0.8, tauPhi=0.9), b)
+        lat.step(steps, -2e-5)
+        o.step(steps, -2e-5)
+        assert_fields_close(lat.fields(), o.moments(), rel=tol, utol=tol * U_TOL / 1e-5, what=f"{storage} {steps}")
+        f, g = lat.dist()
+        fo, go = o.dist()
+        assert rel_err(f, fo) <= tol and rel_err(g, go) <= tol
