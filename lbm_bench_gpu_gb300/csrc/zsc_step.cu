@@ -48,9 +48,6 @@ namespace {
 #ifndef ZSC_TILE_Y
 #define ZSC_TILE_Y 8
 #endif
-#ifndef ZSC_MIN_BLOCKS
-#define ZSC_MIN_BLOCKS 2
-#endif
 constexpr int TX = 32;              // tile width in x (one warp per row)
 constexpr int TY = ZSC_TILE_Y;      // tile height in y
 constexpr int NT = TX * TY;         // threads per block
@@ -91,23 +88,29 @@ struct Dir {
     static constexpr int value = I;
 };
 
-// Storage formats: element conversions.
+// Storage formats: element conversions, and the resident blocks per SM the
+// launch bounds ask for.  FP32 stages 108 KB of shared memory per block (2
+// blocks per SM); the 16-bit formats stage 70 KB, and 3 blocks per SM fit when
+// the kernel stays within 85 registers (it does, without spills).
 template <typename ST>
 struct Fmt;
 template <>
 struct Fmt<float> {
+    static constexpr int kMinBlocks = 2;
     static constexpr bool kMapped = false;
     __device__ static float load(float v) { return v; }
     __device__ static float store(float v) { return v; }
 };
 template <>
 struct Fmt<__half> {
+    static constexpr int kMinBlocks = 3;
     static constexpr bool kMapped = true;
     __device__ static float load(__half v) { return __half2float(v); }
     __device__ static __half store(float v) { return __float2half_rn(v); }
 };
 template <>
 struct Fmt<__nv_bfloat16> {
+    static constexpr int kMinBlocks = 3;
     static constexpr bool kMapped = true;
     __device__ static float load(__nv_bfloat16 v) { return __bfloat162float(v); }
     __device__ static __nv_bfloat16 store(float v) { return __float2bfloat16_rn(v); }
@@ -172,7 +175,7 @@ __device__ __forceinline__ void for_dirs_from(F &&f)
 }
 
 template <typename ST, bool STREAMED, bool ODD>
-__global__ void __launch_bounds__(NT, ZSC_MIN_BLOCKS)
+__global__ void __launch_bounds__(NT, Fmt<ST>::kMinBlocks)
 zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Quant q, const int tz,
                 const int write_moments)
 {
