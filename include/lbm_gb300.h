@@ -145,6 +145,45 @@ int lbm_get_dist(lbm_ctx *c, float *f, float *g);
  * their moments.  Synchronises. */
 int lbm_set_dist(lbm_ctx *c, const float *f, const float *g);
 
+/* Objectives of lbm_step_adjoint, on the moments of the streamed state
+ * (phi = sum f, rho = sum g, u = sum c g / rho) with the smooth light-phase
+ * weight w = (phiStar - phi) / (2 phiStar):
+ *   LBM_OBJ_LIGHT_UZ_MEAN     mean over the last `window` states of
+ *                             sum(w u_z) / sum(w): rise velocity of the light phase
+ *   LBM_OBJ_LIGHT_Z_CENTROID  sum(w z) / sum(w) of the final state (z = plane
+ *                             index + 1, the reference's z coordinate) */
+#define LBM_OBJ_LIGHT_UZ_MEAN 0
+#define LBM_OBJ_LIGHT_Z_CENTROID 1
+
+typedef struct lbm_adjoint_opts {
+    int objective;            /* LBM_OBJ_* */
+    int nsteps;               /* T: steps of the run, starting from the initial state */
+    int window;               /* states averaged by LBM_OBJ_LIGHT_UZ_MEAN (the last `window`) */
+    float grav;               /* body force of the run */
+    double checkpoint_bytes;  /* device memory for checkpoints; <= 0: half of the free memory */
+} lbm_adjoint_opts;
+
+typedef struct lbm_adjoint_out {
+    double J;                 /* objective (FP64 accumulation) */
+    double dJ_dgrav;          /* dJ / d grav (FP64 accumulation) */
+    float *dJ_dphi0;          /* caller's nx*ny*nz host buffer for dJ / d phi0, or NULL */
+    int slots;                /* checkpoints held, the initial state included */
+    long long forward_steps;  /* forward steps run, recomputation included */
+    long long adjoint_steps;  /* = nsteps */
+    double seconds;           /* wall time of the call */
+    double checkpoint_bytes_used;
+} lbm_adjoint_out;
+
+/* Gradient of an objective over T steps with respect to the body force and
+ * the initial phi field, by the discrete adjoint of the fused step (reverse
+ * streaming, transposed collisions, transposed gradient / Laplacian stencils,
+ * force terms) with binomial checkpointing of the forward trajectory.  No
+ * counterpart in the reference.  The context must hold its initial state
+ * (lbm_init / lbm_init_bubbles / lbm_set_dist, no step taken); the gradient
+ * with respect to phi0 passes through the initial equilibrium with periodic
+ * z.  On return the context holds the initial state again.  Synchronises. */
+int lbm_step_adjoint(lbm_ctx *c, const lbm_adjoint_opts *o, lbm_adjoint_out *out);
+
 /* Largest box lbm_stats_noalloc accepts: 512^3 nodes. */
 #define LBM_NOALLOC_MAX_NODES 134217728LL
 /* Number of doubles lbm_stats_noalloc writes. */

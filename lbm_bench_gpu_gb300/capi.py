@@ -22,8 +22,9 @@ STORAGE = {"fp32": 0, "fp16": 1, "bf16": 2}
 EXPORTS = [
     "lbm_read_inputs", "lbm_derive", "lbm_init", "lbm_init_bubbles", "lbm_step", "lbm_stats",
     "lbm_get_dist", "lbm_set_dist", "lbm_steps_done", "lbm_stream", "lbm_sync", "lbm_destroy",
-    "lbm_strerror", "lbm_last_error", "lbm_stats_noalloc",
+    "lbm_strerror", "lbm_last_error", "lbm_stats_noalloc", "lbm_step_adjoint",
 ]
+OBJECTIVES = {"light_uz_mean": 0, "light_z_centroid": 1}
 
 
 class Params(C.Structure):
@@ -64,6 +65,17 @@ class StatsOut(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class AdjointOpts(C.Structure):
+    _fields_ = [("objective", C.c_int), ("nsteps", C.c_int), ("window", C.c_int), ("grav", C.c_float),
+                ("checkpoint_bytes", C.c_double)]
+
+
+class AdjointOut(C.Structure):
+    _fields_ = [("J", C.c_double), ("dJ_dgrav", C.c_double), ("dJ_dphi0", C.POINTER(C.c_float)),
+                ("slots", C.c_int), ("forward_steps", C.c_longlong), ("adjoint_steps", C.c_longlong),
+                ("seconds", C.c_double), ("checkpoint_bytes_used", C.c_double)]
+
+
 class LbmError(RuntimeError):
     def __init__(self, code: int, what: str, detail: str):
         super().__init__(f"{what}: status {code} ({detail})")
@@ -94,6 +106,7 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.lbm_set_dist.argtypes = [C.c_void_p, _F, _F]
     lib.lbm_stats_noalloc.argtypes = [C.POINTER(Params), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                       C.c_void_p, C.c_void_p, C.c_void_p]
+    lib.lbm_step_adjoint.argtypes = [C.c_void_p, C.POINTER(AdjointOpts), C.POINTER(AdjointOut)]
     lib.lbm_steps_done.argtypes = [C.c_void_p]
     lib.lbm_steps_done.restype = C.c_longlong
     lib.lbm_stream.argtypes = [C.c_void_p]
@@ -212,6 +225,18 @@ class Lattice:
         f = np.ascontiguousarray(f, np.float32)
         g = np.ascontiguousarray(g, np.float32)
         check(load().lbm_set_dist(self._h, fptr(f), fptr(g)), "lbm_set_dist")
+
+    def adjoint(self, nsteps: int, grav: float, objective: str = "light_uz_mean", window: int = 1,
+                checkpoint_bytes: float = 0.0, want_phi0: bool = True) -> dict:
+        """lbm_step_adjoint: J, dJ/dgrav and dJ/dphi0 over nsteps from the initial state."""
+        o = AdjointOpts(OBJECTIVES[objective], int(nsteps), int(window), float(grav), float(checkpoint_bytes))
+        out = AdjointOut()
+        grad = np.zeros(self.shape, np.float32) if want_phi0 else None
+        out.dJ_dphi0 = fptr(grad) if want_phi0 else None
+        check(load().lbm_step_adjoint(self._h, C.byref(o), C.byref(out)), "lbm_step_adjoint")
+        return {"J": out.J, "dJ_dgrav": out.dJ_dgrav, "dJ_dphi0": grad, "slots": out.slots,
+                "forward_steps": out.forward_steps, "adjoint_steps": out.adjoint_steps, "seconds": out.seconds,
+                "checkpoint_bytes_used": out.checkpoint_bytes_used}
 
     @property
     def steps(self) -> int:

@@ -1,0 +1,331 @@
+// lbm_adjoint.cu -- lbm_step_adjoint: gradient of a light-phase objective with
+// respect to the body force and the initial phi field, by the discrete adjoint
+// of the fused step with binomial checkpointing.  No counterpart in the
+// reference.
+//
+// Schedule.  The forward trajectory s^0 .. s^T is not kept: native state
+// snapshots (the step's own buffers, 26 distributions) go into a pool of slots
+// sized from the memory budget, and missing states are recomputed from the
+// nearest snapshot.  With c free slots and r sweeps at most
+// beta(c, r) = C(c + r, r) steps can be reversed; a segment [s, e) with its
+// start stored is split at m = e - min(beta(c - 1, r), e - s - 1) with r the
+// smallest sweep count that covers it: m is stored, [m, e) is reversed with
+// c - 1 free slots, then [s, m) with c (Griewank's binomial checkpointing).
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "lbm_internal.h"
+
+namespace {
+
+using lbm::cuda_fail;
+using lbm::fail;
+
+double beta(int c, int r)
+{
+    // C(c + r, r), saturating
+    double v = 1.0;
+    for (int i = 1; i <= r; i++) {
+        v = v * (double)(c + i) / (double)i;
+        if (v > 1e18) return 1e18;
+    }
+    return v;
+}
+
+struct Snapshot {
+    long long step = -1;
+    bool f_streamed = false, g_odd_next = false;
+};
+
+struct Adjoint {
+    lbm_ctx *c;
+    lbm_adjoint_opts o;
+    size_t n, snap_bytes;
+    // work buffers
+    float *F = nullptr, *G = nullptr, *phi = nullptr;
+    float *lam[2] = {nullptr, nullptr};   // 26 x n each: f (7) then g (19)
+    float *lst[2] = {nullptr, nullptr};
+    float *llap = nullptr, *lgrad = nullptr, *phi0 = nullptr, *mom_save = nullptr;
+    double *partials = nullptr, *ab = nullptr, *acc = nullptr;
+    unsigned char *slots = nullptr;
+    std::vector<Snapshot> snaps;
+    std::vector<int> free_slots;
+    int cur = 0;                 // lam[cur] holds lambda^{k+1}
+    bool lambda_ready = false;
+    long long fwd_steps = 0, adj_steps = 0;
+    lbm::StepConst k;
+    int first_source;            // first state index with an objective term
+    double scale;
+
+    unsigned char *slot_ptr(int s) { return slots + (size_t)s * snap_bytes; }
+
+    int save(int s, long long step)
+    {
+        lbm::StepView v = lbm::state_view(c, c->st.f_cur);
+        unsigned char *d = slot_ptr(s);
+        const size_t b0 = sizeof(float) * n, bq = c->esz * (lbm::kQf - 1) * n, bg = c->esz * lbm::kQg * n;
+        cudaError_t e = cudaMemcpyAsync(d, v.f0_in, b0, cudaMemcpyDeviceToDevice, c->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(d + b0, v.fq_in, bq, cudaMemcpyDeviceToDevice, c->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(d + b0 + bq, c->st.g, bg, cudaMemcpyDeviceToDevice, c->stream);
+        if (e != cudaSuccess) return cuda_fail(e, "adjoint: snapshot");
+        snaps[s].step = step;
+        snaps[s].f_streamed = c->st.f_streamed;
+        snaps[s].g_odd_next = c->st.g_odd_next;
+        return LBM_OK;
+    }
+
+    int restore(int s)
+    {
+        lbm::StepView v = lbm::state_view(c, 0);
+        const unsigned char *d = slot_ptr(s);
+        const size_t b0 = sizeof(float) * n, bq = c->esz * (lbm::kQf - 1) * n, bg = c->esz * lbm::kQg * n;
+        cudaError_t e = cudaMemcpyAsync(c->st.f0, d, b0, cudaMemcpyDeviceToDevice, c->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(const_cast<void *>(v.fq_in), d + b0, bq, cudaMemcpyDeviceToDevice, c->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(c->st.g, d + b0 + bq, bg, cudaMemcpyDeviceToDevice, c->stream);
+        if (e != cudaSuccess) return cuda_fail(e, "adjoint: restore");
+        c->st.f_cur = 0;
+        c->st.f_streamed = snaps[s].f_streamed;
+        c->st.g_odd_next = snaps[s].g_odd_next;
+        c->st.steps = snaps[s].step;
+        return LBM_OK;
+    }
+
+    int forward(long long nsteps)
+    {
+        if (nsteps <= 0) return LBM_OK;
+        fwd_steps += nsteps;
+        return lbm_step(c, (int)nsteps, o.grav);
+    }
+
+    // streamed FP32 copy of the current state and its phi
+    int prepare()
+    {
+        cudaError_t e = lbm::launch_stream_out(c->box, c->d.eta, c->q, lbm::state_view(c, c->st.f_cur),
+                                               c->st.f_streamed, c->st.g_odd_next, F, G, c->stream);
+        if (e == cudaSuccess) e = lbm::launch_phi(c->box, F, phi, c->stream);
+        return e == cudaSuccess ? LBM_OK : cuda_fail(e, "adjoint: prepare");
+    }
+
+    bool has_source(long long step) const { return step >= first_source; }
+
+    // lambda^T from the final state (the context holds s^T)
+    int terminal()
+    {
+        int rc = prepare();
+        if (rc) return rc;
+        cudaError_t e = cudaSuccess;
+        if (has_source(o.nsteps)) {
+            e = lbm::launch_objective(c->box, o.objective, c->d.phiStar, scale, phi, G, partials, ab, acc, c->stream);
+            if (e == cudaSuccess)
+                e = lbm::launch_source_init(c->box, o.objective, scale, ab, c->d.phiStar, phi, G, lam[cur],
+                                            lam[cur] + lbm::kQf * n, lst[cur], c->stream);
+        } else {
+            e = cudaMemsetAsync(lam[cur], 0, sizeof(float) * (lbm::kQf + lbm::kQg) * n, c->stream);
+            if (e == cudaSuccess) e = cudaMemsetAsync(lst[cur], 0, sizeof(float) * n, c->stream);
+        }
+        if (e != cudaSuccess) return cuda_fail(e, "adjoint: terminal source");
+        lambda_ready = true;
+        return LBM_OK;
+    }
+
+    // lambda^step from lambda^{step+1}; the context holds s^step
+    int adjoint_step(long long step)
+    {
+        int rc = prepare();
+        if (rc) return rc;
+        const bool src = has_source(step);
+        cudaError_t e = cudaSuccess;
+        if (src)
+            e = lbm::launch_objective(c->box, o.objective, c->d.phiStar, scale, phi, G, partials, ab, acc, c->stream);
+        lbm::AdjointBuffers a;
+        a.F = F;
+        a.G = G;
+        a.phi = phi;
+        a.lf_in = lam[cur];
+        a.lg_in = lam[cur] + lbm::kQf * n;
+        a.lst_in = lst[cur];
+        a.lf_out = lam[1 - cur];
+        a.lg_out = lam[1 - cur] + lbm::kQf * n;
+        a.lst_out = lst[1 - cur];
+        a.llap = llap;
+        a.lgrad = lgrad;
+        a.partials = partials;
+        a.ab = ab;
+        if (e == cudaSuccess)
+            e = lbm::launch_adjoint_step(c->box, k, c->d.phiStar, a, src, o.objective, scale, acc, c->stream);
+        if (e != cudaSuccess) return cuda_fail(e, "adjoint step");
+        cur = 1 - cur;
+        adj_steps++;
+        return LBM_OK;
+    }
+
+    // adjoint of step s (the segment [s, s + 1)); slot si holds s^s
+    int leaf(long long s, int si)
+    {
+        int rc;
+        if (!lambda_ready) {   // s + 1 == T: build lambda^T first
+            if ((rc = restore(si)) || (rc = forward(1)) || (rc = terminal())) return rc;
+        }
+        if ((rc = restore(si))) return rc;
+        return adjoint_step(s);
+    }
+
+    int take_slot()
+    {
+        if (free_slots.empty()) return -1;
+        const int s = free_slots.back();
+        free_slots.pop_back();
+        return s;
+    }
+
+    // reverse [s, e) with s^s in slot si and `cfree` slots available
+    int revolve(long long s, long long e, int si, int cfree)
+    {
+        const long long len = e - s;
+        int rc;
+        if (len <= 0) return LBM_OK;
+        if (len == 1) return leaf(s, si);
+        if (cfree == 0) {
+            for (long long j = e - 1; j >= s; j--) {
+                if (!lambda_ready) {
+                    if ((rc = restore(si)) || (rc = forward(o.nsteps - s)) || (rc = terminal())) return rc;
+                }
+                if ((rc = restore(si)) || (rc = forward(j - s)) || (rc = adjoint_step(j))) return rc;
+            }
+            return LBM_OK;
+        }
+        int r = 1;
+        while (beta(cfree, r) < (double)len) r++;
+        const long long right = std::min<long long>((long long)beta(cfree - 1, r), len - 1);
+        const long long m = e - right;
+        const int sj = take_slot();
+        if (sj < 0) return fail(LBM_ESTATE, "adjoint: checkpoint pool exhausted");
+        if ((rc = restore(si)) || (rc = forward(m - s)) || (rc = save(sj, m))) return rc;
+        if ((rc = revolve(m, e, sj, cfree - 1))) return rc;
+        free_slots.push_back(sj);
+        return revolve(s, m, si, cfree);
+    }
+
+    void release()
+    {
+        cudaStreamSynchronize(c->stream);
+        void *p[] = {F, G, phi, lam[0], lam[1], lst[0], lst[1], llap, lgrad, phi0, mom_save, partials, ab, acc, slots};
+        for (void *q : p) cudaFree(q);
+    }
+};
+
+}  // namespace
+
+extern "C" int lbm_step_adjoint(lbm_ctx *c, const lbm_adjoint_opts *o, lbm_adjoint_out *out)
+{
+    if (!c || !o || !out) return fail(LBM_EINVAL, "lbm_step_adjoint: NULL argument");
+    if (o->nsteps < 1) return fail(LBM_EINVAL, "lbm_step_adjoint: nsteps must be >= 1");
+    if (o->objective != LBM_OBJ_LIGHT_UZ_MEAN && o->objective != LBM_OBJ_LIGHT_Z_CENTROID)
+        return fail(LBM_EINVAL, "lbm_step_adjoint: unknown objective");
+    if (o->objective == LBM_OBJ_LIGHT_UZ_MEAN && (o->window < 1 || o->window > o->nsteps))
+        return fail(LBM_EINVAL, "lbm_step_adjoint: window must be in [1, nsteps]");
+    if (!std::isfinite(o->grav)) return fail(LBM_EINVAL, "lbm_step_adjoint: grav is not finite");
+    if (c->st.steps != 0)
+        return fail(LBM_ESTATE, "lbm_step_adjoint: the context must hold its initial state (no step taken)");
+    const auto t0 = std::chrono::steady_clock::now();
+    cudaError_t e = cudaSetDevice(c->p.device);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+
+    Adjoint A;
+    A.c = c;
+    A.o = *o;
+    A.n = (size_t)c->box.n;
+    const size_t n = A.n;
+    A.snap_bytes = sizeof(float) * n + c->esz * (lbm::kQf - 1 + lbm::kQg) * n;
+    A.k = lbm::step_const(c->d, c->p, o->grav);
+    A.first_source = o->objective == LBM_OBJ_LIGHT_UZ_MEAN ? o->nsteps - o->window + 1 : o->nsteps;
+    A.scale = o->objective == LBM_OBJ_LIGHT_UZ_MEAN ? 1.0 / o->window : 1.0;
+    const size_t npart = lbm::adjoint_partial_count(c->box);
+
+    auto alloc = [&](void **p, size_t bytes) {
+        if (e == cudaSuccess) e = cudaMalloc(p, bytes);
+    };
+    alloc((void **)&A.F, sizeof(float) * lbm::kQf * n);
+    alloc((void **)&A.G, sizeof(float) * lbm::kQg * n);
+    alloc((void **)&A.phi, sizeof(float) * n);
+    alloc((void **)&A.lam[0], sizeof(float) * (lbm::kQf + lbm::kQg) * n);
+    alloc((void **)&A.lam[1], sizeof(float) * (lbm::kQf + lbm::kQg) * n);
+    alloc((void **)&A.lst[0], sizeof(float) * n);
+    alloc((void **)&A.lst[1], sizeof(float) * n);
+    alloc((void **)&A.llap, sizeof(float) * n);
+    alloc((void **)&A.lgrad, sizeof(float) * 3 * n);
+    alloc((void **)&A.phi0, sizeof(float) * n);
+    alloc((void **)&A.mom_save, sizeof(float) * 5 * n);
+    alloc((void **)&A.partials, sizeof(double) * 2 * npart);
+    alloc((void **)&A.ab, sizeof(double) * 2);
+    alloc((void **)&A.acc, sizeof(double) * 2);
+    if (e != cudaSuccess) {
+        A.release();
+        return cuda_fail(e, "lbm_step_adjoint: work buffers");
+    }
+    // checkpoint pool
+    double budget = o->checkpoint_bytes;
+    if (!(budget > 0)) {
+        size_t fr = 0, tot = 0;
+        cudaMemGetInfo(&fr, &tot);
+        budget = 0.5 * (double)fr;
+    }
+    long long nslots = (long long)(budget / (double)A.snap_bytes);
+    nslots = std::min<long long>(nslots, (long long)o->nsteps + 1);
+    if (nslots < 1) {
+        A.release();
+        return fail(LBM_ENOMEM, "lbm_step_adjoint: checkpoint budget below one snapshot (" +
+                                    std::to_string(A.snap_bytes) + " bytes)");
+    }
+    e = cudaMalloc(&A.slots, (size_t)nslots * A.snap_bytes);
+    if (e != cudaSuccess) {
+        A.release();
+        return cuda_fail(e, "lbm_step_adjoint: checkpoint pool");
+    }
+    A.snaps.assign((size_t)nslots, Snapshot());
+    for (long long s = nslots - 1; s >= 1; s--) A.free_slots.push_back((int)s);
+
+    int rc = LBM_OK;
+    e = cudaMemsetAsync(A.acc, 0, sizeof(double) * 2, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(A.phi0, c->st.mom, sizeof(float) * n, cudaMemcpyDeviceToDevice, c->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(A.mom_save, c->st.mom, sizeof(float) * 5 * n, cudaMemcpyDeviceToDevice, c->stream);
+    if (e != cudaSuccess) rc = cuda_fail(e, "lbm_step_adjoint: setup");
+    if (!rc) rc = A.save(0, 0);
+    if (!rc) rc = A.revolve(0, o->nsteps, 0, (int)(nslots - 1));
+    // lambda^0 -> dJ/dphi0 through the initial equilibrium (output in llap,
+    // lgrad as the scratch for the Laplacian's adjoint)
+    float *lphi0 = A.llap;
+    if (!rc) {
+        e = lbm::launch_init_adjoint(c->box, c->d, c->p.Gamma, A.phi0, A.lam[A.cur], A.lst[A.cur],
+                                     A.lam[A.cur] + lbm::kQf * n, lphi0, A.lgrad, c->stream);
+        if (e != cudaSuccess) rc = cuda_fail(e, "lbm_step_adjoint: initial-state adjoint");
+    }
+    double acc[2] = {0.0, 0.0};
+    if (!rc) {
+        e = cudaMemcpyAsync(acc, A.acc, sizeof(acc), cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess && out->dJ_dphi0)
+            e = cudaMemcpyAsync(out->dJ_dphi0, lphi0, sizeof(float) * n, cudaMemcpyDeviceToHost, c->stream);
+        // leave the context at its initial state with its initial fields
+        if (e == cudaSuccess) rc = A.restore(0);
+        if (e == cudaSuccess && !rc)
+            e = cudaMemcpyAsync(c->st.mom, A.mom_save, sizeof(float) * 5 * n, cudaMemcpyDeviceToDevice, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess && !rc) rc = cuda_fail(e, "lbm_step_adjoint: results");
+    }
+    A.release();
+    if (rc) return rc;
+    out->J = acc[0];
+    out->dJ_dgrav = acc[1];
+    out->slots = (int)nslots;
+    out->forward_steps = A.fwd_steps;
+    out->adjoint_steps = A.adj_steps;
+    out->checkpoint_bytes_used = (double)nslots * (double)A.snap_bytes;
+    out->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return LBM_OK;
+}

@@ -6,37 +6,14 @@
 
 #include "lbm_internal.h"
 
-struct lbm_ctx {
-    lbm_params p;
-    lbm_derived d;
-    lbm::Box box;
-    cudaStream_t stream = nullptr;
-    lbm::State st;
-    lbm::Quant q;
-    size_t esz = 4;                // bytes per element of fq / g
-    double *partials = nullptr;    // stats scratch: per-block partial sums
-    size_t partial_count = 0;
-    double *result = nullptr;      // stats result (device)
-    double *result_host = nullptr; // pinned copy
-};
-
 namespace {
 
 constexpr double kW[lbm::kQg] = {1.0 / 3,  1.0 / 18, 1.0 / 18, 1.0 / 18, 1.0 / 18, 1.0 / 18, 1.0 / 18,
                                  1.0 / 36, 1.0 / 36, 1.0 / 36, 1.0 / 36, 1.0 / 36, 1.0 / 36, 1.0 / 36,
                                  1.0 / 36, 1.0 / 36, 1.0 / 36, 1.0 / 36, 1.0 / 36};   // src/constants.h:52-54
 
-int fail(int code, const std::string &msg)
-{
-    lbm::set_error(msg);
-    return code;
-}
-
-int cuda_fail(cudaError_t e, const char *what)
-{
-    return fail(e == cudaErrorMemoryAllocation ? LBM_ENOMEM : LBM_ECUDA,
-                std::string(what) + ": " + cudaGetErrorString(e));
-}
+using lbm::cuda_fail;
+using lbm::fail;
 
 #define LBM_CUDA(call, what)                               \
     do {                                                   \
@@ -119,22 +96,7 @@ int create(lbm_ctx **out, const lbm_params *p)
     return LBM_OK;
 }
 
-// The buffers of a step that reads half `in` of f.
-lbm::StepView view(lbm_ctx *c, int in)
-{
-    const size_t n = (size_t)c->box.n;
-    const int out = 1 - in;
-    unsigned char *fq = static_cast<unsigned char *>(c->st.fq);
-    lbm::StepView v;
-    v.storage = c->p.storage;
-    v.f0_in = c->st.f0 + (size_t)in * n;
-    v.f0_out = c->st.f0 + (size_t)out * n;
-    v.fq_in = fq + (size_t)in * (lbm::kQf - 1) * n * c->esz;
-    v.fq_out = fq + (size_t)out * (lbm::kQf - 1) * n * c->esz;
-    v.g = c->st.g;
-    v.mom = c->st.mom;
-    return v;
-}
+lbm::StepView view(lbm_ctx *c, int in) { return lbm::state_view(c, in); }
 
 // Stats reduction of the mom arrays into c->result_host (synchronises).
 int reduce_stats(lbm_ctx *c)
@@ -228,6 +190,20 @@ int init_from_mom(lbm_ctx *c, const float *ghost_lo, const float *ghost_hi)
 }
 
 }  // namespace
+
+namespace lbm {
+int fail(int code, const std::string &msg)
+{
+    set_error(msg);
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char *what)
+{
+    return fail(e == cudaErrorMemoryAllocation ? LBM_ENOMEM : LBM_ECUDA,
+                std::string(what) + ": " + cudaGetErrorString(e));
+}
+}  // namespace lbm
 
 extern "C" int lbm_init(lbm_ctx **out, const lbm_params *p, const float *phi0, const float *rho0, const float *ux0,
                         const float *uy0, const float *uz0, const float *phi_ghost)

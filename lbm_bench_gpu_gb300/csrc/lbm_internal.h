@@ -74,6 +74,17 @@ struct StepView {
 
 size_t storage_bytes(int storage);   // bytes per element of fq / g
 
+// Buffers of one adjoint step (all FP32, n elements per field).
+struct AdjointBuffers {
+    const float *F, *G, *phi;          // streamed state s^n (7 + 19 fields) and its phi
+    const float *lf_in, *lg_in;        // lambda^{n+1} (f part without its stencil term)
+    const float *lst_in;               //   stencil term of lambda^{n+1}, common to the 7 f fields
+    float *lf_out, *lg_out, *lst_out;  // lambda^n
+    float *llap, *lgrad;               // scratch: lambda of the Laplacian (n) and gradient (3 n)
+    double *partials;                  // per-block partial sums (adjoint_partial_count doubles, >= 2 per block)
+    const double *ab;                  // objective sums of s^n
+};
+
 void set_error(const std::string &msg);
 const std::string &last_error();
 
@@ -104,7 +115,55 @@ cudaError_t launch_stats(const Box &b, const lbm_derived &d, const float *mom, d
                          size_t partial_count, double *result, unsigned long long *counters, cudaStream_t s);
 size_t stats_partial_count(const Box &b);
 
+// Adjoint (zsc_adjoint.cu).  acc[0] accumulates J, acc[1] dJ/dgrav (FP64).
+size_t adjoint_partial_count(const Box &b);
+cudaError_t launch_phi(const Box &b, const float *F, float *phi, cudaStream_t s);
+cudaError_t launch_objective(const Box &b, int objective, float phiStar, double scale, const float *phi,
+                             const float *G, double *partials, double *ab, double *acc, cudaStream_t s);
+cudaError_t launch_source_init(const Box &b, int objective, double scale, const double *ab, float phiStar,
+                               const float *phi, const float *G, float *lf, float *lg, float *lst, cudaStream_t s);
+cudaError_t launch_adjoint_step(const Box &b, const StepConst &c, float phiStar, const AdjointBuffers &a,
+                                bool add_source, int objective, double scale, double *acc, cudaStream_t s);
+cudaError_t launch_init_adjoint(const Box &b, const lbm_derived &d, float Gamma, const float *phi0, const float *lf,
+                                const float *lst, const float *lg, float *lphi0, float *llap, cudaStream_t s);
+
 // Number of doubles produced by launch_stats in `result`.
 constexpr int kStatsValues = 16;
 
+}  // namespace lbm
+
+// One simulation context (the opaque lbm_ctx of the C-ABI).
+struct lbm_ctx {
+    lbm_params p;
+    lbm_derived d;
+    lbm::Box box;
+    cudaStream_t stream = nullptr;
+    lbm::State st;
+    lbm::Quant q;
+    size_t esz = 4;                // bytes per element of fq / g
+    double *partials = nullptr;    // stats scratch: per-block partial sums
+    size_t partial_count = 0;
+    double *result = nullptr;      // stats result (device)
+    double *result_host = nullptr; // pinned copy
+};
+
+namespace lbm {
+// The buffers of a step that reads half `in` of f.
+inline StepView state_view(lbm_ctx *c, int in)
+{
+    const size_t n = (size_t)c->box.n;
+    const int out = 1 - in;
+    unsigned char *fq = static_cast<unsigned char *>(c->st.fq);
+    StepView v;
+    v.storage = c->p.storage;
+    v.f0_in = c->st.f0 + (size_t)in * n;
+    v.f0_out = c->st.f0 + (size_t)out * n;
+    v.fq_in = fq + (size_t)in * (kQf - 1) * n * c->esz;
+    v.fq_out = fq + (size_t)out * (kQf - 1) * n * c->esz;
+    v.g = c->st.g;
+    v.mom = c->st.mom;
+    return v;
+}
+int fail(int code, const std::string &msg);
+int cuda_fail(cudaError_t e, const char *what);
 }  // namespace lbm

@@ -58,6 +58,11 @@ def oracle_lib() -> C.CDLL:
         lib.zo_steps.argtypes = [C.c_void_p]
         lib.zo_steps.restype = C.c_long
         lib.zo_threads.restype = C.c_int
+        lib.zo_adjoint_run.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_int, C.c_int, _D, _D, _D]
+        lib.zo_adjoint_run.restype = C.c_double
+        lib.zo_objective_run.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_int, C.c_int]
+        lib.zo_objective_run.restype = C.c_double
+        lib.zo_init_adjoint.argtypes = [C.c_void_p, _D, _D, _D, _D, _D]
         _oracle_lib = lib
     return _oracle_lib
 
@@ -141,6 +146,31 @@ class Oracle:
     @property
     def steps(self) -> int:
         return int(self.lib.zo_steps(self.h))
+
+    # --- discrete adjoint (FP64) ---
+    OBJECTIVES = {"light_uz_mean": 0, "light_z_centroid": 1}
+
+    def adjoint(self, T: int, grav: float, objective: str = "light_uz_mean", window: int = 1):
+        """J, dJ/dgrav and dJ/ds^0 (f: 7 x shape, g: 19 x shape) over T steps from
+        the current state; the oracle ends at s^T."""
+        dg = C.c_double(0.0)
+        lf = np.zeros((7,) + self.shape, np.float64)
+        lg = np.zeros((19,) + self.shape, np.float64)
+        J = self.lib.zo_adjoint_run(self.h, int(T), float(grav), self.OBJECTIVES[objective], int(window),
+                                    C.byref(dg), _dptr(lf), _dptr(lg))
+        return J, dg.value, lf, lg
+
+    def objective(self, T: int, grav: float, objective: str = "light_uz_mean", window: int = 1) -> float:
+        return float(self.lib.zo_objective_run(self.h, int(T), float(grav), self.OBJECTIVES[objective], int(window)))
+
+    def init_adjoint(self, phi0, lf, lg):
+        """dJ/dphi0 and dJ/drho0 from dJ/ds^0 through the initial equilibrium (periodic z)."""
+        lphi = np.zeros(self.shape, np.float64)
+        lrho = np.zeros(self.shape, np.float64)
+        self.lib.zo_init_adjoint(self.h, _dptr(np.ascontiguousarray(phi0, np.float64)),
+                                 _dptr(np.ascontiguousarray(lf, np.float64)),
+                                 _dptr(np.ascontiguousarray(lg, np.float64)), _dptr(lphi), _dptr(lrho))
+        return lphi, lrho
 
     @staticmethod
     def threads() -> int:

@@ -515,3 +515,365 @@ int zo_threads(void)
     return 1;
 #endif
 }
+
+/* ------------------------------------------------------------------------- */
+/* Discrete adjoint (FP64).  No counterpart in the reference: it is the exact
+ * transpose of the step restated above, used to check the GPU adjoint.
+ *
+ * Objectives on the moments of a streamed state (phi = sum f, rho = sum g,
+ * u = sum c g / rho), with the smooth light-phase weight
+ * w(phi) = (phiStar - phi) / (2 phiStar):
+ *   0: mean over the last `window` states s^{T-window+1..T} of
+ *      sum(w u_z) / sum(w)                         (light-phase rise velocity)
+ *   1: sum(w z) / sum(w) of the final state s^T   (light-phase z-centroid,
+ *      z = reference plane index = z + 1)
+ * State s^k is the streamed (f, g) after k steps; s^0 the initial state.     */
+
+static double zo_objective_state(const zo_ctx *s, const double *const *f, const double *const *g, int objective,
+                                 double *A_out, double *B_out)
+{
+    const double phiStar = s->c.phiStar;
+    double A = 0.0, B = 0.0;
+#pragma omp parallel for schedule(static) reduction(+ : A, B)
+    for (long id = 0; id < s->n; id++) {
+        double ph = 0.0, rh = 0.0;
+        for (int i = 0; i < 7; i++) ph += f[i][id];
+        for (int i = 0; i < 19; i++) rh += g[i][id];
+        const double w = (phiStar - ph) / (2.0 * phiStar);
+        if (objective == 0) {
+            const double mz = g[5][id] - g[6][id] + g[11][id] - g[12][id] - g[13][id] + g[14][id] + g[15][id]
+                              - g[16][id] - g[17][id] + g[18][id];
+            A += w * mz / rh;
+        } else {
+            const long z = id / ((long)s->nx * s->ny);
+            A += w * (double)(z + 1);
+        }
+        B += w;
+    }
+    *A_out = A;
+    *B_out = B;
+    return A / B;
+}
+
+/* Add d(scale * A/B)/d(state) to (lf, lg) at every node. */
+static void zo_objective_source(const zo_ctx *s, const double *const *f, const double *const *g, int objective,
+                                double scale, double A, double B, double **lf, double **lg)
+{
+    const double phiStar = s->c.phiStar;
+    const double dw = -1.0 / (2.0 * phiStar);
+    const double ratio = A / B;
+#pragma omp parallel for schedule(static)
+    for (long id = 0; id < s->n; id++) {
+        double ph = 0.0, rh = 0.0;
+        for (int i = 0; i < 7; i++) ph += f[i][id];
+        for (int i = 0; i < 19; i++) rh += g[i][id];
+        const double w = (phiStar - ph) / (2.0 * phiStar);
+        double dphi, drho = 0.0, dmz = 0.0;
+        if (objective == 0) {
+            const double mz = g[5][id] - g[6][id] + g[11][id] - g[12][id] - g[13][id] + g[14][id] + g[15][id]
+                              - g[16][id] - g[17][id] + g[18][id];
+            const double uz = mz / rh;
+            dphi = scale * dw * (uz - ratio) / B;
+            const double duz = scale * w / B;
+            dmz = duz / rh;
+            drho = -duz * uz / rh;
+        } else {
+            const long z = id / ((long)s->nx * s->ny);
+            dphi = scale * dw * ((double)(z + 1) - ratio) / B;
+        }
+        for (int i = 0; i < 7; i++) lf[i][id] += dphi;
+        for (int i = 0; i < 19; i++) lg[i][id] += drho + (double)CG[i][2] * dmz;
+    }
+}
+
+/* One adjoint step.  In: the streamed state s^n (f, g), lambda^{n+1}
+ * (lf_in, lg_in).  Out: lambda^n (lf_out, lg_out), without objective sources;
+ * dgrav += sum over nodes of lambda_{F_z} H(phi > 0). */
+static void zo_adjoint_step(const zo_ctx *s, const double *const *f, const double *const *g, const double *const *lf_in,
+                            const double *const *lg_in, double grav, double **lf_out, double **lg_out, double *dgrav,
+                            double *phi, double *llap, double *lgx, double *lgy, double *lgz)
+{
+    const zo_const *c = &s->c;
+    (void)grav;
+#pragma omp parallel for schedule(static)
+    for (long id = 0; id < s->n; id++) {
+        double ph = 0.0;
+        for (int i = 0; i < 7; i++) ph += f[i][id];
+        phi[id] = ph;
+    }
+    double dg = 0.0;
+#pragma omp parallel for schedule(static) reduction(+ : dg)
+    for (int z = 0; z < s->nz; z++) {
+        for (int y = 0; y < s->ny; y++) {
+            for (int x = 0; x < s->nx; x++) {
+                const long id = zo_idx(s, x, y, z);
+                /* forward quantities at the node */
+                double lap, gr[3];
+                stencil(s, phi, NULL, x, y, z, &lap, &gr[0], &gr[1], &gr[2]);
+                const double ph = phi[id];
+                double rh = 0.0, m[3] = {0, 0, 0};
+                for (int i = 0; i < 19; i++) {
+                    rh += g[i][id];
+                    for (int k = 0; k < 3; k++) m[k] += CG[i][k] * g[i][id];
+                }
+                const double u[3] = {m[0] / rh, m[1] / rh, m[2] / rh};
+                const double mu = c->alpha4 * ph * (ph * ph - c->phiStarSq) - c->kappa * lap;
+                double F[3] = {mu * gr[0], mu * gr[1], mu * gr[2]};
+                const int heavy = ph > 0.0;
+                if (heavy) F[2] += grav;
+                const double us[3] = {u[0] + 0.5 * F[0] / rh, u[1] + 0.5 * F[1] / rh, u[2] + 0.5 * F[2] / rh};
+                const double v[3] = {3.0 * us[0], 3.0 * us[1], 3.0 * us[2]};
+                const double vsq6 = (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]) / 6.0;
+                const double Cf = c->invTauPhi * c->invEta2 * ph;
+
+                /* stream adjoint: lambda of the post-collision values at this node */
+                double lP[7], lQ[19];
+                lP[0] = lf_in[0][id];
+                for (int i = 1; i < 7; i++) {
+                    const long dn = zo_idx(s, wrap(x + CF[i][0], s->nx), wrap(y + CF[i][1], s->ny),
+                                           wrap(z + CF[i][2], s->nz));
+                    lP[i] = c->eta * lf_in[i][dn] + c->eta2 * lf_in[i][id];
+                }
+                for (int i = 0; i < 19; i++) {
+                    const long dn = zo_idx(s, wrap(x + CG[i][0], s->nx), wrap(y + CG[i][1], s->ny),
+                                           wrap(z + CG[i][2], s->nz));
+                    lQ[i] = lg_in[i][dn];
+                }
+
+                /* D3Q7 collision */
+                double lphi = 0.0, lmu = 0.0, lus[3] = {0, 0, 0}, lF[3] = {0, 0, 0}, lrho = 0.0;
+                {
+                    const double lAf = -6.0 * lP[0] + lP[1] + lP[2] + lP[3] + lP[4] + lP[5] + lP[6];
+                    double lCf = 0.0;
+                    for (int k = 0; k < 3; k++) {
+                        const double d = lP[1 + 2 * k] - lP[2 + 2 * k];
+                        lCf += us[k] * d;
+                        lus[k] += Cf * d;
+                    }
+                    lphi += c->invTauPhi * lP[0] + c->invTauPhi * c->invEta2 * lCf;
+                    lmu += 0.5 * c->Gamma * c->invTauPhi * lAf;
+                }
+                /* D3Q19 collision with forcing */
+                double ls = 0.0, lvsq6 = 0.0, lUF = 0.0, lv[3] = {0, 0, 0};
+                {
+                    ls += -2.0 * c->K0 * lQ[0];
+                    lrho += c->K0 * (1.0 - vsq6) * lQ[0];
+                    lvsq6 += -c->K0 * rh * lQ[0];
+                    lUF += -c->KC0 * lQ[0];
+                    double ltemp1 = 0.0;
+                    for (int k = 0; k < 3; k++) {
+                        const double S = lQ[1 + 2 * k] + lQ[2 + 2 * k], A = lQ[1 + 2 * k] - lQ[2 + 2 * k];
+                        ltemp1 += S;
+                        lrho += 0.5 * c->K1 * v[k] * v[k] * S + c->K1 * v[k] * A;
+                        lv[k] += c->K1 * rh * v[k] * S + c->KC1 * F[k] * S + (c->K1 * rh + c->KC1 * F[k]) * A;
+                        lF[k] += c->KC1 * v[k] * S + c->KC1 * v[k] * A;
+                        lUF += -c->KC1 * S;
+                    }
+                    ls += c->K1 * ltemp1;
+                    lrho += c->K1 * (1.0 - vsq6) * ltemp1;
+                    lvsq6 += -c->K1 * rh * ltemp1;
+                    /* pairs (7,8) x+y, (9,10) x-y, (11,12) x+z, (13,14) x-z, (15,16) y+z, (17,18) y-z */
+                    static const int PA[6] = {0, 0, 0, 0, 1, 1}, PB[6] = {1, 1, 2, 2, 2, 2};
+                    static const double SG[6] = {1, -1, 1, -1, 1, -1};
+                    double ltemp2 = 0.0;
+                    for (int p = 0; p < 6; p++) {
+                        const int a = PA[p], b = PB[p];
+                        const double sg = SG[p];
+                        const double w = v[a] + sg * v[b], G = F[a] + sg * F[b];
+                        const double S = lQ[7 + 2 * p] + lQ[8 + 2 * p], A = lQ[7 + 2 * p] - lQ[8 + 2 * p];
+                        ltemp2 += S;
+                        lrho += 0.5 * c->K2 * w * w * S + c->K2 * w * A;
+                        const double lw = c->K2 * rh * w * S + c->KC2 * G * S + c->K2 * rh * A;
+                        const double lG = c->KC2 * w * S + c->KC2 * A;
+                        lUF += -c->KC2 * S;
+                        lv[a] += lw;
+                        lv[b] += sg * lw;
+                        lF[a] += lG;
+                        lF[b] += sg * lG;
+                    }
+                    ls += c->K2 * ltemp2;
+                    lrho += c->K2 * (1.0 - vsq6) * ltemp2;
+                    lvsq6 += -c->K2 * rh * ltemp2;
+                }
+                for (int k = 0; k < 3; k++) lv[k] += lvsq6 * v[k] / 3.0;
+                for (int k = 0; k < 3; k++) {
+                    lus[k] += lUF * F[k] + 3.0 * lv[k];
+                    lF[k] += lUF * us[k];
+                }
+                lphi += 3.0 * mu * ls;
+                lmu += 3.0 * ph * ls;
+                /* us = u + 0.5 F / rho, u = m / rho */
+                double lm[3];
+                for (int k = 0; k < 3; k++) {
+                    lF[k] += 0.5 * lus[k] / rh;
+                    lrho += -0.5 * lus[k] * F[k] / (rh * rh);
+                    lm[k] = lus[k] / rh;
+                    lrho += -lus[k] * u[k] / rh;
+                }
+                /* F = mu grad (+ grav on phi > 0) */
+                for (int k = 0; k < 3; k++) lmu += gr[k] * lF[k];
+                if (heavy) dg += lF[2];
+                lgx[id] = mu * lF[0];
+                lgy[id] = mu * lF[1];
+                lgz[id] = mu * lF[2];
+                /* mu = alpha4 phi (phi^2 - phiStar^2) - kappa lap */
+                lphi += c->alpha4 * (3.0 * ph * ph - c->phiStarSq) * lmu;
+                llap[id] = -c->kappa * lmu;
+                /* collisions' direct terms and the moments */
+                lf_out[0][id] = c->invTauPhiOne * lP[0] + lphi;
+                for (int i = 1; i < 7; i++) lf_out[i][id] = c->invTauPhiOne * lP[i] + lphi;
+                for (int i = 0; i < 19; i++)
+                    lg_out[i][id] = c->invTauRhoOne * lQ[i] + lrho + CG[i][0] * lm[0] + CG[i][1] * lm[1]
+                                    + CG[i][2] * lm[2];
+            }
+        }
+    }
+    *dgrav += dg;
+    /* transposed stencils: lapT = lap (symmetric), gradT = -grad (antisymmetric) */
+#pragma omp parallel for schedule(static)
+    for (int z = 0; z < s->nz; z++) {
+        for (int y = 0; y < s->ny; y++) {
+            for (int x = 0; x < s->nx; x++) {
+                const long id = zo_idx(s, x, y, z);
+                double l1, d, gxv, gyv, gzv;
+                stencil(s, llap, NULL, x, y, z, &l1, &d, &d, &d);
+                stencil(s, lgx, NULL, x, y, z, &d, &gxv, &d, &d);
+                stencil(s, lgy, NULL, x, y, z, &d, &d, &gyv, &d);
+                stencil(s, lgz, NULL, x, y, z, &d, &d, &d, &gzv);
+                const double add = l1 - gxv - gyv - gzv;
+                for (int i = 0; i < 7; i++) lf_out[i][id] += add;
+            }
+        }
+    }
+}
+
+/* J and its adjoint over T steps from the current state s^0, storing every
+ * state (test sizes).  dgrav receives dJ/dgrav; lf0 (7N) / lg0 (19N) receive
+ * dJ/ds^0.  The context ends at s^T. */
+double zo_adjoint_run(zo_ctx *s, int T, double grav, int objective, int window, double *dgrav, double *lf0,
+                      double *lg0)
+{
+    const long N = s->n;
+    double *store = (double *)malloc(sizeof(double) * 26 * N * (size_t)(T + 1));
+    double *work = (double *)calloc((size_t)(26 * 2 + 5) * N, sizeof(double));
+    if (!store || !work) {
+        free(store);
+        free(work);
+        return NAN;
+    }
+    for (int i = 0; i < 7; i++) memcpy(store + (long)i * N, s->f[i], sizeof(double) * N);
+    for (int i = 0; i < 19; i++) memcpy(store + (long)(7 + i) * N, s->g[i], sizeof(double) * N);
+    for (int k = 1; k <= T; k++) {
+        zo_step(s, 1, grav);
+        double *st = store + (size_t)k * 26 * N;
+        for (int i = 0; i < 7; i++) memcpy(st + (long)i * N, s->f[i], sizeof(double) * N);
+        for (int i = 0; i < 19; i++) memcpy(st + (long)(7 + i) * N, s->g[i], sizeof(double) * N);
+    }
+    double *la[26], *lb[26];
+    for (int i = 0; i < 26; i++) {
+        la[i] = work + (long)i * N;
+        lb[i] = work + (long)(26 + i) * N;
+    }
+    double *phi = work + 52L * N, *llap = work + 53L * N, *lgx = work + 54L * N, *lgy = work + 55L * N,
+           *lgz = work + 56L * N;
+    const double *fk[7], *gk[19];
+    double J = 0.0, A, B;
+    const int first = objective == 0 ? T - window + 1 : T;
+    const double scale = objective == 0 ? 1.0 / window : 1.0;
+    /* lambda^T: source of the final state */
+    {
+        double *st = store + (size_t)T * 26 * N;
+        for (int i = 0; i < 7; i++) fk[i] = st + (long)i * N;
+        for (int i = 0; i < 19; i++) gk[i] = st + (long)(7 + i) * N;
+        J += scale * zo_objective_state(s, fk, gk, objective, &A, &B);
+        zo_objective_source(s, fk, gk, objective, scale, A, B, la, la + 7);
+    }
+    *dgrav = 0.0;
+    for (int k = T - 1; k >= 0; k--) {
+        double *st = store + (size_t)k * 26 * N;
+        for (int i = 0; i < 7; i++) fk[i] = st + (long)i * N;
+        for (int i = 0; i < 19; i++) gk[i] = st + (long)(7 + i) * N;
+        zo_adjoint_step(s, fk, gk, (const double *const *)la, (const double *const *)(la + 7), grav, lb, lb + 7,
+                        dgrav, phi, llap, lgx, lgy, lgz);
+        if (k >= first) {
+            J += scale * zo_objective_state(s, fk, gk, objective, &A, &B);
+            zo_objective_source(s, fk, gk, objective, scale, A, B, lb, lb + 7);
+        }
+        for (int i = 0; i < 26; i++) {
+            double *t = la[i];
+            la[i] = lb[i];
+            lb[i] = t;
+        }
+    }
+    for (int i = 0; i < 7; i++) memcpy(lf0 + (long)i * N, la[i], sizeof(double) * N);
+    for (int i = 0; i < 19; i++) memcpy(lg0 + (long)i * N, la[7 + i], sizeof(double) * N);
+    free(store);
+    free(work);
+    return J;
+}
+
+/* J alone (forward only), for finite differences. */
+double zo_objective_run(zo_ctx *s, int T, double grav, int objective, int window)
+{
+    const int first = objective == 0 ? T - window + 1 : T;
+    const double scale = objective == 0 ? 1.0 / window : 1.0;
+    double J = 0.0, A, B;
+    const double *fk[7], *gk[19];
+    for (int k = 0; k <= T; k++) {
+        if (k > 0) zo_step(s, 1, grav);
+        if (k >= first) {
+            for (int i = 0; i < 7; i++) fk[i] = s->f[i];
+            for (int i = 0; i < 19; i++) gk[i] = s->g[i];
+            J += scale * zo_objective_state(s, fk, gk, objective, &A, &B);
+        }
+    }
+    return J;
+}
+
+/* dJ/dphi0 and dJ/drho0 from dJ/ds^0 through the initial equilibrium
+ * (src/init_f.cu:57-78, src/init_g.cu:69-91) with periodic z. */
+void zo_init_adjoint(const zo_ctx *s, const double *phi0, const double *lf0, const double *lg0, double *lphi0,
+                     double *lrho0)
+{
+    const zo_const *c = &s->c;
+    const long N = s->n;
+    double *llap = (double *)malloc(sizeof(double) * N);
+#pragma omp parallel for schedule(static)
+    for (int z = 0; z < s->nz; z++) {
+        for (int y = 0; y < s->ny; y++) {
+            for (int x = 0; x < s->nx; x++) {
+                const long id = zo_idx(s, x, y, z);
+                double lap, gx, gy, gz;
+                stencil(s, phi0, NULL, x, y, z, &lap, &gx, &gy, &gz);
+                const double ph = phi0[id];
+                const double mu = c->alpha4 * ph * (ph * ph - c->phiStarSq) - c->kappa * lap;
+                const double l0 = lf0[id];
+                double lfs = 0.0, lga = 0.0, lgd = 0.0;
+                for (int i = 1; i < 7; i++) lfs += lf0[i * N + id];
+                for (int i = 1; i < 7; i++) lga += lg0[i * N + id];
+                for (int i = 7; i < 19; i++) lgd += lg0[i * N + id];
+                const double lg00 = lg0[id];
+                /* f0 = phi - 3 Gamma mu; fi = Gamma mu / 2; g0 = W0 (rho - 6 phi mu);
+                 * g axis = W1 (3 phi mu + rho); g diag = W2 (3 phi mu + rho) */
+                const double lmu = -3.0 * c->Gamma * l0 + 0.5 * c->Gamma * lfs - 6.0 * ZO_W0 * ph * lg00
+                                   + 3.0 * ZO_W1 * ph * lga + 3.0 * ZO_W2 * ph * lgd;
+                double lphi = l0 - 6.0 * ZO_W0 * mu * lg00 + 3.0 * ZO_W1 * mu * lga + 3.0 * ZO_W2 * mu * lgd;
+                lphi += c->alpha4 * (3.0 * ph * ph - c->phiStarSq) * lmu;
+                llap[id] = -c->kappa * lmu;
+                lphi0[id] = lphi;
+                if (lrho0) lrho0[id] = ZO_W0 * lg00 + ZO_W1 * lga + ZO_W2 * lgd;
+            }
+        }
+    }
+#pragma omp parallel for schedule(static)
+    for (int z = 0; z < s->nz; z++) {
+        for (int y = 0; y < s->ny; y++) {
+            for (int x = 0; x < s->nx; x++) {
+                double l1, d;
+                stencil(s, llap, NULL, x, y, z, &l1, &d, &d, &d);
+                lphi0[zo_idx(s, x, y, z)] += l1;
+            }
+        }
+    }
+    free(llap);
+}

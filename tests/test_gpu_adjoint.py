@@ -1,0 +1,69 @@
+"""lbm_step_adjoint (GPU, FP32 with FP64 sums) against the FP64 CPU adjoint
+of the oracle (itself checked against FP64 finite differences in
+test_adjoint_oracle.py).  Tolerances: J 1e-5 relative; dJ/dgrav 1e-3
+relative; dJ/dphi0 max |error| <= 2e-3 max |dJ/dphi0| (the FP32 adjoint sums
+~20 terms per node and step)."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from oracle.oracle import Oracle
+
+pytestmark = pytest.mark.gpu
+
+KW = dict(rhoL=0.1, rhoH=1.0, tauRho=0.7, tauPhi=0.9, width=4.0, sigma=1e-3, Gamma=1.0)
+SHAPE = (16, 32, 32)
+
+
+def fields():
+    o = Oracle(32, 32, 16, **KW)
+    pg = o.bubble_phi(np.array([[15.5, 16.3, 8.4, 6.0], [5.0, 6.0, 12.0, 3.5]], np.float32))
+    return pg[1:-1].copy(), np.full(SHAPE, 0.55)
+
+
+@pytest.mark.parametrize("objective,window,T", [("light_uz_mean", 5, 12), ("light_z_centroid", 1, 10)])
+def test_gpu_adjoint_matches_oracle(lib, objective, window, T):
+    from lbm_bench_gpu_gb300 import capi
+    phi0, rho0 = fields()
+    grav = -3e-5
+    p = capi.make_params(32, 32, 16, **KW)
+    o = Oracle.from_params(p)
+    o.init(phi0.astype(np.float32).astype(np.float64), rho0)
+    J, dg, lf, lg = o.adjoint(T, grav, objective, window)
+    lphi, _ = o.init_adjoint(phi0.astype(np.float32).astype(np.float64), lf, lg)
+    with capi.Lattice.from_fields(p, phi0.astype(np.float32), rho0.astype(np.float32)) as lat:
+        r = lat.adjoint(T, grav, objective, window)
+        assert lat.steps == 0
+    assert r["adjoint_steps"] == T
+    assert r["J"] == pytest.approx(J, rel=1e-5)
+    assert r["dJ_dgrav"] == pytest.approx(dg, rel=1e-3)
+    err = np.abs(r["dJ_dphi0"] - lphi).max()
+    assert err <= 2e-3 * np.abs(lphi).max(), err / np.abs(lphi).max()
+
+
+def test_checkpoint_budget_does_not_change_the_gradient(lib):
+    """3 slots for 20 steps forces recomputation (binomial schedule); the
+    trajectory is deterministic, so J and the gradients are identical."""
+    from lbm_bench_gpu_gb300 import capi
+    phi0, rho0 = fields()
+    p = capi.make_params(32, 32, 16, **KW)
+    with capi.Lattice.from_fields(p, phi0.astype(np.float32), rho0.astype(np.float32)) as lat:
+        full = lat.adjoint(20, -3e-5, "light_uz_mean", 6)
+        snap = 26 * 4 * 32 * 32 * 16
+        tight = lat.adjoint(20, -3e-5, "light_uz_mean", 6, checkpoint_bytes=3.5 * snap)
+    assert full["slots"] == 21 and tight["slots"] == 3
+    assert full["forward_steps"] == 20 and tight["forward_steps"] > 20
+    assert tight["J"] == full["J"] and tight["dJ_dgrav"] == full["dJ_dgrav"]
+    assert np.array_equal(tight["dJ_dphi0"], full["dJ_dphi0"])
+
+
+def test_adjoint_needs_initial_state(lib):
+    from lbm_bench_gpu_gb300 import capi
+    phi0, rho0 = fields()
+    p = capi.make_params(32, 32, 16, **KW)
+    with capi.Lattice.from_fields(p, phi0.astype(np.float32), rho0.astype(np.float32)) as lat:
+        lat.step(1)
+        with pytest.raises(capi.LbmError) as e:
+            lat.adjoint(5, -3e-5)
+        assert e.value.code == capi.LBM_ESTATE
