@@ -53,6 +53,9 @@ def parse_args(argv=None):
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-variants", action="store_true", help="time only --storage (not the other formats)")
     ap.add_argument("--stat-every", type=int, default=100, help="lbm_stats cadence inside the e2e run")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint / forward time ratio")
+    ap.add_argument("--adjoint-long", action="store_true",
+                    help="also run the long-horizon adjoint (256^3, 64 bubbles, T = 20000, FP16 state, 40 GB)")
     return ap.parse_args(argv)
 
 
@@ -287,9 +290,67 @@ def run_ours(args, rank, world, local):
         result["storage_variants"] = variants
     if rank == 0 and not args.no_e2e:
         result["e2e"] = run_e2e(args, inp, p, grav, local)
+    if rank == 0 and not args.no_adjoint:
+        result["adjoint"] = run_adjoint(local)
+        if args.adjoint_long:
+            result["adjoint_long"] = run_adjoint(local, long_horizon=True)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         result["cpu_baseline"] = cpu_baseline(inp)
     return result
+
+
+def run_adjoint(local, long_horizon=False):
+    """Adjoint / forward wall-time ratio through lbm_step_adjoint.
+
+    short: 128^3, 8 bubbles R = 10, tau_rho = 0.8, gravity -1e-6, T = 2000,
+           J = light-phase mean u_z over the last 200 states, FP32 state;
+    long:  256^3, 64 bubbles R ~ U[6, 10], T = 20000, J = final light-phase
+           z-centroid, FP16 live state.
+    Both with a 40 GB checkpoint budget.  dJ/dgrav is checked against central
+    differences of the same (GPU) forward run, step 1e-6 on the force."""
+    import torch
+    from lbm_bench_gpu_gb300 import capi, inputs
+    if long_horizon:
+        inp = inputs.bubbly(256, 64, gravity=-1e-6, tauRho=0.7)
+        T, objective, window, storage = 20000, "light_z_centroid", 1, "fp16"
+    else:
+        inp = inputs.adjoint_short()
+        T, objective, window, storage = 2000, "light_uz_mean", 200, "fp32"
+    p = params_for(inp, storage, local)
+    grav = float(capi.derive(p).grav)
+    budget = 40e9
+
+    def forward_J(g):
+        with capi.Lattice.from_bubbles(p, inp.bubbles) as lat:
+            lat.sync()
+            t0 = time.perf_counter()
+            lat.step(T, g)
+            lat.sync()
+            return time.perf_counter() - t0
+
+    t_fwd = min(forward_J(grav) for _ in range(2))
+    with capi.Lattice.from_bubbles(p, inp.bubbles) as lat:
+        lat.sync()
+        torch.cuda.synchronize()
+        r = lat.adjoint(T, grav, objective, window, checkpoint_bytes=budget)
+        Jp = lat.adjoint(T, grav + 1e-6, objective, window, checkpoint_bytes=budget, want_phi0=False)["J"] \
+            if not long_horizon else None
+        Jm = lat.adjoint(T, grav - 1e-6, objective, window, checkpoint_bytes=budget, want_phi0=False)["J"] \
+            if not long_horizon else None
+    out = {"workload": ("long: 256^3, 64 bubbles, T=20000, final light-phase z-centroid, FP16 state"
+                        if long_horizon else
+                        "short: 128^3, 8 bubbles R=10, tau_rho=0.8, T=2000, light-phase mean u_z over the "
+                        "last 200 states, FP32 state"),
+           "T": T, "forward_s": round(t_fwd, 4), "adjoint_s": round(r["seconds"], 4),
+           "ratio": round(r["seconds"] / t_fwd, 3), "slots": r["slots"],
+           "checkpoint_GB": round(r["checkpoint_bytes_used"] / 1e9, 2), "forward_steps": r["forward_steps"],
+           "J": r["J"], "dJ_dgrav": r["dJ_dgrav"],
+           "dJ_dphi0_norm": float(np.sqrt((r["dJ_dphi0"].astype(np.float64) ** 2).sum()))}
+    if Jp is not None:
+        fd = (Jp - Jm) / 2e-6
+        out["fd_dJ_dgrav"] = fd
+        out["fd_rel_err"] = abs(r["dJ_dgrav"] - fd) / abs(fd)
+    return out
 
 
 def run_e2e(args, inp, p, grav, local):

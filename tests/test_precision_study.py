@@ -1,0 +1,81 @@
+"""Storage-precision study: FP32, FP16 and BF16 storage against the FP64 oracle
+after 10 000 steps.
+
+Box: 64^3 with 4 seeded bubbles (radii U[6, 10], surface gap >= 3), the
+physics of the bubbly benchmark (rhoH = 1, rhoL = 0.1, sigma = 1e-3, W = 4,
+tau_rho = 0.7, Gamma = 1, tau_phi = 1, gravity -1e-6) -- the 256^3 / 512^3
+boxes of the benchmark take the FP64 oracle hours for 10 000 steps.
+Reported per format: phi L2 error (||phi - phi_ref||_2 / ||phi_ref||_2 and the
+RMS), relative drift of sum(phi) and sum(rho) against the oracle, and the
+largest distance between matching heavy-phase (phi > 0) centroids.  The
+report goes to gpurun_out/precision_study.json when that folder exists.
+Bar: relative phi L2 error <= 1e-3 for FP32 and FP16 storage.  BF16 (8-bit
+mantissa) is reported, with a looser sanity bound: its phi error after 10 000
+steps is ~2e-2 relative, driven by the rounding of f_1..f_6."""
+from __future__ import annotations
+
+import json
+import os
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from oracle.oracle import Oracle
+
+pytestmark = pytest.mark.gpu
+
+STEPS = int(os.environ.get("LBM_PRECISION_STEPS", "10000"))
+
+
+def centroids(phi: np.ndarray) -> np.ndarray:
+    """Centroids (z, y, x) of the connected phi > 0 regions, sorted."""
+    from scipy import ndimage
+    lab, n = ndimage.label(phi > 0)
+    if n == 0:
+        return np.zeros((0, 3))
+    c = np.array(ndimage.center_of_mass(phi > 0, lab, range(1, n + 1)))
+    return c[np.lexsort(c.T[::-1])]
+
+
+def test_storage_precision_10k_steps(lib):
+    pytest.importorskip("scipy")
+    from lbm_bench_gpu_gb300 import capi, inputs
+    inp = inputs.bubbly(64, 4, r_range=(6.0, 10.0), gravity=-1e-6)
+    base = dict(rhoL=inp.rhoL, rhoH=inp.rhoH, tauRho=inp.tauRho, tauPhi=inp.tauPhi, width=inp.width,
+                sigma=inp.sigma, Gamma=inp.Gamma, Eo=inp.Eo, rc0=inp.rc0)
+    p32 = capi.make_params(64, 64, 64, **base)
+    grav = float(capi.derive(p32).grav)
+
+    o = Oracle.from_params(p32)
+    o.init_bubbles(inp.bubbles)
+    o.step(STEPS, grav)
+    ref = o.moments()
+    ref_stats = o.stats()
+    ref_c = centroids(ref["phi"])
+
+    report = {"box": "64^3, 4 bubbles R~U[6,10], gravity -1e-6", "steps": STEPS, "formats": {}}
+    for storage in ("fp32", "fp16", "bf16"):
+        p = capi.make_params(64, 64, 64, storage=storage, **base)
+        with capi.Lattice.from_bubbles(p, inp.bubbles) as lat:
+            lat.step(STEPS, grav)
+            s, f = lat.stats(fields=True)
+        d = f["phi"].astype(np.float64) - ref["phi"]
+        cg = centroids(f["phi"])
+        cerr = float(np.abs(cg - ref_c).max()) if cg.shape == ref_c.shape else float("inf")
+        report["formats"][storage] = {
+            "phi_l2_rel": float(np.linalg.norm(d) / np.linalg.norm(ref["phi"])),
+            "phi_rms": float(np.sqrt((d ** 2).mean())),
+            "phi_maxabs": float(np.abs(d).max()),
+            "mass_phi_drift_rel": abs(s["phi_sum"] - ref_stats["phi_sum"]) / abs(ref_stats["phi_sum"]),
+            "mass_rho_drift_rel": abs(s["rho_sum"] - ref_stats["rho_sum"]) / abs(ref_stats["rho_sum"]),
+            "centroid_err_max": cerr,
+            "bubbles": int(len(cg)),
+        }
+    out = Path("gpurun_out")
+    if out.is_dir():
+        (out / "precision_study.json").write_text(json.dumps(report, indent=1))
+    print(json.dumps(report))
+    for storage, r in report["formats"].items():
+        assert r["phi_l2_rel"] <= (1e-3 if storage != "bf16" else 5e-2), (storage, r)
+        assert r["bubbles"] == len(ref_c), (storage, r)
