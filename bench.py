@@ -305,9 +305,13 @@ def run_adjoint(local, long_horizon=False):
     short: 128^3, 8 bubbles R = 10, tau_rho = 0.8, gravity -1e-6, T = 2000,
            J = light-phase mean u_z over the last 200 states, FP32 state;
     long:  256^3, 64 bubbles R ~ U[6, 10], T = 20000, J = final light-phase
-           z-centroid, FP16 live state.
-    Both with a 40 GB checkpoint budget.  dJ/dgrav is checked against central
-    differences of the same (GPU) forward run, step 1e-6 on the force."""
+           z-centroid, FP16 live state (native FP16 snapshots).
+    Both with a 40 GB checkpoint budget.  The forward time is lbm_step over T
+    steps on the same context.  dJ/dgrav is checked against central
+    differences of J from lbm_objective (the GPU forward run) with steps
+    h = 1e-6, 5e-7 and 2.5e-7 on the force, and their Richardson extrapolation;
+    on the short run dJ/dphi0 is checked the same way (h = 1e-4) on 16 seeded
+    random nodes among those with |dJ/dphi0| above 10% of its maximum."""
     import torch
     from lbm_bench_gpu_gb300 import capi, inputs
     if long_horizon:
@@ -320,7 +324,11 @@ def run_adjoint(local, long_horizon=False):
     grav = float(capi.derive(p).grav)
     budget = 40e9
 
-    def forward_J(g):
+    with capi.Lattice.from_bubbles(p, inp.bubbles) as lat:
+        phi0 = lat.fields()["phi"]
+        rho0 = lat.fields()["rho"]
+
+    def forward_time(g):
         with capi.Lattice.from_bubbles(p, inp.bubbles) as lat:
             lat.sync()
             t0 = time.perf_counter()
@@ -328,15 +336,16 @@ def run_adjoint(local, long_horizon=False):
             lat.sync()
             return time.perf_counter() - t0
 
-    t_fwd = min(forward_J(grav) for _ in range(2))
-    with capi.Lattice.from_bubbles(p, inp.bubbles) as lat:
+    t_fwd = min(forward_time(grav) for _ in range(2))
+    with capi.Lattice.from_fields(p, phi0, rho0) as lat:
         lat.sync()
         torch.cuda.synchronize()
         r = lat.adjoint(T, grav, objective, window, checkpoint_bytes=budget)
-        Jp = lat.adjoint(T, grav + 1e-6, objective, window, checkpoint_bytes=budget, want_phi0=False)["J"] \
-            if not long_horizon else None
-        Jm = lat.adjoint(T, grav - 1e-6, objective, window, checkpoint_bytes=budget, want_phi0=False)["J"] \
-            if not long_horizon else None
+        fd = {}
+        for h in (1e-6, 5e-7, 2.5e-7):
+            fd[h] = (lat.objective(T, grav + h, objective, window)
+                     - lat.objective(T, grav - h, objective, window)) / (2 * h)
+    rich = (4 * fd[5e-7] - fd[1e-6]) / 3
     out = {"workload": ("long: 256^3, 64 bubbles, T=20000, final light-phase z-centroid, FP16 state"
                         if long_horizon else
                         "short: 128^3, 8 bubbles R=10, tau_rho=0.8, T=2000, light-phase mean u_z over the "
@@ -345,11 +354,28 @@ def run_adjoint(local, long_horizon=False):
            "ratio": round(r["seconds"] / t_fwd, 3), "slots": r["slots"],
            "checkpoint_GB": round(r["checkpoint_bytes_used"] / 1e9, 2), "forward_steps": r["forward_steps"],
            "J": r["J"], "dJ_dgrav": r["dJ_dgrav"],
+           "fd_dJ_dgrav": {f"{h:g}": v for h, v in fd.items()}, "fd_richardson": rich,
+           "fd_rel_err": abs(r["dJ_dgrav"] - fd[1e-6]) / abs(fd[1e-6]),
+           "fd_rel_err_richardson": abs(r["dJ_dgrav"] - rich) / abs(rich),
            "dJ_dphi0_norm": float(np.sqrt((r["dJ_dphi0"].astype(np.float64) ** 2).sum()))}
-    if Jp is not None:
-        fd = (Jp - Jm) / 2e-6
-        out["fd_dJ_dgrav"] = fd
-        out["fd_rel_err"] = abs(r["dJ_dgrav"] - fd) / abs(fd)
+    if not long_horizon:
+        g0 = r["dJ_dphi0"]
+        big = np.flatnonzero(np.abs(g0) > 0.1 * np.abs(g0).max())
+        nodes = np.random.default_rng(20261203).choice(big, size=min(16, len(big)), replace=False)
+        h = 1e-4
+        errs = []
+        for k in nodes:
+            vals = []
+            for sgn in (1, -1):
+                ph = phi0.copy()
+                ph.flat[k] += sgn * h
+                with capi.Lattice.from_fields(p, ph, rho0) as lat:
+                    vals.append(lat.objective(T, grav, objective, window))
+            fdk = (vals[0] - vals[1]) / (2 * h)
+            errs.append(abs(float(g0.flat[k]) - fdk) / max(abs(fdk), 1e-300))
+        out["phi0_fd_nodes"] = len(nodes)
+        out["phi0_fd_rel_err_max"] = float(max(errs))
+        out["phi0_fd_rel_err_median"] = float(np.median(errs))
     return out
 
 

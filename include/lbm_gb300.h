@@ -184,6 +184,13 @@ typedef struct lbm_adjoint_out {
  * z.  On return the context holds the initial state again.  Synchronises. */
 int lbm_step_adjoint(lbm_ctx *c, const lbm_adjoint_opts *o, lbm_adjoint_out *out);
 
+/* The objective of lbm_step_adjoint alone (forward run, no gradient), e.g.
+ * for finite-difference checks of the gradient: o->checkpoint_bytes is
+ * ignored, one state snapshot is held.  No counterpart in the reference.
+ * Same preconditions; on return the context holds the initial state again.
+ * Synchronises. */
+int lbm_objective(lbm_ctx *c, const lbm_adjoint_opts *o, double *J);
+
 /* Largest box lbm_stats_noalloc accepts: 512^3 nodes. */
 #define LBM_NOALLOC_MAX_NODES 134217728LL
 /* Number of doubles lbm_stats_noalloc writes. */

@@ -23,6 +23,7 @@ EXPORTS = [
     "lbm_read_inputs", "lbm_derive", "lbm_init", "lbm_init_bubbles", "lbm_step", "lbm_stats",
     "lbm_get_dist", "lbm_set_dist", "lbm_steps_done", "lbm_stream", "lbm_sync", "lbm_destroy",
     "lbm_strerror", "lbm_last_error", "lbm_stats_noalloc", "lbm_step_adjoint",
+    "lbm_objective",
 ]
 OBJECTIVES = {"light_uz_mean": 0, "light_z_centroid": 1}
 
@@ -107,6 +108,7 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.lbm_stats_noalloc.argtypes = [C.POINTER(Params), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                       C.c_void_p, C.c_void_p, C.c_void_p]
     lib.lbm_step_adjoint.argtypes = [C.c_void_p, C.POINTER(AdjointOpts), C.POINTER(AdjointOut)]
+    lib.lbm_objective.argtypes = [C.c_void_p, C.POINTER(AdjointOpts), C.POINTER(C.c_double)]
     lib.lbm_steps_done.argtypes = [C.c_void_p]
     lib.lbm_steps_done.restype = C.c_longlong
     lib.lbm_stream.argtypes = [C.c_void_p]
@@ -237,6 +239,13 @@ class Lattice:
         return {"J": out.J, "dJ_dgrav": out.dJ_dgrav, "dJ_dphi0": grad, "slots": out.slots,
                 "forward_steps": out.forward_steps, "adjoint_steps": out.adjoint_steps, "seconds": out.seconds,
                 "checkpoint_bytes_used": out.checkpoint_bytes_used}
+
+    def objective(self, nsteps: int, grav: float, objective: str = "light_uz_mean", window: int = 1) -> float:
+        """lbm_objective: J alone over nsteps from the initial state (forward run)."""
+        o = AdjointOpts(OBJECTIVES[objective], int(nsteps), int(window), float(grav), 0.0)
+        J = C.c_double()
+        check(load().lbm_objective(self._h, C.byref(o), C.byref(J)), "lbm_objective")
+        return float(J.value)
 
     @property
     def steps(self) -> int:

@@ -1,0 +1,59 @@
+// lattice.cuh -- lattice vectors of the reference's D3Q7 / D3Q19 order and the
+// storage element formats, shared by the step and adjoint kernels.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include "lbm_internal.h"
+
+namespace lbm {
+
+// D3Q19 lattice vectors and opposite directions (reference order,
+// src/stream_g.cu:58-76; the first seven are the D3Q7 set, src/stream_f.cu:54-59).
+__host__ __device__ constexpr int kCx(int i)
+{
+    return (i == 1 || i == 7 || i == 9 || i == 11 || i == 13) ? 1
+           : (i == 2 || i == 8 || i == 10 || i == 12 || i == 14) ? -1 : 0;
+}
+__host__ __device__ constexpr int kCy(int i)
+{
+    return (i == 3 || i == 7 || i == 10 || i == 15 || i == 17) ? 1
+           : (i == 4 || i == 8 || i == 9 || i == 16 || i == 18) ? -1 : 0;
+}
+__host__ __device__ constexpr int kCz(int i)
+{
+    return (i == 5 || i == 11 || i == 14 || i == 15 || i == 18) ? 1
+           : (i == 6 || i == 12 || i == 13 || i == 16 || i == 17) ? -1 : 0;
+}
+__host__ __device__ constexpr int kOpp(int i) { return i == 0 ? 0 : ((i & 1) ? i + 1 : i - 1); }
+
+// Storage formats: element conversions, and the resident blocks per SM the
+// step kernel's launch bounds ask for.  FP32 stages 108 KB of shared memory
+// per block (2 blocks per SM); the 16-bit formats stage 70 KB, and 3 blocks per
+// SM fit when the kernel stays within 85 registers (it does, without spills).
+template <typename ST>
+struct Fmt;
+template <>
+struct Fmt<float> {
+    static constexpr int kMinBlocks = 2;
+    static constexpr bool kMapped = false;
+    __device__ static float load(float v) { return v; }
+    __device__ static float store(float v) { return v; }
+};
+template <>
+struct Fmt<__half> {
+    static constexpr int kMinBlocks = 3;
+    static constexpr bool kMapped = true;
+    __device__ static float load(__half v) { return __half2float(v); }
+    __device__ static __half store(float v) { return __float2half_rn(v); }
+};
+template <>
+struct Fmt<__nv_bfloat16> {
+    static constexpr int kMinBlocks = 3;
+    static constexpr bool kMapped = true;
+    __device__ static float load(__nv_bfloat16 v) { return __bfloat162float(v); }
+    __device__ static __nv_bfloat16 store(float v) { return __float2bfloat16_rn(v); }
+};
+
+}  // namespace lbm

@@ -46,11 +46,12 @@ struct Adjoint {
     lbm_adjoint_opts o;
     size_t n, snap_bytes;
     // work buffers
-    float *F = nullptr, *G = nullptr, *phi = nullptr;
+    float *phi = nullptr;
     float *lam[2] = {nullptr, nullptr};   // 26 x n each: f (7) then g (19)
     float *lst[2] = {nullptr, nullptr};
-    float *llap = nullptr, *lgrad = nullptr, *phi0 = nullptr, *mom_save = nullptr;
-    double *partials = nullptr, *ab = nullptr, *acc = nullptr;
+    float4 *lsrc = nullptr;
+    float *phi0 = nullptr, *mom_save = nullptr;
+    double *partials = nullptr, *dgrav = nullptr, *ab = nullptr, *acc = nullptr;
     unsigned char *slots = nullptr;
     std::vector<Snapshot> snaps;
     std::vector<int> free_slots;
@@ -62,6 +63,22 @@ struct Adjoint {
     double scale;
 
     unsigned char *slot_ptr(int s) { return slots + (size_t)s * snap_bytes; }
+
+    // the state in slot s, read in place
+    lbm::NativeState slot_state(int s)
+    {
+        const unsigned char *d = slot_ptr(s);
+        const size_t b0 = sizeof(float) * n, bq = c->esz * (lbm::kQf - 1) * n;
+        return lbm::NativeState{c->p.storage, reinterpret_cast<const float *>(d), d + b0, d + b0 + bq,
+                                snaps[s].f_streamed, snaps[s].g_odd_next};
+    }
+
+    // the context's current state
+    lbm::NativeState ctx_state()
+    {
+        const lbm::StepView v = lbm::state_view(c, c->st.f_cur);
+        return lbm::NativeState{c->p.storage, v.f0_in, v.fq_in, v.g, c->st.f_streamed, c->st.g_odd_next};
+    }
 
     int save(int s, long long step)
     {
@@ -102,13 +119,58 @@ struct Adjoint {
         return lbm_step(c, (int)nsteps, o.grav);
     }
 
-    // streamed FP32 copy of the current state and its phi
-    int prepare()
+    // One step of the state src (at step `step`) with its output in the
+    // context (f half 0) or in slot `to`: checkpoints are read and written in
+    // place, never copied through the context.
+    int step_out_of_place(const lbm::NativeState &src, long long step, int to)
     {
-        cudaError_t e = lbm::launch_stream_out(c->box, c->d.eta, c->q, lbm::state_view(c, c->st.f_cur),
-                                               c->st.f_streamed, c->st.g_odd_next, F, G, c->stream);
-        if (e == cudaSuccess) e = lbm::launch_phi(c->box, F, phi, c->stream);
-        return e == cudaSuccess ? LBM_OK : cuda_fail(e, "adjoint: prepare");
+        lbm::StepView v = lbm::state_view(c, 1);   // f out: half 0
+        v.f0_in = src.f0;
+        v.fq_in = src.fq;
+        v.g_in = src.g;
+        if (to >= 0) {
+            unsigned char *d = slot_ptr(to);
+            const size_t b0 = sizeof(float) * n, bq = c->esz * (lbm::kQf - 1) * n;
+            v.f0_out = reinterpret_cast<float *>(d);
+            v.fq_out = d + b0;
+            v.g = d + b0 + bq;
+        }
+        cudaError_t e = lbm::launch_step(c->box, k, c->q, v, src.f_streamed, src.g_odd, false, c->stream);
+        if (e != cudaSuccess) return cuda_fail(e, "adjoint: step kernel launch");
+        fwd_steps++;
+        if (to >= 0) {
+            snaps[to].step = step + 1;
+            snaps[to].f_streamed = false;
+            snaps[to].g_odd_next = !src.g_odd;
+        } else {
+            c->st.f_cur = 0;
+            c->st.f_streamed = false;
+            c->st.g_odd_next = !src.g_odd;
+            c->st.steps = step + 1;
+        }
+        return LBM_OK;
+    }
+
+    // the context holds s^j, from s^s in slot si (j > s)
+    int advance(int si, long long s, long long j)
+    {
+        int rc = step_out_of_place(slot_state(si), s, -1);
+        return rc ? rc : forward(j - s - 1);
+    }
+
+    // slot sj holds s^m, from s^s in slot si (m > s)
+    int advance_to_slot(int si, long long s, long long m, int sj)
+    {
+        if (m - s == 1) return step_out_of_place(slot_state(si), s, sj);
+        int rc = advance(si, s, m - 1);
+        return rc ? rc : step_out_of_place(ctx_state(), m - 1, sj);
+    }
+
+    // phi of state st
+    int prepare(const lbm::NativeState &st)
+    {
+        cudaError_t e = lbm::launch_adjoint_phi(c->box, c->d.eta, c->q, st, phi, c->stream);
+        return e == cudaSuccess ? LBM_OK : cuda_fail(e, "adjoint: phi");
     }
 
     bool has_source(long long step) const { return step >= first_source; }
@@ -116,13 +178,15 @@ struct Adjoint {
     // lambda^T from the final state (the context holds s^T)
     int terminal()
     {
-        int rc = prepare();
+        const lbm::NativeState st = ctx_state();
+        int rc = prepare(st);
         if (rc) return rc;
         cudaError_t e = cudaSuccess;
         if (has_source(o.nsteps)) {
-            e = lbm::launch_objective(c->box, o.objective, c->d.phiStar, scale, phi, G, partials, ab, acc, c->stream);
+            e = lbm::launch_objective(c->box, o.objective, c->d.phiStar, scale, c->q, st, phi, partials, ab, acc,
+                                      c->stream);
             if (e == cudaSuccess)
-                e = lbm::launch_source_init(c->box, o.objective, scale, ab, c->d.phiStar, phi, G, lam[cur],
+                e = lbm::launch_source_init(c->box, o.objective, scale, ab, c->d.phiStar, c->q, st, phi, lam[cur],
                                             lam[cur] + lbm::kQf * n, lst[cur], c->stream);
         } else {
             e = cudaMemsetAsync(lam[cur], 0, sizeof(float) * (lbm::kQf + lbm::kQg) * n, c->stream);
@@ -133,18 +197,17 @@ struct Adjoint {
         return LBM_OK;
     }
 
-    // lambda^step from lambda^{step+1}; the context holds s^step
-    int adjoint_step(long long step)
+    // lambda^step from lambda^{step+1}; st is s^step
+    int adjoint_step(long long step, const lbm::NativeState &st)
     {
-        int rc = prepare();
+        int rc = prepare(st);
         if (rc) return rc;
         const bool src = has_source(step);
         cudaError_t e = cudaSuccess;
         if (src)
-            e = lbm::launch_objective(c->box, o.objective, c->d.phiStar, scale, phi, G, partials, ab, acc, c->stream);
+            e = lbm::launch_objective(c->box, o.objective, c->d.phiStar, scale, c->q, st, phi, partials, ab, acc,
+                                      c->stream);
         lbm::AdjointBuffers a;
-        a.F = F;
-        a.G = G;
         a.phi = phi;
         a.lf_in = lam[cur];
         a.lg_in = lam[cur] + lbm::kQf * n;
@@ -152,12 +215,11 @@ struct Adjoint {
         a.lf_out = lam[1 - cur];
         a.lg_out = lam[1 - cur] + lbm::kQf * n;
         a.lst_out = lst[1 - cur];
-        a.llap = llap;
-        a.lgrad = lgrad;
-        a.partials = partials;
+        a.lsrc = lsrc;
+        a.dgrav = dgrav;
         a.ab = ab;
         if (e == cudaSuccess)
-            e = lbm::launch_adjoint_step(c->box, k, c->d.phiStar, a, src, o.objective, scale, acc, c->stream);
+            e = lbm::launch_adjoint_step(c->box, k, c->d.phiStar, c->q, st, a, src, o.objective, scale, c->stream);
         if (e != cudaSuccess) return cuda_fail(e, "adjoint step");
         cur = 1 - cur;
         adj_steps++;
@@ -169,10 +231,9 @@ struct Adjoint {
     {
         int rc;
         if (!lambda_ready) {   // s + 1 == T: build lambda^T first
-            if ((rc = restore(si)) || (rc = forward(1)) || (rc = terminal())) return rc;
+            if ((rc = advance(si, s, s + 1)) || (rc = terminal())) return rc;
         }
-        if ((rc = restore(si))) return rc;
-        return adjoint_step(s);
+        return adjoint_step(s, slot_state(si));
     }
 
     int take_slot()
@@ -193,9 +254,13 @@ struct Adjoint {
         if (cfree == 0) {
             for (long long j = e - 1; j >= s; j--) {
                 if (!lambda_ready) {
-                    if ((rc = restore(si)) || (rc = forward(o.nsteps - s)) || (rc = terminal())) return rc;
+                    if ((rc = advance(si, s, o.nsteps)) || (rc = terminal())) return rc;
                 }
-                if ((rc = restore(si)) || (rc = forward(j - s)) || (rc = adjoint_step(j))) return rc;
+                if (j == s) {
+                    if ((rc = adjoint_step(j, slot_state(si)))) return rc;
+                } else if ((rc = advance(si, s, j)) || (rc = adjoint_step(j, ctx_state()))) {
+                    return rc;
+                }
             }
             return LBM_OK;
         }
@@ -205,7 +270,7 @@ struct Adjoint {
         const long long m = e - right;
         const int sj = take_slot();
         if (sj < 0) return fail(LBM_ESTATE, "adjoint: checkpoint pool exhausted");
-        if ((rc = restore(si)) || (rc = forward(m - s)) || (rc = save(sj, m))) return rc;
+        if ((rc = advance_to_slot(si, s, m, sj))) return rc;
         if ((rc = revolve(m, e, sj, cfree - 1))) return rc;
         free_slots.push_back(sj);
         return revolve(s, m, si, cfree);
@@ -214,54 +279,118 @@ struct Adjoint {
     void release()
     {
         cudaStreamSynchronize(c->stream);
-        void *p[] = {F, G, phi, lam[0], lam[1], lst[0], lst[1], llap, lgrad, phi0, mom_save, partials, ab, acc, slots};
+        void *p[] = {phi, lam[0], lam[1], lst[0], lst[1], lsrc, phi0, mom_save, partials, dgrav, ab, acc, slots};
         for (void *q : p) cudaFree(q);
     }
 };
 
 }  // namespace
 
-extern "C" int lbm_step_adjoint(lbm_ctx *c, const lbm_adjoint_opts *o, lbm_adjoint_out *out)
+namespace {
+
+int check_opts(lbm_ctx *c, const lbm_adjoint_opts *o, const void *out, const char *fn)
 {
-    if (!c || !o || !out) return fail(LBM_EINVAL, "lbm_step_adjoint: NULL argument");
-    if (o->nsteps < 1) return fail(LBM_EINVAL, "lbm_step_adjoint: nsteps must be >= 1");
+    const std::string f(fn);
+    if (!c || !o || !out) return fail(LBM_EINVAL, f + ": NULL argument");
+    if (o->nsteps < 1) return fail(LBM_EINVAL, f + ": nsteps must be >= 1");
     if (o->objective != LBM_OBJ_LIGHT_UZ_MEAN && o->objective != LBM_OBJ_LIGHT_Z_CENTROID)
-        return fail(LBM_EINVAL, "lbm_step_adjoint: unknown objective");
+        return fail(LBM_EINVAL, f + ": unknown objective");
     if (o->objective == LBM_OBJ_LIGHT_UZ_MEAN && (o->window < 1 || o->window > o->nsteps))
-        return fail(LBM_EINVAL, "lbm_step_adjoint: window must be in [1, nsteps]");
-    if (!std::isfinite(o->grav)) return fail(LBM_EINVAL, "lbm_step_adjoint: grav is not finite");
+        return fail(LBM_EINVAL, f + ": window must be in [1, nsteps]");
+    if (!std::isfinite(o->grav)) return fail(LBM_EINVAL, f + ": grav is not finite");
     if (c->st.steps != 0)
-        return fail(LBM_ESTATE, "lbm_step_adjoint: the context must hold its initial state (no step taken)");
-    const auto t0 = std::chrono::steady_clock::now();
+        return fail(LBM_ESTATE, f + ": the context must hold its initial state (no step taken)");
     cudaError_t e = cudaSetDevice(c->p.device);
     if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+    return LBM_OK;
+}
 
-    Adjoint A;
+void setup(Adjoint &A, lbm_ctx *c, const lbm_adjoint_opts *o)
+{
     A.c = c;
     A.o = *o;
     A.n = (size_t)c->box.n;
-    const size_t n = A.n;
-    A.snap_bytes = sizeof(float) * n + c->esz * (lbm::kQf - 1 + lbm::kQg) * n;
+    A.snap_bytes = sizeof(float) * A.n + c->esz * (lbm::kQf - 1 + lbm::kQg) * A.n;
     A.k = lbm::step_const(c->d, c->p, o->grav);
     A.first_source = o->objective == LBM_OBJ_LIGHT_UZ_MEAN ? o->nsteps - o->window + 1 : o->nsteps;
     A.scale = o->objective == LBM_OBJ_LIGHT_UZ_MEAN ? 1.0 / o->window : 1.0;
-    const size_t npart = lbm::adjoint_partial_count(c->box);
+}
+
+}  // namespace
+
+extern "C" int lbm_objective(lbm_ctx *c, const lbm_adjoint_opts *o, double *J)
+{
+    int rc = check_opts(c, o, J, "lbm_objective");
+    if (rc) return rc;
+    Adjoint A;
+    setup(A, c, o);
+    const size_t n = A.n, nblocks = lbm::adjoint_blocks(c->box);
+    cudaError_t e = cudaMalloc((void **)&A.phi, sizeof(float) * n);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&A.mom_save, sizeof(float) * 5 * n);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&A.partials, sizeof(double) * 2 * nblocks);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&A.ab, sizeof(double) * 2);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&A.acc, sizeof(double) * 2);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&A.slots, A.snap_bytes);
+    if (e != cudaSuccess) {
+        A.release();
+        return cuda_fail(e, "lbm_objective: buffers");
+    }
+    A.snaps.assign(1, Snapshot());
+    e = cudaMemsetAsync(A.acc, 0, sizeof(double) * 2, c->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(A.mom_save, c->st.mom, sizeof(float) * 5 * n, cudaMemcpyDeviceToDevice, c->stream);
+    if (e != cudaSuccess) rc = cuda_fail(e, "lbm_objective: setup");
+    if (!rc) rc = A.save(0, 0);
+    if (!rc) rc = A.forward(A.first_source);
+    for (long long k = A.first_source; !rc && k <= o->nsteps; k++) {
+        const lbm::NativeState st = A.ctx_state();
+        rc = A.prepare(st);
+        if (!rc) {
+            e = lbm::launch_objective(c->box, o->objective, c->d.phiStar, A.scale, c->q, st, A.phi, A.partials, A.ab,
+                                      A.acc, c->stream);
+            if (e != cudaSuccess) rc = cuda_fail(e, "lbm_objective: objective");
+        }
+        if (!rc && k < o->nsteps) rc = A.forward(1);
+    }
+    double acc[2] = {0.0, 0.0};
+    if (!rc) {
+        e = cudaMemcpyAsync(acc, A.acc, sizeof(acc), cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess) rc = A.restore(0);
+        if (e == cudaSuccess && !rc)
+            e = cudaMemcpyAsync(c->st.mom, A.mom_save, sizeof(float) * 5 * n, cudaMemcpyDeviceToDevice, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess && !rc) rc = cuda_fail(e, "lbm_objective: results");
+    }
+    A.release();
+    if (rc) return rc;
+    *J = acc[0];
+    return LBM_OK;
+}
+
+extern "C" int lbm_step_adjoint(lbm_ctx *c, const lbm_adjoint_opts *o, lbm_adjoint_out *out)
+{
+    int rc0 = check_opts(c, o, out, "lbm_step_adjoint");
+    if (rc0) return rc0;
+    const auto t0 = std::chrono::steady_clock::now();
+    cudaError_t e = cudaSuccess;
+    Adjoint A;
+    setup(A, c, o);
+    const size_t n = A.n;
+    const size_t nblocks = lbm::adjoint_blocks(c->box);
 
     auto alloc = [&](void **p, size_t bytes) {
         if (e == cudaSuccess) e = cudaMalloc(p, bytes);
     };
-    alloc((void **)&A.F, sizeof(float) * lbm::kQf * n);
-    alloc((void **)&A.G, sizeof(float) * lbm::kQg * n);
     alloc((void **)&A.phi, sizeof(float) * n);
     alloc((void **)&A.lam[0], sizeof(float) * (lbm::kQf + lbm::kQg) * n);
     alloc((void **)&A.lam[1], sizeof(float) * (lbm::kQf + lbm::kQg) * n);
     alloc((void **)&A.lst[0], sizeof(float) * n);
     alloc((void **)&A.lst[1], sizeof(float) * n);
-    alloc((void **)&A.llap, sizeof(float) * n);
-    alloc((void **)&A.lgrad, sizeof(float) * 3 * n);
+    alloc((void **)&A.lsrc, sizeof(float4) * n);
     alloc((void **)&A.phi0, sizeof(float) * n);
     alloc((void **)&A.mom_save, sizeof(float) * 5 * n);
-    alloc((void **)&A.partials, sizeof(double) * 2 * npart);
+    alloc((void **)&A.partials, sizeof(double) * 2 * nblocks);
+    alloc((void **)&A.dgrav, sizeof(double) * nblocks);
     alloc((void **)&A.ab, sizeof(double) * 2);
     alloc((void **)&A.acc, sizeof(double) * 2);
     if (e != cudaSuccess) {
@@ -292,18 +421,21 @@ extern "C" int lbm_step_adjoint(lbm_ctx *c, const lbm_adjoint_opts *o, lbm_adjoi
 
     int rc = LBM_OK;
     e = cudaMemsetAsync(A.acc, 0, sizeof(double) * 2, c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(A.dgrav, 0, sizeof(double) * nblocks, c->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(A.phi0, c->st.mom, sizeof(float) * n, cudaMemcpyDeviceToDevice, c->stream);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(A.mom_save, c->st.mom, sizeof(float) * 5 * n, cudaMemcpyDeviceToDevice, c->stream);
     if (e != cudaSuccess) rc = cuda_fail(e, "lbm_step_adjoint: setup");
     if (!rc) rc = A.save(0, 0);
     if (!rc) rc = A.revolve(0, o->nsteps, 0, (int)(nslots - 1));
-    // lambda^0 -> dJ/dphi0 through the initial equilibrium (output in llap,
-    // lgrad as the scratch for the Laplacian's adjoint)
-    float *lphi0 = A.llap;
+    // lambda^0 -> dJ/dphi0 through the initial equilibrium (output in the
+    // lsrc buffer, phi as the scratch for the Laplacian's adjoint)
+    float *lphi0 = reinterpret_cast<float *>(A.lsrc);
     if (!rc) {
-        e = lbm::launch_init_adjoint(c->box, c->d, c->p.Gamma, A.phi0, A.lam[A.cur], A.lst[A.cur],
-                                     A.lam[A.cur] + lbm::kQf * n, lphi0, A.lgrad, c->stream);
+        e = lbm::launch_dgrav_fold(c->box, A.dgrav, A.acc, c->stream);
+        if (e == cudaSuccess)
+            e = lbm::launch_init_adjoint(c->box, c->d, c->p.Gamma, A.phi0, A.lam[A.cur], A.lst[A.cur],
+                                         A.lam[A.cur] + lbm::kQf * n, lphi0, A.phi, c->stream);
         if (e != cudaSuccess) rc = cuda_fail(e, "lbm_step_adjoint: initial-state adjoint");
     }
     double acc[2] = {0.0, 0.0};

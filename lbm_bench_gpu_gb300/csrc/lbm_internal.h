@@ -68,20 +68,32 @@ struct StepView {
     float *f0_out;
     const void *fq_in;        // 6 arrays of n elements
     void *fq_out;
-    void *g;                  // 19 arrays of n elements
+    void *g;                  // 19 arrays of n elements, written (and read when g_in is NULL)
+    const void *g_in;         // g read by the step when it is not g (a checkpoint), else NULL
     float *mom;
 };
 
 size_t storage_bytes(int storage);   // bytes per element of fq / g
 
-// Buffers of one adjoint step (all FP32, n elements per field).
+// A forward state as the step kernel stores it (the context's current half or
+// a checkpoint slot): f_0 FP32, f_1..f_6 and g in the storage type.
+struct NativeState {
+    int storage;              // LBM_STORAGE_*
+    const float *f0;          // n floats
+    const void *fq;           // 6 x n: streamed f_1..f_6 when f_streamed, else post-collision P
+    const void *g;            // 19 x n, AA layout
+    bool f_streamed;
+    bool g_odd;               // g in the reversed layout (the next step is odd)
+};
+
+// Buffers of one adjoint step (FP32, n elements per field).
 struct AdjointBuffers {
-    const float *F, *G, *phi;          // streamed state s^n (7 + 19 fields) and its phi
+    const float *phi;                  // phi of s^n
     const float *lf_in, *lg_in;        // lambda^{n+1} (f part without its stencil term)
     const float *lst_in;               //   stencil term of lambda^{n+1}, common to the 7 f fields
     float *lf_out, *lg_out, *lst_out;  // lambda^n
-    float *llap, *lgrad;               // scratch: lambda of the Laplacian (n) and gradient (3 n)
-    double *partials;                  // per-block partial sums (adjoint_partial_count doubles, >= 2 per block)
+    float4 *lsrc;                      // scratch per node: (lambda_lap, mu lambda_F)
+    double *dgrav;                     // per-block running sums of the dJ/dgrav terms
     const double *ab;                  // objective sums of s^n
 };
 
@@ -116,14 +128,23 @@ cudaError_t launch_stats(const Box &b, const lbm_derived &d, const float *mom, d
 size_t stats_partial_count(const Box &b);
 
 // Adjoint (zsc_adjoint.cu).  acc[0] accumulates J, acc[1] dJ/dgrav (FP64).
-size_t adjoint_partial_count(const Box &b);
-cudaError_t launch_phi(const Box &b, const float *F, float *phi, cudaStream_t s);
-cudaError_t launch_objective(const Box &b, int objective, float phiStar, double scale, const float *phi,
-                             const float *G, double *partials, double *ab, double *acc, cudaStream_t s);
+// All adjoint kernels run on one grid of 32 x 8 column tiles, each block
+// marching a few z planes; adjoint_blocks is its block count (the length of
+// the dgrav array, and half the length of the objective partials).
+size_t adjoint_blocks(const Box &b);
+cudaError_t launch_adjoint_phi(const Box &b, float eta, const Quant &q, const NativeState &st, float *phi,
+                               cudaStream_t s);
+cudaError_t launch_objective(const Box &b, int objective, float phiStar, double scale, const Quant &q,
+                             const NativeState &st, const float *phi, double *partials, double *ab, double *acc,
+                             cudaStream_t s);
 cudaError_t launch_source_init(const Box &b, int objective, double scale, const double *ab, float phiStar,
-                               const float *phi, const float *G, float *lf, float *lg, float *lst, cudaStream_t s);
-cudaError_t launch_adjoint_step(const Box &b, const StepConst &c, float phiStar, const AdjointBuffers &a,
-                                bool add_source, int objective, double scale, double *acc, cudaStream_t s);
+                               const Quant &q, const NativeState &st, const float *phi, float *lf, float *lg,
+                               float *lst, cudaStream_t s);
+cudaError_t launch_adjoint_step(const Box &b, const StepConst &c, float phiStar, const Quant &q,
+                                const NativeState &st, const AdjointBuffers &a, bool add_source, int objective,
+                                double scale, cudaStream_t s);
+// acc[1] = sum of the per-block dgrav sums.
+cudaError_t launch_dgrav_fold(const Box &b, const double *dgrav, double *acc, cudaStream_t s);
 cudaError_t launch_init_adjoint(const Box &b, const lbm_derived &d, float Gamma, const float *phi0, const float *lf,
                                 const float *lst, const float *lg, float *lphi0, float *llap, cudaStream_t s);
 
@@ -161,6 +182,7 @@ inline StepView state_view(lbm_ctx *c, int in)
     v.fq_in = fq + (size_t)in * (kQf - 1) * n * c->esz;
     v.fq_out = fq + (size_t)out * (kQf - 1) * n * c->esz;
     v.g = c->st.g;
+    v.g_in = nullptr;
     v.mom = c->st.mom;
     return v;
 }

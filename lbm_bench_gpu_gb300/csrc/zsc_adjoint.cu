@@ -15,218 +15,295 @@
 //             (the Laplacian stencil is symmetric, the gradient antisymmetric)
 //   moments:  lf_i += lambda_phi;  lg_i += lambda_rho + c_i . lambda_m
 // The stencil part is kept as a separate field lst (the same for all seven f
-// populations) and added when lambda is read.  All per-node arithmetic is FP32;
-// the objective sums and the gradient with respect to gravity are FP64.
-#include "lbm_internal.h"
+// populations) and added when lambda is read.
+//
+// The forward state is read where the step kernel keeps it (a checkpoint slot
+// or the context's buffers): f_0 FP32, f_1..f_6 post-collision (the eta-blend
+// is redone on read), g in the AA layout, 16-bit formats mapped back to FP32.
+// The collision's Jacobian needs g only through rho and the momentum, and f
+// only through phi, so only phi is materialised (the stencil needs it at the
+// neighbours).  Per step:
+//   adjoint_phi_kernel     s^n -> phi                          ~32 B/node (FP32)
+//   adjoint_local_kernel   lambda^{n+1}, s^n, phi -> lambda^n   ~320 B/node
+//                          and (lambda_lap, mu lambda_F) as one float4
+//   adjoint_stencil_kernel float4 -> lst                        ~20 B/node
+// All per-node arithmetic is FP32; the objective sums and dJ/dgrav are FP64.
+// Every kernel runs on one grid: 32 x 8 column tiles, each block marching
+// kPlanes z planes, 32-bit node indices (n * 19 < 2^32 is checked at init).
+#include <type_traits>
+
+#include "lattice.cuh"
 
 namespace lbm {
 namespace {
 
-constexpr int kThreads = 256;
+constexpr int TXA = 32, TYA = 8, NTA = TXA * TYA;
+constexpr int kPlanes = 4;
 constexpr float kInv6 = 0.16666666666666666667f;
 constexpr float kInv12 = 0.08333333333333333333f;
 constexpr float kW0 = 0.33333333333333333333f, kW1 = 0.05555555555555555556f, kW2 = 0.02777777777777777778f;
 
-__constant__ int aCf[kQf][3] = {{0, 0, 0}, {1, 0, 0}, {-1, 0, 0}, {0, 1, 0}, {0, -1, 0}, {0, 0, 1}, {0, 0, -1}};
-__constant__ int aCg[kQg][3] = {{0, 0, 0},  {1, 0, 0},   {-1, 0, 0}, {0, 1, 0},  {0, -1, 0},
-                                {0, 0, 1},  {0, 0, -1},  {1, 1, 0},  {-1, -1, 0}, {1, -1, 0},
-                                {-1, 1, 0}, {1, 0, 1},   {-1, 0, -1}, {1, 0, -1}, {-1, 0, 1},
-                                {0, 1, 1},  {0, -1, -1}, {0, 1, -1}, {0, -1, 1}};
-
-struct Coord {
-    int x, y, z;
+// Node indices of the 3 x 3 x 3 neighbourhood of (x, y, z), periodic.
+struct Nb {
+    unsigned X[3], Y[3], Z[3];
+    __device__ __forceinline__ unsigned at(int dx, int dy, int dz) const { return X[dx + 1] + Y[dy + 1] + Z[dz + 1]; }
 };
 
-__device__ __forceinline__ Coord coord(const Box &b, long long t)
+__device__ __forceinline__ Nb neighbourhood(const Box &b, int x, int y, int z)
 {
-    Coord c;
-    c.x = (int)(t % b.nx);
-    c.y = (int)((t / b.nx) % b.ny);
-    c.z = (int)(t / b.nxy);
-    return c;
+    Nb r;
+    const unsigned nx = (unsigned)b.nx, nxy = (unsigned)b.nxy;
+    r.X[0] = x == 0 ? nx - 1 : x - 1;
+    r.X[1] = x;
+    r.X[2] = x == b.nx - 1 ? 0 : x + 1;
+    r.Y[0] = (y == 0 ? b.ny - 1 : y - 1) * nx;
+    r.Y[1] = y * nx;
+    r.Y[2] = (y == b.ny - 1 ? 0 : y + 1) * nx;
+    r.Z[0] = (z == 0 ? b.nz - 1 : z - 1) * nxy;
+    r.Z[1] = z * nxy;
+    r.Z[2] = (z == b.nz - 1 ? 0 : z + 1) * nxy;
+    return r;
 }
 
-__device__ __forceinline__ long long at(const Box &b, Coord c, int dx, int dy, int dz)
+// index of the node at sign * c_i from the centre of p
+__device__ __forceinline__ unsigned dir_at(const Nb &p, int i, int sign)
 {
-    int x = c.x + dx, y = c.y + dy, z = c.z + dz;
-    x = x < 0 ? x + b.nx : (x >= b.nx ? x - b.nx : x);
-    y = y < 0 ? y + b.ny : (y >= b.ny ? y - b.ny : y);
-    z = z < 0 ? z + b.nz : (z >= b.nz ? z - b.nz : z);
-    return x + (long long)b.nx * (y + (long long)b.ny * z);
+    return p.at(sign * kCx(i), sign * kCy(i), sign * kCz(i));
 }
 
-// 19-point Laplacian and gradient of field p at c (src/collision_f.cu:61-94).
-__device__ __forceinline__ void stencil(const Box &b, const float *__restrict__ p, Coord c, float &lap, float &gx,
-                                        float &gy, float &gz)
+// 19-point Laplacian and gradient of field v at the centre of p
+// (src/collision_f.cu:61-94), the stencil points taken in D3Q19 order.
+__device__ __forceinline__ void stencil19(const float *__restrict__ v, const Nb &p, float &lap, float &gx, float &gy,
+                                          float &gz)
 {
-    auto P = [&](int dx, int dy, int dz) { return p[at(b, c, dx, dy, dz)]; };
-    const float pc = P(0, 0, 0);
-    const float pe = P(1, 0, 0), pw = P(-1, 0, 0), pn = P(0, 1, 0), ps = P(0, -1, 0), pt = P(0, 0, 1),
-                pb = P(0, 0, -1);
-    const float pen = P(1, 1, 0), pws = P(-1, -1, 0), pes = P(1, -1, 0), pwn = P(-1, 1, 0);
-    const float pet = P(1, 0, 1), pwb = P(-1, 0, -1), peb = P(1, 0, -1), pwt = P(-1, 0, 1);
-    const float pnt = P(0, 1, 1), psb = P(0, -1, -1), pnb = P(0, 1, -1), pst = P(0, -1, 1);
-    lap = (pen + pws + pes + pwn + pet + pwb + peb + pwt + pnt + psb + pnb + pst
-           + 2.f * (pe + pw + pn + ps + pt + pb - 12.f * pc)) * kInv6;
-    gx = (2.f * (pe - pw) + pen - pws + pes - pwn + pet - pwb + peb - pwt) * kInv12;
-    gy = (2.f * (pn - ps) + pen - pws + pwn - pes + pnt - psb + pnb - pst) * kInv12;
-    gz = (2.f * (pt - pb) + pet - pwb + pwt - peb + pnt - psb + pst - pnb) * kInv12;
+    float s[kQg];
+#pragma unroll
+    for (int i = 0; i < kQg; i++) s[i] = __ldg(v + dir_at(p, i, 1));
+    lap = (s[7] + s[8] + s[9] + s[10] + s[11] + s[12] + s[13] + s[14] + s[15] + s[16] + s[17] + s[18]
+           + 2.f * (s[1] + s[2] + s[3] + s[4] + s[5] + s[6] - 12.f * s[0])) * kInv6;
+    gx = (2.f * (s[1] - s[2]) + s[7] - s[8] + s[9] - s[10] + s[11] - s[12] + s[13] - s[14]) * kInv12;
+    gy = (2.f * (s[3] - s[4]) + s[7] - s[8] + s[10] - s[9] + s[15] - s[16] + s[17] - s[18]) * kInv12;
+    gz = (2.f * (s[5] - s[6]) + s[11] - s[12] + s[14] - s[13] + s[15] - s[16] + s[18] - s[17]) * kInv12;
+}
+
+// Streamed g_i at the centre of p, FP32.
+template <typename ST, bool ODD>
+__device__ __forceinline__ float g_streamed(const ST *__restrict__ g, unsigned n, const Quant &q, const Nb &p, int i)
+{
+    const ST v = ODD ? g[kOpp(i) * n + dir_at(p, i, -1)] : g[i * n + p.at(0, 0, 0)];
+    if constexpr (Fmt<ST>::kMapped)
+        return Fmt<ST>::load(v) * q.g_inv[i] + q.g_shift[i];
+    else
+        return Fmt<ST>::load(v);
+}
+
+// rho and momentum of the streamed g at the centre of p.
+template <typename ST, bool ODD>
+__device__ __forceinline__ void g_moments(const ST *__restrict__ g, unsigned n, const Quant &q, const Nb &p,
+                                          float &rho, float m[3])
+{
+    rho = 0.f;
+    m[0] = m[1] = m[2] = 0.f;
+#pragma unroll
+    for (int i = 0; i < kQg; i++) {
+        const float gi = g_streamed<ST, ODD>(g, n, q, p, i);
+        rho += gi;
+        if (kCx(i)) m[0] += kCx(i) * gi;
+        if (kCy(i)) m[1] += kCy(i) * gi;
+        if (kCz(i)) m[2] += kCz(i) * gi;
+    }
 }
 
 __device__ __forceinline__ double block_sum(double v, double *red)
 {
+    const int tid = threadIdx.y * TXA + threadIdx.x;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (lane == 0) red[warp] = v;
+    if ((tid & 31) == 0) red[tid >> 5] = v;
     __syncthreads();
     double r = 0.0;
-    if (threadIdx.x == 0)
-        for (int w = 0; w < kThreads / 32; w++) r += red[w];
+    if (tid == 0)
+        for (int w = 0; w < NTA / 32; w++) r += red[w];
     __syncthreads();
     return r;
 }
 
-// phi = sum f of the streamed state.
-__global__ void phi_kernel(Box b, const float *__restrict__ F, float *__restrict__ phi)
+__device__ __forceinline__ unsigned block_id() { return blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z); }
+
+// phi = sum of the streamed f of a native state.
+template <typename ST>
+__global__ void __launch_bounds__(NTA) adjoint_phi_kernel(Box b, float eta, Quant q, const float *__restrict__ f0,
+                                                          const ST *__restrict__ fq, int f_streamed,
+                                                          float *__restrict__ phi)
 {
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < b.n;
-         t += (long long)gridDim.x * blockDim.x) {
-        float s = F[t];
-        for (int i = 1; i < kQf; i++) s += F[i * b.n + t];
+    const unsigned n = (unsigned)b.n;
+    const float eta2 = 1.f - eta;
+    const int x = blockIdx.x * TXA + threadIdx.x, y = blockIdx.y * TYA + threadIdx.y;
+    for (int z = blockIdx.z; z < b.nz; z += gridDim.z) {
+        const Nb p = neighbourhood(b, x, y, z);
+        const unsigned t = p.at(0, 0, 0);
+        float s = f0[t];
+#pragma unroll
+        for (int i = 1; i < kQf; i++) {
+            const ST *a = fq + (i - 1) * n;
+            const float inv = Fmt<ST>::kMapped ? q.f_inv[i - 1] : 1.f;
+            const float here = Fmt<ST>::load(a[t]) * inv;
+            s += f_streamed ? here : eta * (Fmt<ST>::load(a[dir_at(p, i, -1)]) * inv) + eta2 * here;
+        }
         phi[t] = s;
     }
 }
 
-// Objective sums of one streamed state: A = sum w q, B = sum w, with
+// Objective sums of one state: A = sum w q, B = sum w, with
 // w = (phiStar - phi) / (2 phiStar) and q = u_z (objective 0) or the reference
 // plane index z + 1 (objective 1); per-block partials.
-__global__ void __launch_bounds__(kThreads) objective_kernel(Box b, int objective, float phiStar,
-                                                             const float *__restrict__ phi,
-                                                             const float *__restrict__ G,
-                                                             double *__restrict__ partials)
+template <typename ST, bool ODD>
+__global__ void __launch_bounds__(NTA) objective_kernel(Box b, int objective, float phiStar, Quant q,
+                                                        const ST *__restrict__ g, const float *__restrict__ phi,
+                                                        double *__restrict__ partials)
 {
-    __shared__ double red[kThreads / 32];
+    __shared__ double red[NTA / 32];
+    const unsigned n = (unsigned)b.n;
+    const float half_inv = 0.5f / phiStar;
     double A = 0.0, B = 0.0;
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < b.n;
-         t += (long long)gridDim.x * blockDim.x) {
-        const double w = ((double)phiStar - phi[t]) / (2.0 * phiStar);
-        double q;
+    const int x = blockIdx.x * TXA + threadIdx.x, y = blockIdx.y * TYA + threadIdx.y;
+    for (int z = blockIdx.z; z < b.nz; z += gridDim.z) {
+        const Nb p = neighbourhood(b, x, y, z);
+        const unsigned t = p.at(0, 0, 0);
+        const float w = (phiStar - phi[t]) * half_inv;
+        float qv;
         if (objective == 0) {
-            float rho = 0.f, mz = 0.f;
-            for (int i = 0; i < kQg; i++) {
-                const float gi = G[i * b.n + t];
-                rho += gi;
-                mz += aCg[i][2] * gi;
-            }
-            q = (double)mz / rho;
+            float rho, m[3];
+            g_moments<ST, ODD>(g, n, q, p, rho, m);
+            qv = m[2] / rho;
         } else {
-            q = (double)(t / b.nxy + 1);
+            qv = (float)(z + 1);
         }
-        A += w * q;
-        B += w;
+        A += (double)(w * qv);
+        B += (double)w;
     }
     A = block_sum(A, red);
     B = block_sum(B, red);
-    if (threadIdx.x == 0) {
-        partials[2 * blockIdx.x] = A;
-        partials[2 * blockIdx.x + 1] = B;
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+        partials[2 * block_id()] = A;
+        partials[2 * block_id() + 1] = B;
     }
 }
 
 // ab[0..1] = sums of the partials; acc[0] (J) += scale * A / B.
-__global__ void objective_fold_kernel(const double *__restrict__ partials, int nparts, double scale,
-                                      double *__restrict__ ab, double *__restrict__ acc)
+__global__ void __launch_bounds__(NTA) objective_fold_kernel(const double *__restrict__ partials, int nparts,
+                                                             double scale, double *__restrict__ ab,
+                                                             double *__restrict__ acc)
 {
-    __shared__ double red[kThreads / 32];
+    __shared__ double red[NTA / 32];
     double A = 0.0, B = 0.0;
-    for (int p = threadIdx.x; p < nparts; p += blockDim.x) {
+    for (int p = threadIdx.y * TXA + threadIdx.x; p < nparts; p += NTA) {
         A += partials[2 * p];
         B += partials[2 * p + 1];
     }
     A = block_sum(A, red);
     B = block_sum(B, red);
-    if (threadIdx.x == 0) {
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
         ab[0] = A;
         ab[1] = B;
         acc[0] += scale * A / B;
     }
 }
 
-// d(scale * A / B)/d(state) at node t into lf, lg.
-__device__ __forceinline__ void objective_source(const Box &b, long long t, int objective, double scale,
-                                                 const double *ab, float phiStar, float ph, float rho, float mz,
-                                                 float &dphi, float &drho, float &dmz)
+// Per-launch coefficients of the objective's derivative: J += scale A / B
+// gives dJ/dw = scale (q - A/B) / B and dJ/dq = scale w / B, with
+// dw/dphi = -1 / (2 phiStar).
+struct SourceCoef {
+    float ratio;    // A / B
+    float s_over_b; // scale / B
+    float half_inv; // 1 / (2 phiStar)
+};
+
+__device__ __forceinline__ SourceCoef source_coef(const double *ab, double scale, float phiStar)
 {
-    const double A = ab[0], B = ab[1];
-    const double ratio = A / B;
-    const double dw = -1.0 / (2.0 * phiStar);
-    const double w = ((double)phiStar - ph) / (2.0 * phiStar);
+    SourceCoef k;
+    k.ratio = (float)(ab[0] / ab[1]);
+    k.s_over_b = (float)(scale / ab[1]);
+    k.half_inv = 0.5f / phiStar;
+    return k;
+}
+
+// d(scale * A / B)/d(state) at a node of plane z (FP32 per node).
+__device__ __forceinline__ void objective_source(int z, int objective, const SourceCoef &k, float phiStar, float ph,
+                                                 float rho, float mz, float &dphi, float &drho, float &dmz)
+{
+    const float w = (phiStar - ph) * k.half_inv;
     if (objective == 0) {
-        const double uz = (double)mz / rho;
-        dphi = (float)(scale * dw * (uz - ratio) / B);
-        const double duz = scale * w / B;
-        dmz = (float)(duz / rho);
-        drho = (float)(-duz * uz / rho);
+        const float inv = 1.0f / rho;
+        const float uz = mz * inv;
+        dphi = -k.half_inv * k.s_over_b * (uz - k.ratio);
+        const float duz = k.s_over_b * w;
+        dmz = duz * inv;
+        drho = -duz * uz * inv;
     } else {
-        dphi = (float)(scale * dw * ((double)(t / b.nxy + 1) - ratio) / B);
+        dphi = -k.half_inv * k.s_over_b * ((float)(z + 1) - k.ratio);
         drho = 0.f;
         dmz = 0.f;
     }
 }
 
 // lambda^T: only the objective source of the final state.
-__global__ void source_init_kernel(Box b, int objective, double scale, const double *__restrict__ ab,
-                                   float phiStar, const float *__restrict__ phi, const float *__restrict__ G,
-                                   float *__restrict__ lf, float *__restrict__ lg, float *__restrict__ lst)
+template <typename ST, bool ODD>
+__global__ void __launch_bounds__(NTA) source_init_kernel(Box b, int objective, double scale,
+                                                          const double *__restrict__ ab, float phiStar, Quant q,
+                                                          const ST *__restrict__ g, const float *__restrict__ phi,
+                                                          float *__restrict__ lf, float *__restrict__ lg,
+                                                          float *__restrict__ lst)
 {
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < b.n;
-         t += (long long)gridDim.x * blockDim.x) {
-        float rho = 0.f, mz = 0.f;
-        for (int i = 0; i < kQg; i++) {
-            const float gi = G[i * b.n + t];
-            rho += gi;
-            mz += aCg[i][2] * gi;
-        }
+    const unsigned n = (unsigned)b.n;
+    const SourceCoef k = source_coef(ab, scale, phiStar);
+    const int x = blockIdx.x * TXA + threadIdx.x, y = blockIdx.y * TYA + threadIdx.y;
+    for (int z = blockIdx.z; z < b.nz; z += gridDim.z) {
+        const Nb p = neighbourhood(b, x, y, z);
+        const unsigned t = p.at(0, 0, 0);
+        float rho, m[3];
+        g_moments<ST, ODD>(g, n, q, p, rho, m);
         float dphi, drho, dmz;
-        objective_source(b, t, objective, scale, ab, phiStar, phi[t], rho, mz, dphi, drho, dmz);
-        for (int i = 0; i < kQf; i++) lf[i * b.n + t] = dphi;
-        for (int i = 0; i < kQg; i++) lg[i * b.n + t] = drho + aCg[i][2] * dmz;
+        objective_source(z, objective, k, phiStar, phi[t], rho, m[2], dphi, drho, dmz);
+#pragma unroll
+        for (int i = 0; i < kQf; i++) lf[i * n + t] = dphi;
+#pragma unroll
+        for (int i = 0; i < kQg; i++) lg[i * n + t] = drho + kCz(i) * dmz;
         lst[t] = 0.f;
     }
 }
 
 struct AdjIn {
-    const float *F, *G, *phi;              // streamed s^n and its phi
+    const void *g;                         // native g of s^n
+    const float *phi;                      // phi of s^n
     const float *lf, *lg, *lst;            // lambda^{n+1} (lf without its stencil part lst)
     float *lf_out, *lg_out;                // lambda^n without its stencil part
-    float *llap, *lgrad;                   // lambda of lap and grad (3 x n) at every node
-    double *dgrav_partials;                // per block
+    float4 *lsrc;                          // (lambda_lap, mu lambda_F) at every node
+    double *dgrav;                         // per block, accumulated over steps
     const double *ab;                      // objective sums of s^n (when add_source)
     double scale;
     int objective, add_source;
 };
 
 // The local part of one adjoint step (see the file comment).
-__global__ void __launch_bounds__(kThreads) adjoint_local_kernel(Box b, StepConst c, float phiStar, AdjIn a)
+template <typename ST, bool ODD>
+__global__ void __launch_bounds__(NTA, 3) adjoint_local_kernel(Box b, StepConst c, float phiStar, Quant q, AdjIn a)
 {
-    __shared__ double red[kThreads / 32];
+    __shared__ double red[NTA / 32];
+    const unsigned n = (unsigned)b.n;
+    const ST *__restrict__ g = static_cast<const ST *>(a.g);
+    SourceCoef sk{};
+    if (a.add_source) sk = source_coef(a.ab, a.scale, phiStar);
     double dg = 0.0;
-    const long long n = b.n;
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
-         t += (long long)gridDim.x * blockDim.x) {
-        const Coord cd = coord(b, t);
+    const int x = blockIdx.x * TXA + threadIdx.x, y = blockIdx.y * TYA + threadIdx.y;
+    for (int z = blockIdx.z; z < b.nz; z += gridDim.z) {
+        const Nb p = neighbourhood(b, x, y, z);
+        const unsigned t = p.at(0, 0, 0);
         float lap, gr[3];
-        stencil(b, a.phi, cd, lap, gr[0], gr[1], gr[2]);
-        const float ph = a.phi[t];
-        float g[kQg], rh = 0.f, m[3] = {0.f, 0.f, 0.f};
-        for (int i = 0; i < kQg; i++) {
-            g[i] = a.G[i * n + t];
-            rh += g[i];
-            m[0] += aCg[i][0] * g[i];
-            m[1] += aCg[i][1] * g[i];
-            m[2] += aCg[i][2] * g[i];
-        }
+        stencil19(a.phi, p, lap, gr[0], gr[1], gr[2]);
+        const float ph = __ldg(a.phi + t);
+        float rh, m[3];
+        g_moments<ST, ODD>(g, n, q, p, rh, m);
         const float inv = 1.0f / rh;
         const float u[3] = {m[0] * inv, m[1] * inv, m[2] * inv};
         const float mu = c.alpha4 * ph * (ph * ph - c.phiStarSq) - c.kappa * lap;
@@ -240,19 +317,23 @@ __global__ void __launch_bounds__(kThreads) adjoint_local_kernel(Box b, StepCons
 
         // stream adjoint
         float lP[kQf], lQ[kQg];
-        lP[0] = a.lf[t] + a.lst[t];
-        const float lst_here = a.lst[t];
+        const float lst_here = __ldg(a.lst + t);
+        lP[0] = __ldg(a.lf + t) + lst_here;
+#pragma unroll
         for (int i = 1; i < kQf; i++) {
-            const long long dn = at(b, cd, aCf[i][0], aCf[i][1], aCf[i][2]);
-            lP[i] = c.eta * (a.lf[i * n + dn] + a.lst[dn]) + c.eta2 * (a.lf[i * n + t] + lst_here);
+            const unsigned dn = dir_at(p, i, 1);
+            lP[i] = c.eta * (__ldg(a.lf + i * n + dn) + __ldg(a.lst + dn))
+                    + c.eta2 * (__ldg(a.lf + i * n + t) + lst_here);
         }
-        for (int i = 0; i < kQg; i++) lQ[i] = a.lg[i * n + at(b, cd, aCg[i][0], aCg[i][1], aCg[i][2])];
+#pragma unroll
+        for (int i = 0; i < kQg; i++) lQ[i] = __ldg(a.lg + i * n + dir_at(p, i, 1));
 
         // D3Q7 collision
         float lphi = 0.f, lmu = 0.f, lus[3] = {0.f, 0.f, 0.f}, lF[3] = {0.f, 0.f, 0.f}, lrho = 0.f;
         {
             const float lAf = -6.f * lP[0] + lP[1] + lP[2] + lP[3] + lP[4] + lP[5] + lP[6];
             float lCf = 0.f;
+#pragma unroll
             for (int k = 0; k < 3; k++) {
                 const float d = lP[1 + 2 * k] - lP[2 + 2 * k];
                 lCf += us[k] * d;
@@ -269,6 +350,7 @@ __global__ void __launch_bounds__(kThreads) adjoint_local_kernel(Box b, StepCons
             lvsq6 += -c.K0 * rh * lQ[0];
             lUF += -c.KC0 * lQ[0];
             float ltemp1 = 0.f;
+#pragma unroll
             for (int k = 0; k < 3; k++) {
                 const float S = lQ[1 + 2 * k] + lQ[2 + 2 * k], A = lQ[1 + 2 * k] - lQ[2 + 2 * k];
                 ltemp1 += S;
@@ -281,15 +363,15 @@ __global__ void __launch_bounds__(kThreads) adjoint_local_kernel(Box b, StepCons
             lrho += c.K1 * (1.f - vsq6) * ltemp1;
             lvsq6 += -c.K1 * rh * ltemp1;
             // pairs (7,8) x+y, (9,10) x-y, (11,12) x+z, (13,14) x-z, (15,16) y+z, (17,18) y-z
-            const int PA[6] = {0, 0, 0, 0, 1, 1}, PB[6] = {1, 1, 2, 2, 2, 2};
-            const float SG[6] = {1.f, -1.f, 1.f, -1.f, 1.f, -1.f};
+            constexpr int PA[6] = {0, 0, 0, 0, 1, 1}, PB[6] = {1, 1, 2, 2, 2, 2};
+            constexpr float SG[6] = {1.f, -1.f, 1.f, -1.f, 1.f, -1.f};
             float ltemp2 = 0.f;
 #pragma unroll
-            for (int p = 0; p < 6; p++) {
-                const int ia = PA[p], ib = PB[p];
-                const float sg = SG[p];
+            for (int pp = 0; pp < 6; pp++) {
+                const int ia = PA[pp], ib = PB[pp];
+                const float sg = SG[pp];
                 const float w = v[ia] + sg * v[ib], Gs = F[ia] + sg * F[ib];
-                const float S = lQ[7 + 2 * p] + lQ[8 + 2 * p], A = lQ[7 + 2 * p] - lQ[8 + 2 * p];
+                const float S = lQ[7 + 2 * pp] + lQ[8 + 2 * pp], A = lQ[7 + 2 * pp] - lQ[8 + 2 * pp];
                 ltemp2 += S;
                 lrho += 0.5f * c.K2 * w * w * S + c.K2 * w * A;
                 const float lw = c.K2 * rh * w * S + c.KC2 * Gs * S + c.K2 * rh * A;
@@ -304,7 +386,9 @@ __global__ void __launch_bounds__(kThreads) adjoint_local_kernel(Box b, StepCons
             lrho += c.K2 * (1.f - vsq6) * ltemp2;
             lvsq6 += -c.K2 * rh * ltemp2;
         }
+#pragma unroll
         for (int k = 0; k < 3; k++) lv[k] += lvsq6 * v[k] * (1.f / 3.f);
+#pragma unroll
         for (int k = 0; k < 3; k++) {
             lus[k] += lUF * F[k] + 3.f * lv[k];
             lF[k] += lUF * us[k];
@@ -312,82 +396,107 @@ __global__ void __launch_bounds__(kThreads) adjoint_local_kernel(Box b, StepCons
         lphi += 3.f * mu * ls;
         lmu += 3.f * ph * ls;
         float lm[3];
+#pragma unroll
         for (int k = 0; k < 3; k++) {
             lF[k] += 0.5f * lus[k] * inv;
             lrho += -0.5f * lus[k] * F[k] * inv * inv;
             lm[k] = lus[k] * inv;
             lrho += -lus[k] * u[k] * inv;
         }
+#pragma unroll
         for (int k = 0; k < 3; k++) lmu += gr[k] * lF[k];
         if (heavy) dg += lF[2];
-        a.lgrad[t] = mu * lF[0];
-        a.lgrad[n + t] = mu * lF[1];
-        a.lgrad[2 * n + t] = mu * lF[2];
         lphi += c.alpha4 * (3.f * ph * ph - c.phiStarSq) * lmu;
-        a.llap[t] = -c.kappa * lmu;
+        a.lsrc[t] = make_float4(-c.kappa * lmu, mu * lF[0], mu * lF[1], mu * lF[2]);
         if (a.add_source) {
             float dphi, drho, dmz;
-            objective_source(b, t, a.objective, a.scale, a.ab, phiStar, ph, rh, m[2], dphi, drho, dmz);
+            objective_source(z, a.objective, sk, phiStar, ph, rh, m[2], dphi, drho, dmz);
             lphi += dphi;
             lrho += drho;
             lm[2] += dmz;
         }
-        a.lf_out[t] = c.invTauPhiOne * lP[0] + lphi;
-        for (int i = 1; i < kQf; i++) a.lf_out[i * n + t] = c.invTauPhiOne * lP[i] + lphi;
-        for (int i = 0; i < kQg; i++)
-            a.lg_out[i * n + t] =
-                c.invTauRhoOne * lQ[i] + lrho + aCg[i][0] * lm[0] + aCg[i][1] * lm[1] + aCg[i][2] * lm[2];
+#pragma unroll
+        for (int i = 0; i < kQf; i++) a.lf_out[i * n + t] = c.invTauPhiOne * lP[i] + lphi;
+#pragma unroll
+        for (int i = 0; i < kQg; i++) {
+            float o = c.invTauRhoOne * lQ[i] + lrho;
+            if (kCx(i)) o += kCx(i) * lm[0];
+            if (kCy(i)) o += kCy(i) * lm[1];
+            if (kCz(i)) o += kCz(i) * lm[2];
+            a.lg_out[i * n + t] = o;
+        }
     }
     dg = block_sum(dg, red);
-    if (threadIdx.x == 0) a.dgrav_partials[blockIdx.x] = dg;
+    if (threadIdx.x == 0 && threadIdx.y == 0) a.dgrav[block_id()] += dg;
 }
 
-// lst = L[llap] - sum_k D_k[lgrad_k]: the transposed stencils.
-__global__ void adjoint_stencil_kernel(Box b, const float *__restrict__ llap, const float *__restrict__ lgrad,
-                                       float *__restrict__ lst)
+// lst = L[lambda_lap] - sum_k D_k[lambda_grad_k]: the transposed stencils.
+// Laplacian weights: 2/6 on faces, 1/6 on edges, -4 at the centre; gradient
+// component k: c_ik times 2/12 on faces, 1/12 on edges.
+__global__ void __launch_bounds__(NTA) adjoint_stencil_kernel(Box b, const float4 *__restrict__ lsrc,
+                                                              float *__restrict__ lst)
 {
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < b.n;
-         t += (long long)gridDim.x * blockDim.x) {
-        const Coord cd = coord(b, t);
-        float l1, d0, d1, d2, gxv, gyv, gzv;
-        stencil(b, llap, cd, l1, d0, d1, d2);
-        stencil(b, lgrad, cd, d0, gxv, d1, d2);
-        stencil(b, lgrad + b.n, cd, d0, d1, gyv, d2);
-        stencil(b, lgrad + 2 * b.n, cd, d0, d1, d2, gzv);
-        lst[t] = l1 - gxv - gyv - gzv;
+    const int x = blockIdx.x * TXA + threadIdx.x, y = blockIdx.y * TYA + threadIdx.y;
+    for (int z = blockIdx.z; z < b.nz; z += gridDim.z) {
+        const Nb p = neighbourhood(b, x, y, z);
+        float lface = 0.f, ledge = 0.f, dface = 0.f, dedge = 0.f;
+        const float4 c0 = __ldg(lsrc + p.at(0, 0, 0));
+#pragma unroll
+        for (int i = 1; i < kQg; i++) {
+            const float4 s = __ldg(lsrc + dir_at(p, i, 1));
+            float d = 0.f;
+            if (kCx(i)) d += kCx(i) * s.y;
+            if (kCy(i)) d += kCy(i) * s.z;
+            if (kCz(i)) d += kCz(i) * s.w;
+            if (i < 7) {
+                lface += s.x;
+                dface += d;
+            } else {
+                ledge += s.x;
+                dedge += d;
+            }
+        }
+        const float L = (ledge + 2.f * (lface - 12.f * c0.x)) * kInv6;
+        const float D = (2.f * dface + dedge) * kInv12;
+        lst[p.at(0, 0, 0)] = L - D;
     }
 }
 
-// acc[1] (dJ/dgrav) += sum of the partials.
-__global__ void sum_fold_kernel(const double *__restrict__ partials, int nparts, double *__restrict__ acc)
+// acc[1] (dJ/dgrav) = sum of the per-block sums.
+__global__ void __launch_bounds__(NTA) dgrav_fold_kernel(const double *__restrict__ parts, int nparts,
+                                                         double *__restrict__ acc)
 {
-    __shared__ double red[kThreads / 32];
+    __shared__ double red[NTA / 32];
     double s = 0.0;
-    for (int p = threadIdx.x; p < nparts; p += blockDim.x) s += partials[p];
+    for (int p = threadIdx.y * TXA + threadIdx.x; p < nparts; p += NTA) s += parts[p];
     s = block_sum(s, red);
-    if (threadIdx.x == 0) acc[1] += s;
+    if (threadIdx.x == 0 && threadIdx.y == 0) acc[1] = s;
 }
 
 // dJ/dphi0 through the initial equilibrium (src/init_f.cu:57-78,
 // src/init_g.cu:69-91), local part; llap receives lambda of the Laplacian.
-__global__ void init_adjoint_kernel(Box b, float alpha4, float kappa, float phiStarSq, float Gamma,
-                                    const float *__restrict__ phi0, const float *__restrict__ lf,
-                                    const float *__restrict__ lst, const float *__restrict__ lg,
-                                    float *__restrict__ lphi0, float *__restrict__ llap)
+__global__ void __launch_bounds__(NTA) init_adjoint_kernel(Box b, float alpha4, float kappa, float phiStarSq,
+                                                           float Gamma, const float *__restrict__ phi0,
+                                                           const float *__restrict__ lf,
+                                                           const float *__restrict__ lst,
+                                                           const float *__restrict__ lg, float *__restrict__ lphi0,
+                                                           float *__restrict__ llap)
 {
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < b.n;
-         t += (long long)gridDim.x * blockDim.x) {
-        const Coord cd = coord(b, t);
+    const unsigned n = (unsigned)b.n;
+    const int x = blockIdx.x * TXA + threadIdx.x, y = blockIdx.y * TYA + threadIdx.y;
+    for (int z = blockIdx.z; z < b.nz; z += gridDim.z) {
+        const Nb p = neighbourhood(b, x, y, z);
+        const unsigned t = p.at(0, 0, 0);
         float lap, gx, gy, gz;
-        stencil(b, phi0, cd, lap, gx, gy, gz);
+        stencil19(phi0, p, lap, gx, gy, gz);
         const float ph = phi0[t];
         const float mu = alpha4 * ph * (ph * ph - phiStarSq) - kappa * lap;
         const float add = lst[t];
         const float l0 = lf[t] + add;
         float lfs = 0.f, lga = 0.f, lgd = 0.f;
-        for (int i = 1; i < kQf; i++) lfs += lf[i * b.n + t] + add;
-        for (int i = 1; i < 7; i++) lga += lg[i * b.n + t];
-        for (int i = 7; i < kQg; i++) lgd += lg[i * b.n + t];
+        for (int i = 1; i < kQf; i++) lfs += lf[i * n + t] + add;
+        for (int i = 1; i < 7; i++) lga += lg[i * n + t];
+        for (int i = 7; i < kQg; i++) lgd += lg[i * n + t];
         const float lg0 = lg[t];
         const float lmu = -3.f * Gamma * l0 + 0.5f * Gamma * lfs - 6.f * kW0 * ph * lg0 + 3.f * kW1 * ph * lga
                           + 3.f * kW2 * ph * lgd;
@@ -398,89 +507,128 @@ __global__ void init_adjoint_kernel(Box b, float alpha4, float kappa, float phiS
     }
 }
 
-__global__ void init_adjoint_stencil_kernel(Box b, const float *__restrict__ llap, float *__restrict__ lphi0)
+__global__ void __launch_bounds__(NTA) init_adjoint_stencil_kernel(Box b, const float *__restrict__ llap,
+                                                                   float *__restrict__ lphi0)
 {
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < b.n;
-         t += (long long)gridDim.x * blockDim.x) {
+    const int x = blockIdx.x * TXA + threadIdx.x, y = blockIdx.y * TYA + threadIdx.y;
+    for (int z = blockIdx.z; z < b.nz; z += gridDim.z) {
+        const Nb p = neighbourhood(b, x, y, z);
         float l1, d0, d1, d2;
-        stencil(b, llap, coord(b, t), l1, d0, d1, d2);
-        lphi0[t] += l1;
+        stencil19(llap, p, l1, d0, d1, d2);
+        lphi0[p.at(0, 0, 0)] += l1;
     }
 }
 
-unsigned grid_for(long long n)
+dim3 adjoint_grid(const Box &b)
 {
-    long long blocks = (n + kThreads - 1) / kThreads;
-    if (blocks > 152 * 8) blocks = 152 * 8;
-    return (unsigned)(blocks < 1 ? 1 : blocks);
+    return dim3((unsigned)(b.nx / TXA), (unsigned)(b.ny / TYA), (unsigned)((b.nz + kPlanes - 1) / kPlanes));
+}
+
+const dim3 kBlock(TXA, TYA);
+
+// fn(ST{}, std::integral_constant<bool, ODD>{}) for the state's storage type and g layout.
+template <typename Fn>
+cudaError_t dispatch(const NativeState &st, Fn &&fn)
+{
+    auto with = [&](auto tag) { return st.g_odd ? fn(tag, std::true_type{}) : fn(tag, std::false_type{}); };
+    switch (st.storage) {
+    case LBM_STORAGE_FP32: return with(float{});
+    case LBM_STORAGE_FP16: return with(__half{});
+    case LBM_STORAGE_BF16: return with(__nv_bfloat16{});
+    default: return cudaErrorInvalidValue;
+    }
 }
 
 }  // namespace
 
-size_t adjoint_partial_count(const Box &b) { return grid_for(b.n); }
-
-cudaError_t launch_phi(const Box &b, const float *F, float *phi, cudaStream_t s)
+size_t adjoint_blocks(const Box &b)
 {
-    phi_kernel<<<grid_for(b.n), kThreads, 0, s>>>(b, F, phi);
-    return cudaGetLastError();
+    const dim3 g = adjoint_grid(b);
+    return (size_t)g.x * g.y * g.z;
 }
 
-cudaError_t launch_objective(const Box &b, int objective, float phiStar, double scale, const float *phi,
-                             const float *G, double *partials, double *ab, double *acc, cudaStream_t s)
+cudaError_t launch_adjoint_phi(const Box &b, float eta, const Quant &q, const NativeState &st, float *phi,
+                               cudaStream_t s)
 {
-    const unsigned blocks = grid_for(b.n);
-    objective_kernel<<<blocks, kThreads, 0, s>>>(b, objective, phiStar, phi, G, partials);
-    cudaError_t e = cudaGetLastError();
+    NativeState even = st;
+    even.g_odd = false;   // phi does not read g
+    return dispatch(even, [&](auto tag, auto) {
+        using ST = decltype(tag);
+        adjoint_phi_kernel<ST><<<adjoint_grid(b), kBlock, 0, s>>>(b, eta, q, st.f0, static_cast<const ST *>(st.fq),
+                                                                 st.f_streamed ? 1 : 0, phi);
+        return cudaGetLastError();
+    });
+}
+
+cudaError_t launch_objective(const Box &b, int objective, float phiStar, double scale, const Quant &q,
+                             const NativeState &st, const float *phi, double *partials, double *ab, double *acc,
+                             cudaStream_t s)
+{
+    cudaError_t e = dispatch(st, [&](auto tag, auto odd) {
+        using ST = decltype(tag);
+        objective_kernel<ST, decltype(odd)::value><<<adjoint_grid(b), kBlock, 0, s>>>(
+            b, objective, phiStar, q, static_cast<const ST *>(st.g), phi, partials);
+        return cudaGetLastError();
+    });
     if (e != cudaSuccess) return e;
-    objective_fold_kernel<<<1, kThreads, 0, s>>>(partials, (int)blocks, scale, ab, acc);
+    objective_fold_kernel<<<1, kBlock, 0, s>>>(partials, (int)adjoint_blocks(b), scale, ab, acc);
     return cudaGetLastError();
 }
 
 cudaError_t launch_source_init(const Box &b, int objective, double scale, const double *ab, float phiStar,
-                               const float *phi, const float *G, float *lf, float *lg, float *lst, cudaStream_t s)
+                               const Quant &q, const NativeState &st, const float *phi, float *lf, float *lg,
+                               float *lst, cudaStream_t s)
 {
-    source_init_kernel<<<grid_for(b.n), kThreads, 0, s>>>(b, objective, scale, ab, phiStar, phi, G, lf, lg, lst);
-    return cudaGetLastError();
+    return dispatch(st, [&](auto tag, auto odd) {
+        using ST = decltype(tag);
+        source_init_kernel<ST, decltype(odd)::value><<<adjoint_grid(b), kBlock, 0, s>>>(
+            b, objective, scale, ab, phiStar, q, static_cast<const ST *>(st.g), phi, lf, lg, lst);
+        return cudaGetLastError();
+    });
 }
 
-cudaError_t launch_adjoint_step(const Box &b, const StepConst &c, float phiStar, const AdjointBuffers &a,
-                                bool add_source, int objective, double scale, double *acc, cudaStream_t s)
+cudaError_t launch_adjoint_step(const Box &b, const StepConst &c, float phiStar, const Quant &q,
+                                const NativeState &st, const AdjointBuffers &a, bool add_source, int objective,
+                                double scale, cudaStream_t s)
 {
-    const unsigned blocks = grid_for(b.n);
     AdjIn in;
-    in.F = a.F;
-    in.G = a.G;
+    in.g = st.g;
     in.phi = a.phi;
     in.lf = a.lf_in;
     in.lg = a.lg_in;
     in.lst = a.lst_in;
     in.lf_out = a.lf_out;
     in.lg_out = a.lg_out;
-    in.llap = a.llap;
-    in.lgrad = a.lgrad;
-    in.dgrav_partials = a.partials;
+    in.lsrc = a.lsrc;
+    in.dgrav = a.dgrav;
     in.ab = a.ab;
     in.scale = scale;
     in.objective = objective;
     in.add_source = add_source ? 1 : 0;
-    adjoint_local_kernel<<<blocks, kThreads, 0, s>>>(b, c, phiStar, in);
-    cudaError_t e = cudaGetLastError();
+    cudaError_t e = dispatch(st, [&](auto tag, auto odd) {
+        adjoint_local_kernel<decltype(tag), decltype(odd)::value>
+            <<<adjoint_grid(b), kBlock, 0, s>>>(b, c, phiStar, q, in);
+        return cudaGetLastError();
+    });
     if (e != cudaSuccess) return e;
-    sum_fold_kernel<<<1, kThreads, 0, s>>>(a.partials, (int)blocks, acc);
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    adjoint_stencil_kernel<<<grid_for(b.n), kThreads, 0, s>>>(b, a.llap, a.lgrad, a.lst_out);
+    adjoint_stencil_kernel<<<adjoint_grid(b), kBlock, 0, s>>>(b, a.lsrc, a.lst_out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_dgrav_fold(const Box &b, const double *dgrav, double *acc, cudaStream_t s)
+{
+    dgrav_fold_kernel<<<1, kBlock, 0, s>>>(dgrav, (int)adjoint_blocks(b), acc);
     return cudaGetLastError();
 }
 
 cudaError_t launch_init_adjoint(const Box &b, const lbm_derived &d, float Gamma, const float *phi0, const float *lf,
                                 const float *lst, const float *lg, float *lphi0, float *llap, cudaStream_t s)
 {
-    init_adjoint_kernel<<<grid_for(b.n), kThreads, 0, s>>>(b, d.alpha4, d.kappa, d.phiStarSq, Gamma, phi0, lf, lst,
+    init_adjoint_kernel<<<adjoint_grid(b), kBlock, 0, s>>>(b, d.alpha4, d.kappa, d.phiStarSq, Gamma, phi0, lf, lst,
                                                            lg, lphi0, llap);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    init_adjoint_stencil_kernel<<<grid_for(b.n), kThreads, 0, s>>>(b, llap, lphi0);
+    init_adjoint_stencil_kernel<<<adjoint_grid(b), kBlock, 0, s>>>(b, llap, lphi0);
     return cudaGetLastError();
 }
 

@@ -40,7 +40,7 @@
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
-#include "lbm_internal.h"
+#include "lattice.cuh"
 
 namespace lbm {
 namespace {
@@ -65,55 +65,9 @@ static_assert(TX == 32 && TY == 8, "issuer roles assume a 32 x 8 tile");
 constexpr float kInv6 = 0.16666666666666666667f;
 constexpr float kInv12 = 0.08333333333333333333f;
 
-// D3Q19 lattice vectors and opposite directions (reference order).
-__host__ __device__ constexpr int kCx(int i)
-{
-    return (i == 1 || i == 7 || i == 9 || i == 11 || i == 13) ? 1
-           : (i == 2 || i == 8 || i == 10 || i == 12 || i == 14) ? -1 : 0;
-}
-__host__ __device__ constexpr int kCy(int i)
-{
-    return (i == 3 || i == 7 || i == 10 || i == 15 || i == 17) ? 1
-           : (i == 4 || i == 8 || i == 9 || i == 16 || i == 18) ? -1 : 0;
-}
-__host__ __device__ constexpr int kCz(int i)
-{
-    return (i == 5 || i == 11 || i == 14 || i == 15 || i == 18) ? 1
-           : (i == 6 || i == 12 || i == 13 || i == 16 || i == 17) ? -1 : 0;
-}
-__host__ __device__ constexpr int kOpp(int i) { return i == 0 ? 0 : ((i & 1) ? i + 1 : i - 1); }
-
 template <int I>
 struct Dir {
     static constexpr int value = I;
-};
-
-// Storage formats: element conversions, and the resident blocks per SM the
-// launch bounds ask for.  FP32 stages 108 KB of shared memory per block (2
-// blocks per SM); the 16-bit formats stage 70 KB, and 3 blocks per SM fit when
-// the kernel stays within 85 registers (it does, without spills).
-template <typename ST>
-struct Fmt;
-template <>
-struct Fmt<float> {
-    static constexpr int kMinBlocks = 2;
-    static constexpr bool kMapped = false;
-    __device__ static float load(float v) { return v; }
-    __device__ static float store(float v) { return v; }
-};
-template <>
-struct Fmt<__half> {
-    static constexpr int kMinBlocks = 3;
-    static constexpr bool kMapped = true;
-    __device__ static float load(__half v) { return __half2float(v); }
-    __device__ static __half store(float v) { return __float2half_rn(v); }
-};
-template <>
-struct Fmt<__nv_bfloat16> {
-    static constexpr int kMinBlocks = 3;
-    static constexpr bool kMapped = true;
-    __device__ static float load(__nv_bfloat16 v) { return __bfloat162float(v); }
-    __device__ static __nv_bfloat16 store(float v) { return __float2bfloat16_rn(v); }
 };
 
 // Staging geometry implied by the element size.
@@ -144,7 +98,8 @@ struct StepPtrs {
     float *f0out;
     const ST *fin[kQf - 1];   // f_1 .. f_6
     ST *fout[kQf - 1];
-    ST *g[kQg];
+    const ST *gin[kQg];       // g read (== g for the in-place AA update)
+    ST *g[kQg];               // g written
     float *mom[5];
 };
 
@@ -294,7 +249,7 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Quan
             const unsigned base = (unsigned)z * (unsigned)b.nxy + (unsigned)(g_row_0 + g_x_hi);
             for_my_dirs([&](auto d) {
                 constexpr int i = decltype(d)::value;
-                cp_async16(dst + i * TY * W + E + E * g_k, P.g[i] + base);
+                cp_async16(dst + i * TY * W + E + E * g_k, P.gin[i] + base);
             });
         } else {
             const unsigned zb0 = (unsigned)z * (unsigned)b.nxy;
@@ -305,7 +260,7 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Quan
                 constexpr int cx = kCx(i), cy = kCy(i), cz = kCz(i);
                 const unsigned zb = cz > 0 ? zbp : (cz < 0 ? zbm : zb0);
                 const int row = cy > 0 ? g_row_p : (cy < 0 ? g_row_m : g_row_0);
-                const ST *src = P.g[kOpp(i)] + (zb + (unsigned)row);
+                const ST *src = P.gin[kOpp(i)] + (zb + (unsigned)row);
                 ST *d_row = dst + i * TY * W;
                 if (cx > 0) {
                     cp_async16(d_row + E * g_k, src + g_x_lo);
@@ -592,11 +547,15 @@ cudaError_t launch_typed(const Box &b, const StepConst &c, const Quant &q, const
     const ST *fin = static_cast<const ST *>(v.fq_in);
     ST *fout = static_cast<ST *>(v.fq_out);
     ST *g = static_cast<ST *>(v.g);
+    const ST *gin = static_cast<const ST *>(v.g_in ? v.g_in : v.g);
     for (int a = 0; a < kQf - 1; a++) {
         P.fin[a] = fin + (size_t)a * b.n;
         P.fout[a] = fout + (size_t)a * b.n;
     }
-    for (int i = 0; i < kQg; i++) P.g[i] = g + (size_t)i * b.n;
+    for (int i = 0; i < kQg; i++) {
+        P.gin[i] = gin + (size_t)i * b.n;
+        P.g[i] = g + (size_t)i * b.n;
+    }
     for (int i = 0; i < 5; i++) P.mom[i] = v.mom + (size_t)i * b.n;
     cudaError_t e = configure<ST, true, false>();
     if (e == cudaSuccess) e = configure<ST, false, true>();

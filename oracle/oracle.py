@@ -62,6 +62,8 @@ def oracle_lib() -> C.CDLL:
         lib.zo_adjoint_run.restype = C.c_double
         lib.zo_objective_run.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_int, C.c_int]
         lib.zo_objective_run.restype = C.c_double
+        lib.zo_heavy_mask.argtypes = [C.c_void_p, C.c_int, C.c_long]
+        lib.zo_heavy_mask.restype = C.c_int
         lib.zo_init_adjoint.argtypes = [C.c_void_p, _D, _D, _D, _D, _D]
         _oracle_lib = lib
     return _oracle_lib
@@ -162,6 +164,13 @@ class Oracle:
 
     def objective(self, T: int, grav: float, objective: str = "light_uz_mean", window: int = 1) -> float:
         return float(self.lib.zo_objective_run(self.h, int(T), float(grav), self.OBJECTIVES[objective], int(window)))
+
+    def heavy_mask(self, mode: str, steps: int = 0) -> None:
+        """Heavy-node log: "record" H(phi > 0) of the next `steps` collisions
+        after init, "replay" it instead of testing phi, "off"."""
+        code = {"off": 0, "record": 1, "replay": 2}[mode]
+        if self.lib.zo_heavy_mask(self.h, code, int(steps)) != 0:
+            raise RuntimeError(f"zo_heavy_mask({mode}) failed")
 
     def init_adjoint(self, phi0, lf, lg):
         """dJ/dphi0 and dJ/drho0 from dJ/ds^0 through the initial equilibrium (periodic z)."""

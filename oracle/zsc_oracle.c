@@ -61,6 +61,11 @@ typedef struct zo_ctx {
     double *f[7], *fp[7];     /* streamed / post-collision (reference lower / upper half) */
     double *g[19], *gp[19];
     double *phi, *rho, *ux, *uy, *uz;   /* moment arrays as the reference holds them */
+    /* Heavy-node log (test aid for finite differences, see zo_heavy_mask):
+     * one byte per node and collision, H(phi > 0) of each step. */
+    unsigned char *heavy_log;
+    long heavy_cap, heavy_pos;
+    int heavy_mode;               /* 0 phi > 0, 1 record, 2 replay */
 } zo_ctx;
 
 static inline long zo_idx(const zo_ctx *s, int x, int y, int z)
@@ -139,6 +144,7 @@ void zo_destroy(zo_ctx *s)
     for (int i = 0; i < 7; i++) { free(s->f[i]); free(s->fp[i]); }
     for (int i = 0; i < 19; i++) { free(s->g[i]); free(s->gp[i]); }
     free(s->phi); free(s->rho); free(s->ux); free(s->uy); free(s->uz);
+    free(s->heavy_log);
     free(s);
 }
 
@@ -247,6 +253,7 @@ void zo_init(zo_ctx *s, const double *phi, const double *rho, const double *ux, 
              const double *uz, const double *ghost)
 {
     const zo_const *c = &s->c;
+    s->heavy_pos = 0;
     memcpy(s->phi, phi, sizeof(double) * s->n);
     memcpy(s->rho, rho, sizeof(double) * s->n);
     memcpy(s->ux, ux, sizeof(double) * s->n);
@@ -301,6 +308,11 @@ static void zo_moments_update(zo_ctx *s)
 static void zo_collide(zo_ctx *s, double grav)
 {
     const zo_const *c = &s->c;
+    unsigned char *heavy_log = NULL;
+    if (s->heavy_mode && s->heavy_log && s->heavy_pos + s->n <= s->heavy_cap) {
+        heavy_log = s->heavy_log + s->heavy_pos;
+        s->heavy_pos += s->n;
+    }
 #pragma omp parallel for schedule(static)
     for (int z = 0; z < s->nz; z++) {
         for (int y = 0; y < s->ny; y++) {
@@ -312,7 +324,12 @@ static void zo_collide(zo_ctx *s, double grav)
                 const double mu = c->alpha4 * ph * (ph * ph - c->phiStarSq) - c->kappa * lap;
                 const double Fx = mu * gx, Fy = mu * gy;
                 double Fz = mu * gz;
-                if (ph > 0.0) Fz += grav;
+                int heavy = ph > 0.0;
+                if (heavy_log) {
+                    if (s->heavy_mode == 2) heavy = heavy_log[id];
+                    else heavy_log[id] = (unsigned char)heavy;
+                }
+                if (heavy) Fz += grav;
                 const double ux = s->ux[id] + 0.5 * Fx / rh;
                 const double uy = s->uy[id] + 0.5 * Fy / rh;
                 const double uz = s->uz[id] + 0.5 * Fz / rh;
@@ -876,4 +893,41 @@ void zo_init_adjoint(const zo_ctx *s, const double *phi0, const double *lf0, con
         }
     }
     free(llap);
+}
+
+/* Heavy-node log for finite-difference checks of the adjoint.  The gravity
+ * term is switched on by H(phi > 0) (src/collision_f.cu:96), so J is only
+ * piecewise smooth in the force: nodes whose phi crosses zero make finite
+ * differences jump.  mode 1 records H of every node and collision for `steps`
+ * collisions after the next zo_init; mode 2 replays the recorded H instead of
+ * testing phi (the forward map with the heavy set frozen, whose derivative is
+ * what the discrete adjoint computes); mode 0 frees the log.  Returns 0, or
+ * -1 when the log cannot be allocated or replay has nothing recorded. */
+int zo_heavy_mask(zo_ctx *s, int mode, long steps)
+{
+    s->heavy_pos = 0;
+    if (mode == 0) {
+        free(s->heavy_log);
+        s->heavy_log = NULL;
+        s->heavy_cap = 0;
+        s->heavy_mode = 0;
+        return 0;
+    }
+    if (mode == 1) {
+        free(s->heavy_log);
+        s->heavy_cap = steps * s->n;
+        s->heavy_log = (unsigned char *)malloc((size_t)s->heavy_cap);
+        if (!s->heavy_log) {
+            s->heavy_cap = 0;
+            s->heavy_mode = 0;
+            return -1;
+        }
+        s->heavy_mode = 1;
+        return 0;
+    }
+    if (mode == 2 && s->heavy_log) {
+        s->heavy_mode = 2;
+        return 0;
+    }
+    return -1;
 }
