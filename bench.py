@@ -54,6 +54,8 @@ def parse_args(argv=None):
     ap.add_argument("--no-variants", action="store_true", help="time only --storage (not the other formats)")
     ap.add_argument("--stat-every", type=int, default=100, help="lbm_stats cadence inside the e2e run")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint / forward time ratio")
+    ap.add_argument("--no-ref-cuda", action="store_true", help="skip timing the reference's own CUDA build")
+    ap.add_argument("--ref-cuda-steps", type=int, default=500)
     ap.add_argument("--adjoint-long", action="store_true",
                     help="also run the long-horizon adjoint (256^3, 64 bubbles, T = 20000, FP16 state, 40 GB)")
     return ap.parse_args(argv)
@@ -296,7 +298,74 @@ def run_ours(args, rank, world, local):
             result["adjoint_long"] = run_adjoint(local, long_horizon=True)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         result["cpu_baseline"] = cpu_baseline(inp)
+    if rank == 0 and world == 1 and not args.no_ref_cuda:
+        result["reference_cuda"] = run_reference_cuda(inp, args.ref_cuda_steps, local, value)
     return result
+
+
+REF_STATS_KEYS = ("ux", "uy", "uz", "Umax", "Vef", "Ref")
+
+
+def run_reference_cuda(inp, steps, local, ours_mlups):
+    """The reference's own CUDA program on this GPU (baseline only).
+
+    oracle/_ref/lbm_ref_cuda is src/main.cu compiled unmodified for sm_103a with
+    src/Makefile's -O3 -use_fast_math and a single-rank MPI stub (one rank
+    exchanges its z halos with itself: periodic wrap, as here).  It runs the
+    same box and physics with the first 20 bubbles of the workload (its
+    MAX_BUBBLES, src/constants.h:28; the step's cost does not depend on the
+    bubbles), relaxStep = 0 and `steps` evolution steps, stats and VTK output
+    outside the loop (its three ASCII VTK files go to /dev/null).  The value is
+    its own "Evolution time" (CUDA events around the evolution loop,
+    src/main.cu:645-653) per step; every step includes its nine kernels and
+    the three host-staged halo exchanges.  Its final stats.out line is
+    compared with lbm_stats of this library after the same steps from the same
+    input."""
+    import dataclasses
+    from lbm_bench_gpu_gb300 import capi, inputs
+    binary = ROOT / "oracle" / "_ref" / "lbm_ref_cuda"
+    if not binary.exists():
+        return {"unavailable": "oracle/_ref/lbm_ref_cuda not built (reference sources absent at build time)"}
+    sub = dataclasses.replace(inp, bubbles=inp.bubbles[:20], max_step=steps + 1, relax_step=0,
+                              save=10 ** 9, stat=10 ** 9)
+    nodes = inp.nx * inp.ny * inp.nz
+    with tempfile.TemporaryDirectory() as d:
+        inputs.write_inputs(d, sub)
+        for name in ("relax_data_00_0000000.vtk", "data_00_0000000.vtk", f"data_00_{steps + 1:07d}.vtk"):
+            os.symlink("/dev/null", os.path.join(d, name))
+        env = dict(os.environ, CUDA_VISIBLE_DEVICES=os.environ.get("CUDA_VISIBLE_DEVICES", str(local)))
+        t0 = time.perf_counter()
+        r = subprocess.run([str(binary)], cwd=d, capture_output=True, text=True, timeout=900, env=env)
+        wall = time.perf_counter() - t0
+        if r.returncode != 0:
+            return {"unavailable": f"reference CUDA build exited {r.returncode}: {r.stderr.strip()[-200:]}"}
+        evo = None
+        for line in r.stdout.splitlines():
+            if line.startswith("Evolution time"):
+                evo = float(line.split(":")[1].split()[0])
+        rows = [l.split() for l in Path(d, "stats.out").read_text().splitlines() if l and not l.startswith("#")]
+    if evo is None or not rows:
+        return {"unavailable": "reference CUDA build printed no evolution time / stats"}
+    ref = dict(zip(REF_STATS_KEYS, map(float, rows[-1][1:7])))
+    ms_step = evo / steps
+    out = {"value": round(nodes / (ms_step / 1e3) / 1e6, 1), "unit": "MLUPS", "ms_per_step": round(ms_step, 4),
+           "steps": steps, "speedup_of_ours": round(ours_mlups / (nodes / (ms_step / 1e3) / 1e6), 2),
+           "kind": "reference src/main.cu, nvcc -O3 -use_fast_math sm_103a, one rank (MPI stub)",
+           "sample": f"{inp.nx}^3, first 20 of the workload's bubbles, {steps} evolution steps, "
+                     f"its own CUDA-event evolution time; process wall {wall:.1f} s",
+           "final_stats": ref}
+    # the same run through this library: moments at the start of the last step, compat stats
+    p = params_for(sub, "fp32", local)
+    grav = float(capi.derive(p).grav)
+    with capi.Lattice.from_bubbles(p, sub.bubbles) as lat:
+        s0, _ = lat.stats()
+        lat.step(steps, grav)
+        s, _ = lat.stats()
+    ours = {"ux": s["ux_av"], "uy": s["uy_av"], "uz": s["uz_av"], "Umax": s["umax"],
+            "Vef": s["vol"] / s0["vol"], "Ref": s["ref"]}
+    out["ours_final_stats"] = ours
+    out["stats_rel_diff"] = {k: abs(ours[k] - ref[k]) / max(abs(ref[k]), 1e-30) for k in REF_STATS_KEYS}
+    return out
 
 
 def run_adjoint(local, long_horizon=False):

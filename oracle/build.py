@@ -5,6 +5,13 @@
 * ``build_reference()`` compiles the reference's own step kernels for the host
   CPU (``oracle/ref_harness/zsc_ref_cpu.cpp`` + the reference sources, through
   the CUDA/MPI emulation shim) into ``oracle/_ref/libzsc_ref.so``.
+* ``build_reference_cuda()`` compiles the reference's own CUDA program
+  (``src/main.cu``, unmodified, with its ``src/Makefile`` flags ``-O3
+  -use_fast_math``) for sm_103a against a single-rank MPI stub
+  (``oracle/ref_harness/mpi_stub/mpi.h``) into ``oracle/_ref/lbm_ref_cuda``:
+  the reference's GPU step, timed beside the product as a baseline.  CUDA 13
+  no longer declares ``cudaThreadSynchronize``; it is mapped to
+  ``cudaDeviceSynchronize`` on the command line.
 
 The reference sources are read from ``$LBM_REFERENCE_SRC`` (default: the
 reference checkout's ``src/`` directory at /root/reference/src).  Where that
@@ -14,7 +21,7 @@ checkout, such as the GPU host, builds from that staged copy).  Nothing is
 patched: inputs with more bubbles than the reference's MAX_BUBBLES are fed in
 as a phi field instead (see ``zr_init``).
 
-Usage: ``python oracle/build.py [oracle|reference|all]``.
+Usage: ``python oracle/build.py [oracle|reference|reference_cuda|all]``.
 """
 from __future__ import annotations
 
@@ -42,6 +49,9 @@ REFERENCE_FILES = [
     "collision_f.cu", "collision_g.cu", "pack_mpi.cu", "pack_mpi_f.cu", "pack_mpi_phi.cu",
     "stream_f.cu", "stream_g.cu", "unpack_mpi.cu", "unpack_mpi_f.cu", "unpack_mpi_phi.cu",
 ]
+# ... and what src/main.cu adds for the GPU program.
+REFERENCE_CUDA_FILES = ["main.cu", "vtksave.c"]
+REF_CUDA_BIN = REF_DIR / "lbm_ref_cuda"
 
 # Deterministic IEEE float arithmetic on x86-64 and aarch64 alike: no
 # contraction into fused multiply-adds, no fast-math.
@@ -81,7 +91,7 @@ def stage_reference() -> Path | None:
     if not all((p / f).exists() for f in REFERENCE_FILES):
         return REF_STAGE if all((REF_STAGE / f).exists() for f in REFERENCE_FILES) else None
     REF_STAGE.mkdir(parents=True, exist_ok=True)
-    for f in REFERENCE_FILES:
+    for f in REFERENCE_FILES + [f for f in REFERENCE_CUDA_FILES if (p / f).exists()]:
         dst = REF_STAGE / f
         if not dst.exists() or dst.read_bytes() != (p / f).read_bytes():
             shutil.copyfile(p / f, dst)
@@ -105,12 +115,34 @@ def build_reference(force: bool = False) -> Path | None:
     return REF_SO
 
 
+def build_reference_cuda(force: bool = False) -> Path | None:
+    """Compile the reference's CUDA program for sm_103a; None if its sources or nvcc are absent."""
+    stage_reference()
+    src_dir = reference_src_dir()
+    if src_dir is None or not all((src_dir / f).exists() for f in REFERENCE_CUDA_FILES):
+        return None
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not Path(nvcc).exists():
+        return None
+    stub = HERE / "ref_harness" / "mpi_stub" / "mpi.h"
+    deps = [stub] + [src_dir / f for f in REFERENCE_FILES + REFERENCE_CUDA_FILES]
+    REF_DIR.mkdir(exist_ok=True)
+    if force or not _newer(REF_CUDA_BIN, deps):
+        cmd = [nvcc, "-O3", "-use_fast_math", "-gencode", "arch=compute_103a,code=sm_103a", "-w",
+               "-DcudaThreadSynchronize=cudaDeviceSynchronize", "-include", "stdlib.h",
+               "-I", str(stub.parent), "-I", str(src_dir), str(src_dir / "main.cu"), "-o", str(REF_CUDA_BIN)]
+        subprocess.run(cmd, check=True)
+    return REF_CUDA_BIN
+
+
 def main(argv: list[str]) -> int:
     what = argv[1] if len(argv) > 1 else "all"
     if what in ("oracle", "all"):
         print(build_oracle(force=True))
     if what in ("reference", "all"):
         print(build_reference(force=True) or "reference sources not found")
+    if what in ("reference_cuda", "all"):
+        print(build_reference_cuda(force=True) or "reference sources or nvcc not found")
     return 0
 
 
