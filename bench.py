@@ -317,7 +317,7 @@ def run_reference_cuda(inp, steps, local, ours_mlups):
     bubbles), relaxStep = 0 and `steps` evolution steps, stats and VTK output
     outside the loop (its three ASCII VTK files go to /dev/null).  The value is
     its own "Evolution time" (CUDA events around the evolution loop,
-    src/main.cu:645-653) per step; every step includes its nine kernels and
+    src/main.cu:613-624) per step; every step includes its nine kernels and
     the three host-staged halo exchanges.  Its final stats.out line is
     compared with lbm_stats of this library after the same steps from the same
     input."""

@@ -72,7 +72,7 @@ typedef struct lbm_derived {
     float eta, eta2, invEta2;
     float invTauPhi, invTauPhiOne;
     float alpha, alpha4, kappa;
-    float gravity, grav;      /* grav: the body force of the evolution loop (src/main.cu:397) */
+    float gravity, grav;      /* grav: the body force of the evolution loop (src/main.cu:479) */
     float K0, K1, K2, KC0, KC1, KC2;
 } lbm_derived;
 
@@ -106,7 +106,7 @@ int lbm_read_inputs(const char *dir, lbm_params *p, lbm_run *run, float *bubbles
 int lbm_derive(const lbm_params *p, lbm_derived *d);
 
 /* Create a context and the initial state from host fields, each nx*ny*nz
- * values: host init -> upload -> init_f/init_g of src/main.cu:213-274.  The
+ * values: host init -> upload -> init_f/init_g of src/main.cu:294-358.  The
  * initial equilibrium is at rest (src/init_f.cu:72-78, src/init_g.cu:77-91);
  * u0 only fills the velocity arrays.  phi_ghost may be NULL (periodic z) or
  * 2*nx*ny values: the plane below z = 0, then the plane above z = nz-1, which
@@ -122,7 +122,7 @@ int lbm_init(lbm_ctx **out, const lbm_params *p, const float *phi0, const float 
 int lbm_init_bubbles(lbm_ctx **out, const lbm_params *p, const float *bubbles, int nbubbles);
 
 /* Advance nsteps time steps with body force grav (0 while relaxing): the loop
- * bodies of src/main.cu:281-392 and :414-528 without their stats/vtk output.
+ * bodies of src/main.cu:363-473 and :496-608 without their stats/vtk output.
  * One fused kernel per step.  Asynchronous on the context's stream. */
 int lbm_step(lbm_ctx *c, int nsteps, float grav);
 
@@ -134,6 +134,26 @@ int lbm_step(lbm_ctx *c, int nsteps, float grav);
  * nx*ny*nz floats.  s may be NULL.  Returns LBM_ENAN (after filling s) when a
  * field holds NaN or Inf.  Synchronises. */
 int lbm_stats(lbm_ctx *c, lbm_stats_out *s, float *phi, float *rho, float *ux, float *uy, float *uz);
+
+/* The same statistics of caller-supplied host fields (nx*ny*nz floats each,
+ * all required), reduced on the context's GPU.  The reference computes its
+ * statistics and Laplace check on its host copies of the fields
+ * (src/stats.c:28-96, src/logsave.c:63-167), which it refreshes only at its
+ * output points (phi and u every `stat` steps, rho every `save` steps,
+ * src/main.cu:457-472); a driver that keeps host copies on the same schedule
+ * reproduces its logs exactly with this call.  Synchronises. */
+int lbm_stats_fields(lbm_ctx *c, lbm_stats_out *s, const float *phi, const float *rho, const float *ux,
+                     const float *uy, const float *uz);
+
+/* Pressure of every node from the current phi and rho (the expression of
+ * src/vtksave.c:63-127, periodic neighbours) into nx*ny*nz host floats.
+ * Synchronises. */
+int lbm_pressure(lbm_ctx *c, float *p);
+
+/* Name (NUL-terminated, truncated to len - 1 characters) and total memory of
+ * a CUDA device, for run logs (src/main.cu:94-119, src/logsave.c:189-194).  Either output may be
+ * NULL. */
+int lbm_device_name(int device, char *name, int len, double *total_bytes);
 
 /* The current distributions in streamed form, as the reference's lower halves
  * hold them after a step: f as 7 blocks and g as 19 blocks of nx*ny*nz floats

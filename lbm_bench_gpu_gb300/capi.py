@@ -23,7 +23,7 @@ EXPORTS = [
     "lbm_read_inputs", "lbm_derive", "lbm_init", "lbm_init_bubbles", "lbm_step", "lbm_stats",
     "lbm_get_dist", "lbm_set_dist", "lbm_steps_done", "lbm_stream", "lbm_sync", "lbm_destroy",
     "lbm_strerror", "lbm_last_error", "lbm_stats_noalloc", "lbm_step_adjoint",
-    "lbm_objective",
+    "lbm_objective", "lbm_stats_fields", "lbm_pressure", "lbm_device_name",
 ]
 OBJECTIVES = {"light_uz_mean": 0, "light_z_centroid": 1}
 
@@ -109,6 +109,9 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
                                       C.c_void_p, C.c_void_p, C.c_void_p]
     lib.lbm_step_adjoint.argtypes = [C.c_void_p, C.POINTER(AdjointOpts), C.POINTER(AdjointOut)]
     lib.lbm_objective.argtypes = [C.c_void_p, C.POINTER(AdjointOpts), C.POINTER(C.c_double)]
+    lib.lbm_stats_fields.argtypes = [C.c_void_p, C.POINTER(StatsOut), _F, _F, _F, _F, _F]
+    lib.lbm_pressure.argtypes = [C.c_void_p, _F]
+    lib.lbm_device_name.argtypes = [C.c_int, C.c_char_p, C.c_int, C.POINTER(C.c_double)]
     lib.lbm_steps_done.argtypes = [C.c_void_p]
     lib.lbm_steps_done.restype = C.c_longlong
     lib.lbm_stream.argtypes = [C.c_void_p]
@@ -216,6 +219,21 @@ class Lattice:
         arrs = [np.empty(self.shape, np.float32) for _ in range(5)]
         check(load().lbm_stats(self._h, None, *[fptr(a) for a in arrs]), "lbm_stats")
         return dict(zip(("phi", "rho", "ux", "uy", "uz"), arrs))
+
+    def stats_of(self, phi, rho, ux, uy, uz, allow_nan: bool = False) -> dict:
+        """lbm_stats_fields: the statistics of the given host fields."""
+        s = StatsOut()
+        arrs = [np.ascontiguousarray(a, np.float32) for a in (phi, rho, ux, uy, uz)]
+        code = load().lbm_stats_fields(self._h, C.byref(s), *[fptr(a) for a in arrs])
+        if not (allow_nan and code == LBM_ENAN):
+            check(code, "lbm_stats_fields")
+        return s.as_dict()
+
+    def pressure(self) -> np.ndarray:
+        """lbm_pressure: the pressure field of the current phi and rho."""
+        p = np.empty(self.shape, np.float32)
+        check(load().lbm_pressure(self._h, fptr(p)), "lbm_pressure")
+        return p
 
     def dist(self):
         f = np.empty((7,) + self.shape, np.float32)

@@ -189,6 +189,10 @@ int init_from_mom(lbm_ctx *c, const float *ghost_lo, const float *ghost_hi)
     return rc;
 }
 
+// lbm_stats_out from the 16 raw stats values (the reference's formulas of
+// src/stats.c:60-91 and src/logsave.c:152-167, in FP64).
+int fill_stats(const lbm_ctx *c, const double *r, lbm_stats_out *s);
+
 }  // namespace
 
 namespace lbm {
@@ -312,7 +316,62 @@ extern "C" int lbm_stats(lbm_ctx *c, lbm_stats_out *s, float *phi, float *rho, f
                      "field copy");
     LBM_CUDA(cudaStreamSynchronize(c->stream), "lbm_stats");
     if (!s) return LBM_OK;
-    const double *r = c->result_host;
+    return fill_stats(c, c->result_host, s);
+}
+
+extern "C" int lbm_stats_fields(lbm_ctx *c, lbm_stats_out *s, const float *phi, const float *rho, const float *ux,
+                                const float *uy, const float *uz)
+{
+    if (!c || !s) return fail(LBM_EINVAL, "lbm_stats_fields: NULL context or output");
+    if (!phi || !rho || !ux || !uy || !uz) return fail(LBM_EINVAL, "lbm_stats_fields: every field is required");
+    LBM_CUDA(cudaSetDevice(c->p.device), "cudaSetDevice");
+    const size_t n = (size_t)c->box.n, bytes = sizeof(float) * n;
+    float *tmp = nullptr;
+    LBM_CUDA(cudaMalloc(&tmp, 5 * bytes), "lbm_stats_fields scratch");
+    const float *src[5] = {phi, rho, ux, uy, uz};
+    cudaError_t e = cudaSuccess;
+    for (int a = 0; a < 5 && e == cudaSuccess; a++)
+        e = cudaMemcpyAsync(tmp + a * n, src[a], bytes, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess)
+        e = lbm::launch_stats(c->box, c->d, tmp, c->partials, c->partial_count, c->result, nullptr, c->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(c->result_host, c->result, sizeof(double) * lbm::kStatsValues, cudaMemcpyDeviceToHost,
+                            c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cudaFree(tmp);
+    if (e != cudaSuccess) return cuda_fail(e, "lbm_stats_fields");
+    return fill_stats(c, c->result_host, s);
+}
+
+extern "C" int lbm_pressure(lbm_ctx *c, float *p)
+{
+    if (!c || !p) return fail(LBM_EINVAL, "lbm_pressure: NULL argument");
+    LBM_CUDA(cudaSetDevice(c->p.device), "cudaSetDevice");
+    const size_t n = (size_t)c->box.n;
+    float *tmp = nullptr;
+    LBM_CUDA(cudaMalloc(&tmp, sizeof(float) * n), "lbm_pressure scratch");
+    cudaError_t e = lbm::launch_pressure(c->box, c->d, c->st.mom, tmp, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(p, tmp, sizeof(float) * n, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cudaFree(tmp);
+    return e == cudaSuccess ? LBM_OK : cuda_fail(e, "lbm_pressure");
+}
+
+extern "C" int lbm_device_name(int device, char *name, int len, double *total_bytes)
+{
+    cudaDeviceProp prop;
+    LBM_CUDA(cudaGetDeviceProperties(&prop, device), "cudaGetDeviceProperties");
+    if (name && len > 0) {
+        std::strncpy(name, prop.name, (size_t)len - 1);
+        name[len - 1] = '\0';
+    }
+    if (total_bytes) *total_bytes = (double)prop.totalGlobalMem;
+    return LBM_OK;
+}
+
+namespace {
+int fill_stats(const lbm_ctx *c, const double *r, lbm_stats_out *s)
+{
     std::memset(s, 0, sizeof(*s));
     s->step = c->st.steps;
     s->umax = std::sqrt(r[0]);
@@ -337,6 +396,7 @@ extern "C" int lbm_stats(lbm_ctx *c, lbm_stats_out *s, float *phi, float *rho, f
     if (s->nonfinite > 0) return fail(LBM_ENAN, std::to_string(s->nonfinite) + " non-finite nodes");
     return LBM_OK;
 }
+}  // namespace
 
 extern "C" int lbm_get_dist(lbm_ctx *c, float *f, float *g)
 {

@@ -126,6 +126,8 @@ cudaError_t launch_moments(const Box &b, const float *f, const float *g, float *
 cudaError_t launch_stats(const Box &b, const lbm_derived &d, const float *mom, double *partials,
                          size_t partial_count, double *result, unsigned long long *counters, cudaStream_t s);
 size_t stats_partial_count(const Box &b);
+// Pressure field (n floats) of the mom arrays (src/vtksave.c:63-127).
+cudaError_t launch_pressure(const Box &b, const lbm_derived &d, const float *mom, float *out, cudaStream_t s);
 
 // Adjoint (zsc_adjoint.cu).  acc[0] accumulates J, acc[1] dJ/dgrav (FP64).
 // All adjoint kernels run on one grid of 32 x 8 column tiles, each block

@@ -150,6 +150,43 @@ __global__ void __launch_bounds__(kThreads) fold_kernel(const double *__restrict
     block_reduce(acc, out);
 }
 
+// Pressure of every node (src/vtksave.c:63-127): the same float expression as
+// the stats, periodic neighbours.  One thread per node of a row-major grid.
+__global__ void __launch_bounds__(kThreads) pressure_kernel(Box b, StatsConst c, const float *__restrict__ phi,
+                                                            const float *__restrict__ rho, float *__restrict__ out)
+{
+    const int nx = b.nx, ny = b.ny, nz = b.nz;
+    const int rows = ny * nz;
+    for (int r = blockIdx.x; r < rows; r += gridDim.x) {
+        const int k = r / ny, j = r - k * ny;
+        const int jn = j == ny - 1 ? 0 : j + 1, js = j == 0 ? ny - 1 : j - 1;
+        const int kt = k == nz - 1 ? 0 : k + 1, kb = k == 0 ? nz - 1 : k - 1;
+        const size_t row_c = (size_t)r * nx;
+        const size_t row_n = ((size_t)kk_row(jn, k, ny)) * nx, row_s = ((size_t)kk_row(js, k, ny)) * nx;
+        const size_t row_t = ((size_t)kk_row(j, kt, ny)) * nx, row_b = ((size_t)kk_row(j, kb, ny)) * nx;
+        const size_t row_nt = ((size_t)kk_row(jn, kt, ny)) * nx, row_sb = ((size_t)kk_row(js, kb, ny)) * nx;
+        const size_t row_nb = ((size_t)kk_row(jn, kb, ny)) * nx, row_st = ((size_t)kk_row(js, kt, ny)) * nx;
+        for (int i = threadIdx.x; i < nx; i += blockDim.x) {
+            const size_t t = row_c + i;
+            const float ph = phi[t];
+            const int ie = i == nx - 1 ? 0 : i + 1, iw = i == 0 ? nx - 1 : i - 1;
+            const float p01 = phi[row_c + ie], p02 = phi[row_c + iw], p03 = phi[row_n + i], p04 = phi[row_s + i];
+            const float p05 = phi[row_t + i], p06 = phi[row_b + i], p07 = phi[row_n + ie], p08 = phi[row_s + iw];
+            const float p09 = phi[row_s + ie], p10 = phi[row_n + iw], p11 = phi[row_t + ie], p12 = phi[row_b + iw];
+            const float p13 = phi[row_b + ie], p14 = phi[row_t + iw], p15 = phi[row_nt + i], p16 = phi[row_sb + i];
+            const float p17 = phi[row_nb + i], p18 = phi[row_st + i];
+            const float lap = (p07 + p08 + p09 + p10 + p11 + p12 + p13 + p14 + p15 + p16 + p17 + p18
+                               + 2.f * (p01 + p02 + p03 + p04 + p05 + p06 - 12.f * ph)) * kInv6;
+            const float gx = (2.f * (p01 - p02) + p07 - p08 + p09 - p10 + p11 - p12 + p13 - p14) * kInv12;
+            const float gy = (2.f * (p03 - p04) + p07 - p08 + p10 - p09 + p15 - p16 + p17 - p18) * kInv12;
+            const float gz = (2.f * (p05 - p06) + p11 - p12 + p14 - p13 + p15 - p16 + p18 - p17) * kInv12;
+            const float ph2 = ph * ph;
+            out[t] = c.alpha * (ph2 * (3.f * ph2 - 2.f * c.phiStarSq) - c.phiStarSq * c.phiStarSq)
+                     - c.kappa * (ph * lap - 0.5f * (gx * gx + gy * gy + gz * gz)) + kCsSq * rho[t];
+        }
+    }
+}
+
 unsigned stats_blocks(const Box &b)
 {
     long long blocks = (long long)b.ny * b.nz;   // one x-row per block and pass
@@ -172,6 +209,15 @@ cudaError_t launch_stats(const Box &b, const lbm_derived &d, const float *mom, d
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     fold_kernel<<<1, kThreads, 0, s>>>(partials, (int)blocks, result);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pressure(const Box &b, const lbm_derived &d, const float *mom, float *out, cudaStream_t s)
+{
+    StatsConst c{d.alpha, d.kappa, d.phiStarSq};
+    long long blocks = (long long)b.ny * b.nz;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    pressure_kernel<<<(unsigned)blocks, kThreads, 0, s>>>(b, c, mom, mom + b.n, out);
     return cudaGetLastError();
 }
 

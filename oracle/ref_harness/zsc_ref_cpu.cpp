@@ -8,7 +8,7 @@
  * (--impl reference).  Nothing in the product links it.
  *
  * The launch sequence is the one of the reference driver: setup as in
- * src/main.cu:156-356 and one loop iteration as in src/main.cu:416-507
+ * src/main.cu:155-357 and one loop iteration as in src/main.cu:496-608
  * (update_phi, update_rho, update_velocity, phi halo, collision_f,
  * collision_g, f halo, stream_f, stream_g, distribution halo).  Kernels are
  * launched by a CPU emulation of the CUDA grid: blocks are spread over OpenMP
@@ -149,7 +149,7 @@ void set_constants()
 extern "C" {
 
 /* Read dir/properties.in and dir/discrete.in, build the initial state exactly
- * as the reference driver does (src/main.cu:156-356).  phi_override, when not
+ * as the reference driver does (src/main.cu:155-357).  phi_override, when not
  * NULL, replaces the host phi array after init() (NX*NY*(zmax+2) values
  * including both ghost planes), so that inputs with more bubbles than the
  * reference's MAX_BUBBLES can be fed in.  Returns 0 on success. */
@@ -228,7 +228,7 @@ ZR_API int zr_init(const char *dir, const float *phi_override)
 }
 
 /* nsteps iterations of the reference loop body with grav_d = grav
- * (src/main.cu:416-507; the relaxation loop is the same with grav_d = 0). */
+ * (src/main.cu:496-608; the relaxation loop is the same with grav_d = 0). */
 ZR_API int zr_step(int nsteps, float grav)
 {
     if (!ready) return 1;

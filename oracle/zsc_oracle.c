@@ -418,8 +418,8 @@ static void zo_stream(zo_ctx *s)
     }
 }
 
-/* One or more steps in the order of src/main.cu:283-373 (relaxation loop) and
- * src/main.cu:416-507 (evolution loop); grav is grav_d (0 while relaxing). */
+/* One or more steps in the order of src/main.cu:363-473 (relaxation loop) and
+ * src/main.cu:496-608 (evolution loop); grav is grav_d (0 while relaxing). */
 void zo_step(zo_ctx *s, int nsteps, double grav)
 {
     for (int t = 0; t < nsteps; t++) {

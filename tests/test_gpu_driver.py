@@ -1,0 +1,174 @@
+"""The C++ host driver (lbm_zsc) against the reference's own program.
+
+Both run the same properties.in / discrete.in: oracle/_ref/lbm_ref_cuda is the
+reference's src/main.cu built for this GPU (one rank, MPI stub), lbm_zsc the
+driver on liblbm_gb300.so.  Every output file the reference writes must exist
+with the same name and layout, and the numbers must agree:
+
+* relax_stats.out / stats.out: same rows and steps; mean velocities within
+  2e-7 + 2e-3 relative (the reference sums them in float), Umax 2e-3, Vef and
+  Ref 5e-4 (one node in ~10^4 changing sides of phi = 0 moves them 1e-4);
+* runlog.out: identical INPUT PARAMETERS / CUDA CONFIGURATION lines; Ref, Vef,
+  velocities as above.  Pin - Pout and the Laplace error: the reference sums
+  ~2.6e5 pressures of ~0.18 sequentially in a float (src/logsave.c:139-143),
+  which moves Pin - Pout (~0.0115, a difference of two such means) by ~1.6%
+  and the Laplace error (x Ro / 2 sigma) by ~1 absolute.  So the reference's
+  printed values are checked against a replay of its float arithmetic, in its
+  loop order (x outermost, z innermost), on this library's fields after the
+  same relaxation (2e-3), and the driver's FP64 values against an FP64 sum of
+  the same pressures (1e-5; the Laplace error 2e-3 absolute);
+* VTK snapshots: same files, same header lines apart from the title; Phi,
+  pressure and velocity within 6e-6 absolute ("%f" prints 1e-6; after 200
+  steps the fast-math build's phi drifts up to 3e-6 from the product's).
+
+The reference build uses -use_fast_math (src/Makefile:5); the product does not."""
+from __future__ import annotations
+
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+ROOT = Path(__file__).resolve().parents[1]
+REF_BIN = ROOT / "oracle" / "_ref" / "lbm_ref_cuda"
+DRIVER = ROOT / "lbm_bench_gpu_gb300" / "bin" / "lbm_zsc"
+
+
+def case():
+    from lbm_bench_gpu_gb300 import inputs
+    inp = inputs.Inputs(nx=64, ny=64, nz=64, max_step=101, relax_step=100, save=50, stat=25,
+                        bubbles=np.array([[22.3, 30.6, 24.2, 10.0], [41.7, 35.1, 42.4, 8.0]], np.float32))
+    inp.Eo = inputs.eo_for_gravity(-1e-5, 10.0, inp.sigma)
+    return inp
+
+
+def laplace_replay():
+    """(Pin - Pout, Laplace error) after the relaxation of case(), as the
+    reference computes them (float sums in its loop order) and in FP64."""
+    from lbm_bench_gpu_gb300 import capi
+    inp = case()
+    p = capi.make_params(inp.nx, inp.ny, inp.nz, rhoL=inp.rhoL, rhoH=inp.rhoH, tauRho=inp.tauRho,
+                         tauPhi=inp.tauPhi, width=inp.width, sigma=inp.sigma, Gamma=inp.Gamma, Eo=inp.Eo,
+                         rc0=inp.rc0)
+    with capi.Lattice.from_bubbles(p, inp.bubbles) as lat:
+        lat.step(inp.relax_step, 0.0)
+        phi = lat.fields()["phi"]
+        pres = lat.pressure()
+    # src/logsave.c:63-66: i (x) outermost, then j (y), k (z) innermost, skipping x, y = 0, n-1
+    ph = np.transpose(phi, (2, 1, 0))[1:-1, 1:-1, :].reshape(-1)
+    pr = np.transpose(pres, (2, 1, 0))[1:-1, 1:-1, :].reshape(-1)
+    inside = ph >= 0
+    sin32 = np.cumsum(pr[inside], dtype=np.float32)[-1]
+    sout32 = np.cumsum(pr[~inside], dtype=np.float32)[-1]
+    vin = np.float32(inside.sum())
+    vout = np.float32(inp.nx * inp.ny * inp.nz) - vin
+    sigma, ro = np.float32(inp.sigma), np.float32(inp.rc0)
+    dp32 = np.float32(sin32 / vin) - np.float32(sout32 / vout)
+    perr32 = np.float32(0.5) * (np.float32(2) * sigma / ro - dp32) * ro / sigma
+    vin64 = float(inside.sum())
+    dp64 = pr[inside].astype(np.float64).sum() / vin64 - pr[~inside].astype(np.float64).sum() / (
+        inp.nx * inp.ny * inp.nz - vin64)
+    perr64 = 0.5 * (2 * inp.sigma / inp.rc0 - dp64) * inp.rc0 / inp.sigma
+    return float(dp32), float(perr32), dp64, perr64
+
+
+def run_both(tmp_path):
+    from lbm_bench_gpu_gb300 import inputs
+    if not REF_BIN.exists():
+        pytest.skip("the reference's CUDA program is not built (reference sources absent at build time)")
+    inp = case()
+    out = {}
+    for name, cmd in (("ref", [str(REF_BIN)]), ("ours", [str(DRIVER), "."])):
+        d = tmp_path / name
+        inputs.write_inputs(d, inp)
+        r = subprocess.run(cmd, cwd=d, capture_output=True, text=True, timeout=600)
+        assert r.returncode == 0, (name, r.stdout[-2000:], r.stderr[-2000:])
+        out[name] = d
+    return out["ref"], out["ours"]
+
+
+def stats_rows(path):
+    return np.array([[float(x) for x in l.split()] for l in path.read_text().splitlines()
+                     if l.strip() and not l.startswith("#")])
+
+
+def runlog_sections(path):
+    sec, out = None, {}
+    for line in path.read_text().splitlines():
+        if line and not line.startswith("*") and "=" not in line:
+            sec = line.strip()
+            out[sec] = {}
+        elif "=" in line and sec:
+            k, v = line.split("=", 1)
+            out[sec][k.strip()] = v.strip()
+    return out
+
+
+def read_vtk(path):
+    lines = path.read_text().split("\n")
+    header = []
+    i = 0
+    data = {}
+    while i < len(lines):
+        l = lines[i]
+        if l.startswith("SCALARS") or l.lower().startswith("vectors"):
+            name = l.split()[1]
+            vec = l.lower().startswith("vectors")
+            i += 1 if vec else 2
+            vals = []
+            while i < len(lines) and lines[i].strip():
+                vals.append(lines[i])
+                i += 1
+            data[name] = np.array(" ".join(vals).split(), np.float64)
+            header.append(l)
+        else:
+            header.append(l)
+            i += 1
+    return header, data
+
+
+def test_driver_outputs_match_reference_program(lib, tmp_path):
+    ref, ours = run_both(tmp_path)
+    for name in ("relax_stats.out", "stats.out"):
+        a, b = stats_rows(ref / name), stats_rows(ours / name)
+        assert a.shape == b.shape, name
+        np.testing.assert_array_equal(a[:, 0], b[:, 0])
+        np.testing.assert_allclose(b[:, 1:4], a[:, 1:4], rtol=2e-3, atol=2e-7, err_msg=name)
+        np.testing.assert_allclose(b[:, 4], a[:, 4], rtol=2e-3, err_msg=name)
+        np.testing.assert_allclose(b[:, 5:7], a[:, 5:7], rtol=5e-4, err_msg=name)
+
+    la, lb = runlog_sections(ref / "runlog.out"), runlog_sections(ours / "runlog.out")
+    assert set(la) == set(lb)
+    assert la["INPUT PARAMETERS"] == lb["INPUT PARAMETERS"]
+    assert la["CUDA CONFIGURATION"] == lb["CUDA CONFIGURATION"]
+    assert set(la["TIMING INFORMATION (seconds)"]) == set(lb["TIMING INFORMATION (seconds)"])
+    tol = {"Effective Radius": (5e-4, 0), "Phase Conservation": (5e-4, 0), "Parasitic Velocity": (4e-3, 1e-12),
+           "Maximum Velocity": (4e-3, 1e-12)}
+    for sec in ("RELAXATION RESULTS", "OUTPUT RESULTS"):
+        assert set(la[sec]) == set(lb[sec]), sec
+        for k, v in la[sec].items():
+            if k in tol:
+                rtol, atol = tol[k]
+                assert float(lb[sec][k]) == pytest.approx(float(v), rel=rtol, abs=atol), (sec, k, v, lb[sec][k])
+    dp32, perr32, dp64, perr64 = laplace_replay()
+    rel = la["RELAXATION RESULTS"]
+    assert float(rel["(Pin - Pout)"]) == pytest.approx(dp32, rel=2e-3)
+    assert float(rel["Laplace Error"]) == pytest.approx(perr32, rel=2e-3, abs=2e-3)
+    ours_rel = lb["RELAXATION RESULTS"]
+    assert float(ours_rel["(Pin - Pout)"]) == pytest.approx(dp64, rel=1e-5)
+    assert float(ours_rel["Laplace Error"]) == pytest.approx(perr64, rel=1e-5, abs=2e-3)
+
+    va = sorted(p.name for p in ref.glob("*.vtk"))
+    assert va == sorted(p.name for p in ours.glob("*.vtk")) and len(va) == 7, va
+    for name in va:
+        ha, da = read_vtk(ref / name)
+        hb, db = read_vtk(ours / name)
+        assert [h for k, h in enumerate(ha) if k != 1] == [h for k, h in enumerate(hb) if k != 1], name
+        assert set(da) == set(db) == {"Phi", "Pressure", "Velocity"}, name
+        for f in da:
+            assert da[f].shape == db[f].shape, (name, f)
+            print(f"{name} {f}: max |diff| {np.abs(db[f] - da[f]).max():.2e}")
+            np.testing.assert_allclose(db[f], da[f], rtol=0, atol=6e-6, err_msg=f"{name} {f}")
