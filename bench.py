@@ -375,7 +375,8 @@ def run_adjoint(local, long_horizon=False):
            J = light-phase mean u_z over the last 200 states, FP32 state;
     long:  256^3, 64 bubbles R ~ U[6, 10], T = 20000, J = final light-phase
            z-centroid, FP16 live state (native FP16 snapshots).
-    Both with a 40 GB checkpoint budget.  The forward time is lbm_step over T
+    Both with a 40 GB checkpoint budget; the short one is repeated with the
+    library's default budget (half of the free device memory).  The forward time is lbm_step over T
     steps on the same context.  dJ/dgrav is checked against central
     differences of J from lbm_objective (the GPU forward run) with steps
     h = 1e-6, 5e-7 and 2.5e-7 on the force, and their Richardson extrapolation;
@@ -410,6 +411,10 @@ def run_adjoint(local, long_horizon=False):
         lat.sync()
         torch.cuda.synchronize()
         r = lat.adjoint(T, grav, objective, window, checkpoint_bytes=budget)
+        r_free = None
+        if not long_horizon:
+            # the same run with the library's default budget (half of the free device memory)
+            r_free = lat.adjoint(T, grav, objective, window, want_phi0=False)
         fd = {}
         for h in (1e-6, 5e-7, 2.5e-7):
             fd[h] = (lat.objective(T, grav + h, objective, window)
@@ -427,6 +432,12 @@ def run_adjoint(local, long_horizon=False):
            "fd_rel_err": abs(r["dJ_dgrav"] - fd[1e-6]) / abs(fd[1e-6]),
            "fd_rel_err_richardson": abs(r["dJ_dgrav"] - rich) / abs(rich),
            "dJ_dphi0_norm": float(np.sqrt((r["dJ_dphi0"].astype(np.float64) ** 2).sum()))}
+    if r_free is not None:
+        out["default_budget"] = {"adjoint_s": round(r_free["seconds"], 4),
+                                 "ratio": round(r_free["seconds"] / t_fwd, 3), "slots": r_free["slots"],
+                                 "checkpoint_GB": round(r_free["checkpoint_bytes_used"] / 1e9, 2),
+                                 "forward_steps": r_free["forward_steps"],
+                                 "same_gradient": r_free["dJ_dgrav"] == r["dJ_dgrav"]}
     if not long_horizon:
         g0 = r["dJ_dphi0"]
         big = np.flatnonzero(np.abs(g0) > 0.1 * np.abs(g0).max())

@@ -328,7 +328,7 @@ extern "C" int lbm_objective(lbm_ctx *c, const lbm_adjoint_opts *o, double *J)
     cudaError_t e = cudaMalloc((void **)&A.phi, sizeof(float) * n);
     if (e == cudaSuccess) e = cudaMalloc((void **)&A.mom_save, sizeof(float) * 5 * n);
     if (e == cudaSuccess) e = cudaMalloc((void **)&A.partials, sizeof(double) * 2 * nblocks);
-    if (e == cudaSuccess) e = cudaMalloc((void **)&A.ab, sizeof(double) * 2);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&A.ab, sizeof(double) * 4);
     if (e == cudaSuccess) e = cudaMalloc((void **)&A.acc, sizeof(double) * 2);
     if (e == cudaSuccess) e = cudaMalloc((void **)&A.slots, A.snap_bytes);
     if (e != cudaSuccess) {
@@ -391,7 +391,7 @@ extern "C" int lbm_step_adjoint(lbm_ctx *c, const lbm_adjoint_opts *o, lbm_adjoi
     alloc((void **)&A.mom_save, sizeof(float) * 5 * n);
     alloc((void **)&A.partials, sizeof(double) * 2 * nblocks);
     alloc((void **)&A.dgrav, sizeof(double) * nblocks);
-    alloc((void **)&A.ab, sizeof(double) * 2);
+    alloc((void **)&A.ab, sizeof(double) * 4);
     alloc((void **)&A.acc, sizeof(double) * 2);
     if (e != cudaSuccess) {
         A.release();

@@ -29,7 +29,11 @@
 //   adjoint_stencil_kernel float4 -> lst                        ~20 B/node
 // All per-node arithmetic is FP32; the objective sums and dJ/dgrav are FP64.
 // Every kernel runs on one grid: 32 x 8 column tiles, each block marching
-// kPlanes z planes, 32-bit node indices (n * 19 < 2^32 is checked at init).
+// kPlanes consecutive z planes (so the z neighbours of one plane are the
+// block's previous and next planes, mostly L1 hits), except the local kernel,
+// whose blocks take planes gridDim.z apart (with consecutive planes the
+// compiler keeps more values live across iterations and spills; measured 1%
+// slower).  32-bit node indices (n * 19 < 2^32 is checked at init).
 #include <type_traits>
 
 #include "lattice.cuh"
@@ -38,7 +42,13 @@ namespace lbm {
 namespace {
 
 constexpr int TXA = 32, TYA = 8, NTA = TXA * TYA;
-constexpr int kPlanes = 4;
+#ifndef ZSC_ADJ_PLANES
+#define ZSC_ADJ_PLANES 4
+#endif
+#ifndef ZSC_ADJ_MIN_BLOCKS
+#define ZSC_ADJ_MIN_BLOCKS 3
+#endif
+constexpr int kPlanes = ZSC_ADJ_PLANES;
 constexpr float kInv6 = 0.16666666666666666667f;
 constexpr float kInv12 = 0.08333333333333333333f;
 constexpr float kW0 = 0.33333333333333333333f, kW1 = 0.05555555555555555556f, kW2 = 0.02777777777777777778f;
@@ -139,7 +149,7 @@ __global__ void __launch_bounds__(NTA) adjoint_phi_kernel(Box b, float eta, Quan
     const unsigned n = (unsigned)b.n;
     const float eta2 = 1.f - eta;
     const int x = blockIdx.x * TXA + threadIdx.x, y = blockIdx.y * TYA + threadIdx.y;
-    for (int z = blockIdx.z; z < b.nz; z += gridDim.z) {
+    for (int z = blockIdx.z * kPlanes, z_end = min(b.nz, z + kPlanes); z < z_end; z++) {
         const Nb p = neighbourhood(b, x, y, z);
         const unsigned t = p.at(0, 0, 0);
         float s = f0[t];
@@ -167,7 +177,7 @@ __global__ void __launch_bounds__(NTA) objective_kernel(Box b, int objective, fl
     const float half_inv = 0.5f / phiStar;
     double A = 0.0, B = 0.0;
     const int x = blockIdx.x * TXA + threadIdx.x, y = blockIdx.y * TYA + threadIdx.y;
-    for (int z = blockIdx.z; z < b.nz; z += gridDim.z) {
+    for (int z = blockIdx.z * kPlanes, z_end = min(b.nz, z + kPlanes); z < z_end; z++) {
         const Nb p = neighbourhood(b, x, y, z);
         const unsigned t = p.at(0, 0, 0);
         const float w = (phiStar - phi[t]) * half_inv;
@@ -190,7 +200,8 @@ __global__ void __launch_bounds__(NTA) objective_kernel(Box b, int objective, fl
     }
 }
 
-// ab[0..1] = sums of the partials; acc[0] (J) += scale * A / B.
+// ab[0..1] = sums of the partials, ab[2] = A / B, ab[3] = scale / B;
+// acc[0] (J) += scale * A / B.
 __global__ void __launch_bounds__(NTA) objective_fold_kernel(const double *__restrict__ partials, int nparts,
                                                              double scale, double *__restrict__ ab,
                                                              double *__restrict__ acc)
@@ -206,6 +217,8 @@ __global__ void __launch_bounds__(NTA) objective_fold_kernel(const double *__res
     if (threadIdx.x == 0 && threadIdx.y == 0) {
         ab[0] = A;
         ab[1] = B;
+        ab[2] = A / B;
+        ab[3] = scale / B;
         acc[0] += scale * A / B;
     }
 }
@@ -219,11 +232,11 @@ struct SourceCoef {
     float half_inv; // 1 / (2 phiStar)
 };
 
-__device__ __forceinline__ SourceCoef source_coef(const double *ab, double scale, float phiStar)
+__device__ __forceinline__ SourceCoef source_coef(const double *ab, float phiStar)
 {
     SourceCoef k;
-    k.ratio = (float)(ab[0] / ab[1]);
-    k.s_over_b = (float)(scale / ab[1]);
+    k.ratio = (float)ab[2];
+    k.s_over_b = (float)ab[3];
     k.half_inv = 0.5f / phiStar;
     return k;
 }
@@ -256,9 +269,9 @@ __global__ void __launch_bounds__(NTA) source_init_kernel(Box b, int objective, 
                                                           float *__restrict__ lst)
 {
     const unsigned n = (unsigned)b.n;
-    const SourceCoef k = source_coef(ab, scale, phiStar);
+    const SourceCoef k = source_coef(ab, phiStar);
     const int x = blockIdx.x * TXA + threadIdx.x, y = blockIdx.y * TYA + threadIdx.y;
-    for (int z = blockIdx.z; z < b.nz; z += gridDim.z) {
+    for (int z = blockIdx.z * kPlanes, z_end = min(b.nz, z + kPlanes); z < z_end; z++) {
         const Nb p = neighbourhood(b, x, y, z);
         const unsigned t = p.at(0, 0, 0);
         float rho, m[3];
@@ -287,13 +300,11 @@ struct AdjIn {
 
 // The local part of one adjoint step (see the file comment).
 template <typename ST, bool ODD>
-__global__ void __launch_bounds__(NTA, 3) adjoint_local_kernel(Box b, StepConst c, float phiStar, Quant q, AdjIn a)
+__global__ void __launch_bounds__(NTA, ZSC_ADJ_MIN_BLOCKS) adjoint_local_kernel(Box b, StepConst c, float phiStar, Quant q, AdjIn a)
 {
     __shared__ double red[NTA / 32];
     const unsigned n = (unsigned)b.n;
     const ST *__restrict__ g = static_cast<const ST *>(a.g);
-    SourceCoef sk{};
-    if (a.add_source) sk = source_coef(a.ab, a.scale, phiStar);
     double dg = 0.0;
     const int x = blockIdx.x * TXA + threadIdx.x, y = blockIdx.y * TYA + threadIdx.y;
     for (int z = blockIdx.z; z < b.nz; z += gridDim.z) {
@@ -410,7 +421,7 @@ __global__ void __launch_bounds__(NTA, 3) adjoint_local_kernel(Box b, StepConst 
         a.lsrc[t] = make_float4(-c.kappa * lmu, mu * lF[0], mu * lF[1], mu * lF[2]);
         if (a.add_source) {
             float dphi, drho, dmz;
-            objective_source(z, a.objective, sk, phiStar, ph, rh, m[2], dphi, drho, dmz);
+            objective_source(z, a.objective, source_coef(a.ab, phiStar), phiStar, ph, rh, m[2], dphi, drho, dmz);
             lphi += dphi;
             lrho += drho;
             lm[2] += dmz;
@@ -433,32 +444,66 @@ __global__ void __launch_bounds__(NTA, 3) adjoint_local_kernel(Box b, StepConst 
 // lst = L[lambda_lap] - sum_k D_k[lambda_grad_k]: the transposed stencils.
 // Laplacian weights: 2/6 on faces, 1/6 on edges, -4 at the centre; gradient
 // component k: c_ik times 2/12 on faces, 1/12 on edges.
+//
+// The block marches its kPlanes planes with a ring of three planes of the
+// float4 source in shared memory, each on the tile plus a one-node ring
+// (34 x 10), split into its four components so that a node reads the 49
+// scalars it needs (lambda_lap at 19 points, each gradient component at the
+// 10 points with c_k != 0) without bank conflicts.
+constexpr int SW = TXA + 2, SH = TYA + 2, SPLANE = SW * SH;
+
 __global__ void __launch_bounds__(NTA) adjoint_stencil_kernel(Box b, const float4 *__restrict__ lsrc,
                                                               float *__restrict__ lst)
 {
-    const int x = blockIdx.x * TXA + threadIdx.x, y = blockIdx.y * TYA + threadIdx.y;
-    for (int z = blockIdx.z; z < b.nz; z += gridDim.z) {
-        const Nb p = neighbourhood(b, x, y, z);
+    __shared__ float sm[3][4][SPLANE];
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TXA + tx;
+    const int x0 = blockIdx.x * TXA, y0 = blockIdx.y * TYA;
+    const int z_begin = blockIdx.z * kPlanes, z_end = min(b.nz, z_begin + kPlanes);
+    const unsigned nx = (unsigned)b.nx;
+    auto load = [&](int z, int slot) {
+        const int zw = z < 0 ? z + b.nz : (z >= b.nz ? z - b.nz : z);
+        const unsigned zo = (unsigned)zw * (unsigned)b.nxy;
+        for (int e = tid; e < SPLANE; e += NTA) {
+            const int r = e / SW, c = e - r * SW;
+            int gx = x0 - 1 + c, gy = y0 - 1 + r;
+            gx = gx < 0 ? gx + b.nx : (gx >= b.nx ? gx - b.nx : gx);
+            gy = gy < 0 ? gy + b.ny : (gy >= b.ny ? gy - b.ny : gy);
+            const float4 v = __ldg(lsrc + zo + (unsigned)gy * nx + (unsigned)gx);
+            sm[slot][0][e] = v.x;
+            sm[slot][1][e] = v.y;
+            sm[slot][2][e] = v.z;
+            sm[slot][3][e] = v.w;
+        }
+    };
+    load(z_begin - 1, (z_begin + 2) % 3);
+    load(z_begin, z_begin % 3);
+    const int cell = (ty + 1) * SW + tx + 1;
+    for (int z = z_begin; z < z_end; z++) {
+        load(z + 1, (z + 1) % 3);
+        __syncthreads();
         float lface = 0.f, ledge = 0.f, dface = 0.f, dedge = 0.f;
-        const float4 c0 = __ldg(lsrc + p.at(0, 0, 0));
 #pragma unroll
         for (int i = 1; i < kQg; i++) {
-            const float4 s = __ldg(lsrc + dir_at(p, i, 1));
+            const int slot = (z + kCz(i) + 3) % 3;
+            const int at = cell + kCy(i) * SW + kCx(i);
+            const float lx = sm[slot][0][at];
             float d = 0.f;
-            if (kCx(i)) d += kCx(i) * s.y;
-            if (kCy(i)) d += kCy(i) * s.z;
-            if (kCz(i)) d += kCz(i) * s.w;
+            if (kCx(i)) d += kCx(i) * sm[slot][1][at];
+            if (kCy(i)) d += kCy(i) * sm[slot][2][at];
+            if (kCz(i)) d += kCz(i) * sm[slot][3][at];
             if (i < 7) {
-                lface += s.x;
+                lface += lx;
                 dface += d;
             } else {
-                ledge += s.x;
+                ledge += lx;
                 dedge += d;
             }
         }
-        const float L = (ledge + 2.f * (lface - 12.f * c0.x)) * kInv6;
+        const float c0 = sm[z % 3][0][cell];
+        const float L = (ledge + 2.f * (lface - 12.f * c0)) * kInv6;
         const float D = (2.f * dface + dedge) * kInv12;
-        lst[p.at(0, 0, 0)] = L - D;
+        lst[(unsigned)z * (unsigned)b.nxy + (unsigned)(y0 + ty) * nx + (unsigned)(x0 + tx)] = L - D;
+        __syncthreads();
     }
 }
 
@@ -484,7 +529,7 @@ __global__ void __launch_bounds__(NTA) init_adjoint_kernel(Box b, float alpha4, 
 {
     const unsigned n = (unsigned)b.n;
     const int x = blockIdx.x * TXA + threadIdx.x, y = blockIdx.y * TYA + threadIdx.y;
-    for (int z = blockIdx.z; z < b.nz; z += gridDim.z) {
+    for (int z = blockIdx.z * kPlanes, z_end = min(b.nz, z + kPlanes); z < z_end; z++) {
         const Nb p = neighbourhood(b, x, y, z);
         const unsigned t = p.at(0, 0, 0);
         float lap, gx, gy, gz;
@@ -511,7 +556,7 @@ __global__ void __launch_bounds__(NTA) init_adjoint_stencil_kernel(Box b, const 
                                                                    float *__restrict__ lphi0)
 {
     const int x = blockIdx.x * TXA + threadIdx.x, y = blockIdx.y * TYA + threadIdx.y;
-    for (int z = blockIdx.z; z < b.nz; z += gridDim.z) {
+    for (int z = blockIdx.z * kPlanes, z_end = min(b.nz, z + kPlanes); z < z_end; z++) {
         const Nb p = neighbourhood(b, x, y, z);
         float l1, d0, d1, d2;
         stencil19(llap, p, l1, d0, d1, d2);

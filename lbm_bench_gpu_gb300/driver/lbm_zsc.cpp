@@ -19,8 +19,15 @@
 // relaxation results of runlog.out are computed from those copies
 // (src/main.cu:475-476 logs before refreshing them).  Statistics are FP64 reductions on the GPU.
 //
+// With --adjoint OBJECTIVE the run is instead the gradient of a light-phase
+// objective over --adjoint-steps steps of evolution from the initial state
+// (lbm_step_adjoint; no counterpart in the reference): J, dJ/dgrav and the
+// schedule go to adjoint.out, dJ/dphi0 to adjoint_dphi0.vtk (binary).
+//
 // Usage: lbm_zsc [DIR] [--storage fp32|fp16|bf16] [--vtk ascii|binary|none]
 //                [--device N] [--no-compat]
+//                [--adjoint light_uz_mean|light_z_centroid --adjoint-steps T
+//                 --adjoint-window W --checkpoint-gb G]
 #include <chrono>
 #include <cmath>
 #include <cstdint>
@@ -44,6 +51,10 @@ struct Options {
     int vtk = 1;   // 0 none, 1 ASCII (the reference's format), 2 binary legacy VTK
     int device = 0;
     int compat = 1;
+    int adjoint = -1;          // LBM_OBJ_*, -1: the reference's run
+    int adjoint_steps = 1000;
+    int adjoint_window = 1;
+    double checkpoint_gb = 0.0;   // <= 0: half of the free device memory
 };
 
 [[noreturn]] void fatal(const std::string &what, int code)
@@ -60,9 +71,13 @@ void check(int code, const char *what)
 void usage(const char *argv0)
 {
     std::printf("usage: %s [DIR] [--storage fp32|fp16|bf16] [--vtk ascii|binary|none] [--device N] [--no-compat]\n"
+                "       [--adjoint light_uz_mean|light_z_centroid [--adjoint-steps T] [--adjoint-window W]\n"
+                "        [--checkpoint-gb G]]\n"
                 "Runs the ZSC multiphase LBM described by DIR/properties.in and DIR/discrete.in\n"
                 "(default DIR: the current directory) and writes runlog.out, relax_stats.out,\n"
-                "stats.out and the VTK snapshots into DIR.\n",
+                "stats.out and the VTK snapshots into DIR.  With --adjoint it computes the\n"
+                "gradient of the objective over T evolution steps from the initial state\n"
+                "instead (adjoint.out, adjoint_dphi0.vtk).\n",
                 argv0);
 }
 
@@ -99,6 +114,19 @@ Options parse(int argc, char **argv)
             o.device = std::atoi(value().c_str());
         } else if (a == "--no-compat") {
             o.compat = 0;
+        } else if (a == "--adjoint") {
+            const std::string v = value();
+            o.adjoint = v == "light_uz_mean" ? LBM_OBJ_LIGHT_UZ_MEAN : v == "light_z_centroid" ? LBM_OBJ_LIGHT_Z_CENTROID : -2;
+            if (o.adjoint < -1) {
+                std::fprintf(stderr, "ERROR: unknown objective '%s'.\n", v.c_str());
+                std::exit(2);
+            }
+        } else if (a == "--adjoint-steps") {
+            o.adjoint_steps = std::atoi(value().c_str());
+        } else if (a == "--adjoint-window") {
+            o.adjoint_window = std::atoi(value().c_str());
+        } else if (a == "--checkpoint-gb") {
+            o.checkpoint_gb = std::atof(value().c_str());
         } else if (!a.empty() && a[0] == '-') {
             std::fprintf(stderr, "ERROR: unknown option '%s'.\n", a.c_str());
             usage(argv[0]);
@@ -136,6 +164,7 @@ public:
         banner();
         check(lbm_init_bubbles(&c_, &p_, bubbles_.data(), nbubbles_), "lbm_init_bubbles");
         check(lbm_derive(&p_, &d_), "lbm_derive");
+        if (o_.adjoint >= 0) return adjoint();
         host_ = new Host((size_t)p_.nx * p_.ny * p_.nz);
         lbm_stats_out s = copy_fields(true);
 
@@ -199,6 +228,48 @@ private:
     static double ms(Clock::time_point a, Clock::time_point b)
     {
         return std::chrono::duration<double, std::milli>(b - a).count();
+    }
+
+    // the gradient run (no counterpart in the reference)
+    int adjoint()
+    {
+        const size_t n = (size_t)p_.nx * p_.ny * p_.nz;
+        std::vector<float> grad(n);
+        lbm_adjoint_opts o{};
+        o.objective = o_.adjoint;
+        o.nsteps = o_.adjoint_steps;
+        o.window = o_.adjoint_window;
+        o.grav = d_.grav;
+        o.checkpoint_bytes = o_.checkpoint_gb * 1e9;
+        lbm_adjoint_out r{};
+        r.dJ_dphi0 = grad.data();
+        check(lbm_step_adjoint(c_, &o, &r), "lbm_step_adjoint");
+        FILE *fp = open("adjoint.out", "w");
+        std::fprintf(fp, "objective          = %s\n", o.objective == LBM_OBJ_LIGHT_UZ_MEAN ? "light_uz_mean" : "light_z_centroid");
+        std::fprintf(fp, "steps              = %d\n", o.nsteps);
+        std::fprintf(fp, "window             = %d\n", o.window);
+        std::fprintf(fp, "grav               = %e\n", (double)o.grav);
+        std::fprintf(fp, "J                  = %.17e\n", r.J);
+        std::fprintf(fp, "dJ/dgrav           = %.17e\n", r.dJ_dgrav);
+        std::fprintf(fp, "checkpoint slots   = %d\n", r.slots);
+        std::fprintf(fp, "checkpoint GB      = %.3f\n", r.checkpoint_bytes_used / 1e9);
+        std::fprintf(fp, "forward steps      = %lld\n", r.forward_steps);
+        std::fprintf(fp, "adjoint steps      = %lld\n", r.adjoint_steps);
+        std::fprintf(fp, "seconds            = %.6f\n", r.seconds);
+        std::fclose(fp);
+        std::printf("J = %.10e  dJ/dgrav = %.10e  (%d slots, %lld forward steps, %.3f s)\n", r.J, r.dJ_dgrav, r.slots,
+                    r.forward_steps, r.seconds);
+        fp = open("adjoint_dphi0.vtk", "wb");
+        std::fprintf(fp, "# vtk DataFile Version 2.0\n");
+        std::fprintf(fp, "dJ/dphi0 (liblbm_gb300 adjoint)\nBINARY\n\nDATASET STRUCTURED_POINTS\n");
+        std::fprintf(fp, "DIMENSIONS %d %d %d\nORIGIN 1 1 1\nSPACING 1 1 1\n\nPOINT_DATA %lld\n\n", p_.nx, p_.ny, p_.nz,
+                     (long long)n);
+        std::fprintf(fp, "SCALARS dJ_dphi0 float\nLOOKUP_TABLE default\n");
+        put_be(fp, grad.data(), n);
+        std::fprintf(fp, "\n");
+        std::fclose(fp);
+        lbm_destroy(c_);
+        return 0;
     }
 
     void read_inputs()

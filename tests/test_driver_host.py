@@ -38,3 +38,8 @@ def test_malformed_inputs(driver, tmp_path):
     (tmp_path / "discrete.in").write_text("nBubbles\n0\n\nxc yc zc Rc\n")
     r = subprocess.run([str(driver), str(tmp_path)], capture_output=True, text=True, timeout=60)
     assert r.returncode == 1 and "ERROR" in r.stderr
+
+
+def test_bad_objective(driver):
+    r = subprocess.run([str(driver), "--adjoint", "drag"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 2 and "unknown objective" in r.stderr

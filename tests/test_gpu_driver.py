@@ -172,3 +172,29 @@ def test_driver_outputs_match_reference_program(lib, tmp_path):
             assert da[f].shape == db[f].shape, (name, f)
             print(f"{name} {f}: max |diff| {np.abs(db[f] - da[f]).max():.2e}")
             np.testing.assert_allclose(db[f], da[f], rtol=0, atol=6e-6, err_msg=f"{name} {f}")
+
+
+def test_driver_adjoint_mode(lib, tmp_path):
+    """lbm_zsc --adjoint gives the numbers of lbm_step_adjoint on the same
+    initial state (bit-identical: same library, same inputs)."""
+    from lbm_bench_gpu_gb300 import capi, inputs
+    inp = case()
+    inputs.write_inputs(tmp_path, inp)
+    r = subprocess.run([str(DRIVER), str(tmp_path), "--adjoint", "light_uz_mean", "--adjoint-steps", "40",
+                        "--adjoint-window", "10", "--checkpoint-gb", "0.5"], capture_output=True, text=True,
+                       timeout=600)
+    assert r.returncode == 0, r.stderr
+    got = dict(l.split("=", 1) for l in (tmp_path / "adjoint.out").read_text().splitlines())
+    got = {k.strip(): v.strip() for k, v in got.items()}
+    p = capi.make_params(inp.nx, inp.ny, inp.nz, rhoL=inp.rhoL, rhoH=inp.rhoH, tauRho=inp.tauRho,
+                         tauPhi=inp.tauPhi, width=inp.width, sigma=inp.sigma, Gamma=inp.Gamma, Eo=inp.Eo,
+                         rc0=inp.rc0, compat=True)
+    grav = float(capi.derive(p).grav)
+    with capi.Lattice.from_bubbles(p, inp.bubbles) as lat:
+        want = lat.adjoint(40, grav, "light_uz_mean", 10, checkpoint_bytes=0.5e9)
+    assert float(got["J"]) == want["J"]
+    assert float(got["dJ/dgrav"]) == want["dJ_dgrav"]
+    assert int(got["checkpoint slots"]) == want["slots"]
+    raw = (tmp_path / "adjoint_dphi0.vtk").read_bytes()
+    data = np.frombuffer(raw[raw.index(b"LOOKUP_TABLE default\n") + 21:][: 4 * inp.nx * inp.ny * inp.nz], ">f4")
+    np.testing.assert_array_equal(data.reshape(want["dJ_dphi0"].shape), want["dJ_dphi0"])
