@@ -11,7 +11,7 @@
 namespace lbm {
 
 // D3Q7 (f) and D3Q19 (g) lattice vectors in the reference order
-// (src/stream_f.cu:52-59, src/stream_g.cu:122-142).
+// (src/stream_f.cu:52-59, src/stream_g.cu:56-76).
 // f: 0 rest, 1 +x, 2 -x, 3 +y, 4 -y, 5 +z, 6 -z
 // g: 0 rest, 1..6 as f, 7 (+x+y), 8 (-x-y), 9 (+x-y), 10 (-x+y), 11 (+x+z),
 //    12 (-x-z), 13 (+x-z), 14 (-x+z), 15 (+y+z), 16 (-y-z), 17 (+y-z), 18 (-y+z)

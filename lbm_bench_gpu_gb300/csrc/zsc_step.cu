@@ -426,7 +426,7 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Quan
             put(5, a * fcur[6] + Af - Cf * usz);
         }
 
-        // D3Q19 collision with forcing, src/collision_g.cu:232-313
+        // D3Q19 collision with forcing, src/collision_g.cu:111-196
         {
             const float bb = c.invTauRhoOne;
             const float K1 = c.K1, K2 = c.K2, KC1 = c.KC1, KC2 = c.KC2;

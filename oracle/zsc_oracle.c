@@ -390,7 +390,7 @@ static const int CG[19][3] = {{0, 0, 0},  {1, 0, 0},  {-1, 0, 0}, {0, 1, 0},  {0
 
 /* stream_f (src/stream_f.cu:52-59): ZSC eta-interpolated push,
  * f_i(x + c_i) = eta * P_i(x) + (1 - eta) * P_i(x + c_i), f_0(x) = P_0(x).
- * stream_g (src/stream_g.cu:122-142): g_i(x + c_i) = P_i(x).
+ * stream_g (src/stream_g.cu:56-76): g_i(x + c_i) = P_i(x).
  * Periodic wrap replaces the ghost exchanges (src/pack_mpi_f.cu, src/pack_mpi.cu
  * and their unpack twins with one rank). */
 static void zo_stream(zo_ctx *s)
