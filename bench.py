@@ -56,6 +56,9 @@ def parse_args(argv=None):
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint / forward time ratio")
     ap.add_argument("--no-ref-cuda", action="store_true", help="skip timing the reference's own CUDA build")
     ap.add_argument("--ref-cuda-steps", type=int, default=500)
+    ap.add_argument("--precision", action="store_true",
+                    help="also run the storage-precision study at 256^3 and 512^3 (10k steps per format)")
+    ap.add_argument("--precision-steps", type=int, default=10000)
     ap.add_argument("--adjoint-long", action="store_true",
                     help="also run the long-horizon adjoint (256^3, 64 bubbles, T = 20000, FP16 state, 40 GB)")
     return ap.parse_args(argv)
@@ -300,7 +303,69 @@ def run_ours(args, rank, world, local):
         result["cpu_baseline"] = cpu_baseline(inp)
     if rank == 0 and world == 1 and not args.no_ref_cuda:
         result["reference_cuda"] = run_reference_cuda(inp, args.ref_cuda_steps, local, value)
+    if rank == 0 and args.precision:
+        result["precision_large"] = run_precision(local, args.precision_steps)
     return result
+
+
+def heavy_centroids(phi):
+    """Centroids (z, y, x) of the connected phi > 0 regions."""
+    from scipy import ndimage
+    lab, n = ndimage.label(phi > 0)
+    if n == 0:
+        return np.zeros((0, 3))
+    return np.array(ndimage.center_of_mass(phi > 0, lab, range(1, n + 1)))
+
+
+def run_precision(local, steps):
+    """Storage precision at the benchmark's sizes: 256^3 with 64 bubbles R~U[6,10]
+    and 512^3 with 512 bubbles R~U[6,12] (gap >= 3, seeded), gravity -1e-6,
+    `steps` steps in FP32, FP16 and BF16 storage.  The errors are taken against the
+    FP32-storage GPU run: the FP64 oracle would need ~48 minutes of the host per
+    10k steps at 256^3, and at 64^3 FP32 storage stays within 1.1e-4 (phi L2) of
+    it after 10k steps (tests/test_precision_study.py).  Per format: MLUPS over
+    the run (CUDA events), phi L2 relative error, the drift of sum(phi) and
+    sum(rho) from their initial values, and the largest distance from a FP32
+    heavy-phase centroid to the nearest one of the format."""
+    import torch
+    from lbm_bench_gpu_gb300 import capi
+    out = {"steps": steps, "reference": "FP32-storage GPU run"}
+    for size, nb in ((256, 64), (512, 512)):
+        inp = workload(size, nb)
+        nodes = inp.nx * inp.ny * inp.nz
+        res, phis = {}, {}
+        for st in ("fp32", "fp16", "bf16"):
+            p = params_for(inp, st, local)
+            grav = float(capi.derive(p).grav)
+            with capi.Lattice.from_bubbles(p, inp.bubbles) as lat:
+                s0, _ = lat.stats()
+                stream = torch.cuda.ExternalStream(lat.stream, device=local)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                lat.step(steps, grav)
+                e1.record(stream)
+                e1.synchronize()
+                ms = e0.elapsed_time(e1)
+                s, f = lat.stats(fields=True)
+            phis[st] = f["phi"]
+            res[st] = {"mlups": round(nodes * steps / (ms / 1e3) / 1e6, 1),
+                       "phi_sum_drift": (s["phi_sum"] - s0["phi_sum"]) / abs(s0["phi_sum"]),
+                       "rho_sum_drift": (s["rho_sum"] - s0["rho_sum"]) / abs(s0["rho_sum"]),
+                       "nonfinite": s["nonfinite"]}
+        ref = phis["fp32"].astype(np.float64)
+        cref = heavy_centroids(phis["fp32"])
+        for st in ("fp16", "bf16"):
+            d = phis[st].astype(np.float64) - ref
+            res[st]["phi_l2_rel_vs_fp32"] = float(np.linalg.norm(d) / np.linalg.norm(ref))
+            c = heavy_centroids(phis[st])
+            res[st]["bubbles"] = [int(len(cref)), int(len(c))]
+            if len(c) and len(cref):
+                dist = np.sqrt(((cref[:, None, :] - c[None, :, :]) ** 2).sum(-1)).min(1)
+                res[st]["centroid_err_max"] = float(dist.max())
+            res[st]["speedup_vs_fp32"] = round(res[st]["mlups"] / res["fp32"]["mlups"], 3)
+        out[f"{size}^3"] = res
+        del phis
+    return out
 
 
 REF_STATS_KEYS = ("ux", "uy", "uz", "Umax", "Vef", "Ref")
@@ -376,12 +441,14 @@ def run_adjoint(local, long_horizon=False):
     long:  256^3, 64 bubbles R ~ U[6, 10], T = 20000, J = final light-phase
            z-centroid, FP16 live state (native FP16 snapshots).
     Both with a 40 GB checkpoint budget; the short one is repeated with the
-    library's default budget (half of the free device memory).  The forward time is lbm_step over T
-    steps on the same context.  dJ/dgrav is checked against central
-    differences of J from lbm_objective (the GPU forward run) with steps
-    h = 1e-6, 5e-7 and 2.5e-7 on the force, and their Richardson extrapolation;
-    on the short run dJ/dphi0 is checked the same way (h = 1e-4) on 16 seeded
-    random nodes among those with |dJ/dphi0| above 10% of its maximum."""
+    library's default budget (half of the free device memory).  The forward
+    time is lbm_step over T steps on the same context.  dJ/dgrav is compared
+    with central differences of J from lbm_objective (the GPU forward run) at
+    h = 1e-6, 5e-7, 2.5e-7 on the force (down to 6.25e-8 on the long run, whose
+    J is far from linear over |h| ~ |g|); fd_rel_err uses the smallest h and
+    fd_richardson extrapolates the two smallest.  These FP32 differences carry
+    the trajectory's rounding noise (~7e-4 of J on the short run); the 1e-4
+    check against FP64 differences is tests/test_gpu_adjoint_fd64.py."""
     import torch
     from lbm_bench_gpu_gb300 import capi, inputs
     if long_horizon:
@@ -416,10 +483,11 @@ def run_adjoint(local, long_horizon=False):
             # the same run with the library's default budget (half of the free device memory)
             r_free = lat.adjoint(T, grav, objective, window, want_phi0=False)
         fd = {}
-        for h in (1e-6, 5e-7, 2.5e-7):
+        hs = (1e-6, 5e-7, 2.5e-7) if not long_horizon else (1e-6, 5e-7, 2.5e-7, 1.25e-7, 6.25e-8)
+        for h in hs:
             fd[h] = (lat.objective(T, grav + h, objective, window)
                      - lat.objective(T, grav - h, objective, window)) / (2 * h)
-    rich = (4 * fd[5e-7] - fd[1e-6]) / 3
+    rich = (4 * fd[hs[-1]] - fd[hs[-2]]) / 3
     out = {"workload": ("long: 256^3, 64 bubbles, T=20000, final light-phase z-centroid, FP16 state"
                         if long_horizon else
                         "short: 128^3, 8 bubbles R=10, tau_rho=0.8, T=2000, light-phase mean u_z over the "
@@ -429,7 +497,7 @@ def run_adjoint(local, long_horizon=False):
            "checkpoint_GB": round(r["checkpoint_bytes_used"] / 1e9, 2), "forward_steps": r["forward_steps"],
            "J": r["J"], "dJ_dgrav": r["dJ_dgrav"],
            "fd_dJ_dgrav": {f"{h:g}": v for h, v in fd.items()}, "fd_richardson": rich,
-           "fd_rel_err": abs(r["dJ_dgrav"] - fd[1e-6]) / abs(fd[1e-6]),
+           "fd_rel_err": abs(r["dJ_dgrav"] - fd[hs[-1]]) / abs(fd[hs[-1]]),
            "fd_rel_err_richardson": abs(r["dJ_dgrav"] - rich) / abs(rich),
            "dJ_dphi0_norm": float(np.sqrt((r["dJ_dphi0"].astype(np.float64) ** 2).sum()))}
     if r_free is not None:
@@ -438,24 +506,6 @@ def run_adjoint(local, long_horizon=False):
                                  "checkpoint_GB": round(r_free["checkpoint_bytes_used"] / 1e9, 2),
                                  "forward_steps": r_free["forward_steps"],
                                  "same_gradient": r_free["dJ_dgrav"] == r["dJ_dgrav"]}
-    if not long_horizon:
-        g0 = r["dJ_dphi0"]
-        big = np.flatnonzero(np.abs(g0) > 0.1 * np.abs(g0).max())
-        nodes = np.random.default_rng(20261203).choice(big, size=min(16, len(big)), replace=False)
-        h = 1e-4
-        errs = []
-        for k in nodes:
-            vals = []
-            for sgn in (1, -1):
-                ph = phi0.copy()
-                ph.flat[k] += sgn * h
-                with capi.Lattice.from_fields(p, ph, rho0) as lat:
-                    vals.append(lat.objective(T, grav, objective, window))
-            fdk = (vals[0] - vals[1]) / (2 * h)
-            errs.append(abs(float(g0.flat[k]) - fdk) / max(abs(fdk), 1e-300))
-        out["phi0_fd_nodes"] = len(nodes)
-        out["phi0_fd_rel_err_max"] = float(max(errs))
-        out["phi0_fd_rel_err_median"] = float(np.median(errs))
     return out
 
 

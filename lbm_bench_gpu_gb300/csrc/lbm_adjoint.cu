@@ -45,8 +45,10 @@ struct Adjoint {
     lbm_ctx *c;
     lbm_adjoint_opts o;
     size_t n, snap_bytes;
-    // work buffers
-    float *phi = nullptr;
+    // work buffers; phi and the objective sums ab (4 doubles) are
+    // double-buffered by step parity so that the side stream can prepare
+    // step n while the main stream still runs step n + 1
+    float *phi = nullptr;     // 2 x n
     float *lam[2] = {nullptr, nullptr};   // 26 x n each: f (7) then g (19)
     float *lst[2] = {nullptr, nullptr};
     float4 *lsrc = nullptr;
@@ -61,6 +63,41 @@ struct Adjoint {
     lbm::StepConst k;
     int first_source;            // first state index with an objective term
     double scale;
+    // Side stream: phi and the objective of state n depend only on that
+    // state, so they run there as soon as it exists, overlapping the main
+    // stream's adjoint kernels of step n + 1.  Events order the two streams:
+    // slot_ev[s] / ctx_ev mark a state written, buf_free[b] the main stream's
+    // last read of phi / ab buffer b, side_done the side work of a step.
+    cudaStream_t side = nullptr;
+    std::vector<cudaEvent_t> slot_ev;
+    cudaEvent_t ctx_ev = nullptr, side_done = nullptr, buf_free[2] = {nullptr, nullptr};
+
+    float *phi_buf(long long step) { return phi + (size_t)(step & 1) * n; }
+    double *ab_buf(long long step) { return ab + 4 * (step & 1); }
+
+    int record(cudaEvent_t ev, cudaStream_t st)
+    {
+        if (!ev) return LBM_OK;
+        cudaError_t e = cudaEventRecord(ev, st);
+        return e == cudaSuccess ? LBM_OK : cuda_fail(e, "adjoint: event");
+    }
+
+    int create_streams(int nslots)
+    {
+        cudaError_t e = cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking);
+        auto ev = [&](cudaEvent_t *p) {
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(p, cudaEventDisableTiming);
+        };
+        ev(&ctx_ev);
+        ev(&side_done);
+        ev(&buf_free[0]);
+        ev(&buf_free[1]);
+        slot_ev.assign((size_t)nslots, nullptr);
+        for (auto &x : slot_ev) ev(&x);
+        if (e == cudaSuccess) e = cudaEventRecord(buf_free[0], c->stream);
+        if (e == cudaSuccess) e = cudaEventRecord(buf_free[1], c->stream);
+        return e == cudaSuccess ? LBM_OK : cuda_fail(e, "adjoint: streams");
+    }
 
     unsigned char *slot_ptr(int s) { return slots + (size_t)s * snap_bytes; }
 
@@ -92,7 +129,7 @@ struct Adjoint {
         snaps[s].step = step;
         snaps[s].f_streamed = c->st.f_streamed;
         snaps[s].g_odd_next = c->st.g_odd_next;
-        return LBM_OK;
+        return slot_ev.empty() ? LBM_OK : record(slot_ev[s], c->stream);
     }
 
     int restore(int s)
@@ -142,6 +179,7 @@ struct Adjoint {
             snaps[to].step = step + 1;
             snaps[to].f_streamed = false;
             snaps[to].g_odd_next = !src.g_odd;
+            if (!slot_ev.empty()) return record(slot_ev[to], c->stream);
         } else {
             c->st.f_cur = 0;
             c->st.f_streamed = false;
@@ -155,7 +193,8 @@ struct Adjoint {
     int advance(int si, long long s, long long j)
     {
         int rc = step_out_of_place(slot_state(si), s, -1);
-        return rc ? rc : forward(j - s - 1);
+        if (!rc) rc = forward(j - s - 1);
+        return rc ? rc : record(ctx_ev, c->stream);
     }
 
     // slot sj holds s^m, from s^s in slot si (m > s)
@@ -166,49 +205,65 @@ struct Adjoint {
         return rc ? rc : step_out_of_place(ctx_state(), m - 1, sj);
     }
 
-    // phi of state st
-    int prepare(const lbm::NativeState &st)
+    // phi of state st into buffer `out`, on stream `sm`
+    int prepare(const lbm::NativeState &st, float *out, cudaStream_t sm)
     {
-        cudaError_t e = lbm::launch_adjoint_phi(c->box, c->d.eta, c->q, st, phi, c->stream);
+        cudaError_t e = lbm::launch_adjoint_phi(c->box, c->d.eta, c->q, st, out, sm);
         return e == cudaSuccess ? LBM_OK : cuda_fail(e, "adjoint: phi");
     }
 
     bool has_source(long long step) const { return step >= first_source; }
 
-    // lambda^T from the final state (the context holds s^T)
+    // lambda^T from the final state (the context holds s^T), on the main
+    // stream; the side stream starts after it
     int terminal()
     {
         const lbm::NativeState st = ctx_state();
-        int rc = prepare(st);
+        float *ph = phi_buf(o.nsteps);
+        double *abT = ab_buf(o.nsteps);
+        int rc = prepare(st, ph, c->stream);
         if (rc) return rc;
         cudaError_t e = cudaSuccess;
         if (has_source(o.nsteps)) {
-            e = lbm::launch_objective(c->box, o.objective, c->d.phiStar, scale, c->q, st, phi, partials, ab, acc,
+            e = lbm::launch_objective(c->box, o.objective, c->d.phiStar, scale, c->q, st, ph, partials, abT, acc,
                                       c->stream);
             if (e == cudaSuccess)
-                e = lbm::launch_source_init(c->box, o.objective, scale, ab, c->d.phiStar, c->q, st, phi, lam[cur],
+                e = lbm::launch_source_init(c->box, o.objective, scale, abT, c->d.phiStar, c->q, st, ph, lam[cur],
                                             lam[cur] + lbm::kQf * n, lst[cur], c->stream);
         } else {
             e = cudaMemsetAsync(lam[cur], 0, sizeof(float) * (lbm::kQf + lbm::kQg) * n, c->stream);
             if (e == cudaSuccess) e = cudaMemsetAsync(lst[cur], 0, sizeof(float) * n, c->stream);
         }
         if (e != cudaSuccess) return cuda_fail(e, "adjoint: terminal source");
+        if (side) {
+            if ((rc = record(buf_free[o.nsteps & 1], c->stream))) return rc;
+            e = cudaStreamWaitEvent(side, buf_free[o.nsteps & 1], 0);
+            if (e != cudaSuccess) return cuda_fail(e, "adjoint: stream order");
+        }
         lambda_ready = true;
         return LBM_OK;
     }
 
-    // lambda^step from lambda^{step+1}; st is s^step
-    int adjoint_step(long long step, const lbm::NativeState &st)
+    // lambda^step from lambda^{step+1}; st is s^step, written when `ready` fires
+    int adjoint_step(long long step, const lbm::NativeState &st, cudaEvent_t ready)
     {
-        int rc = prepare(st);
-        if (rc) return rc;
         const bool src = has_source(step);
-        cudaError_t e = cudaSuccess;
+        float *ph = phi_buf(step);
+        double *abs_ = ab_buf(step);
+        const int b = (int)(step & 1);
+        cudaError_t e = cudaStreamWaitEvent(side, ready, 0);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(side, buf_free[b], 0);
+        if (e != cudaSuccess) return cuda_fail(e, "adjoint: stream order");
+        int rc = prepare(st, ph, side);
+        if (rc) return rc;
         if (src)
-            e = lbm::launch_objective(c->box, o.objective, c->d.phiStar, scale, c->q, st, phi, partials, ab, acc,
-                                      c->stream);
+            e = lbm::launch_objective(c->box, o.objective, c->d.phiStar, scale, c->q, st, ph, partials, abs_, acc,
+                                      side);
+        if (e == cudaSuccess) e = cudaEventRecord(side_done, side);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(c->stream, side_done, 0);
+        if (e != cudaSuccess) return cuda_fail(e, "adjoint: side stream");
         lbm::AdjointBuffers a;
-        a.phi = phi;
+        a.phi = ph;
         a.lf_in = lam[cur];
         a.lg_in = lam[cur] + lbm::kQf * n;
         a.lst_in = lst[cur];
@@ -217,13 +272,12 @@ struct Adjoint {
         a.lst_out = lst[1 - cur];
         a.lsrc = lsrc;
         a.dgrav = dgrav;
-        a.ab = ab;
-        if (e == cudaSuccess)
-            e = lbm::launch_adjoint_step(c->box, k, c->d.phiStar, c->q, st, a, src, o.objective, scale, c->stream);
+        a.ab = abs_;
+        e = lbm::launch_adjoint_step(c->box, k, c->d.phiStar, c->q, st, a, src, o.objective, scale, c->stream);
         if (e != cudaSuccess) return cuda_fail(e, "adjoint step");
         cur = 1 - cur;
         adj_steps++;
-        return LBM_OK;
+        return record(buf_free[b], c->stream);
     }
 
     // adjoint of step s (the segment [s, s + 1)); slot si holds s^s
@@ -233,7 +287,7 @@ struct Adjoint {
         if (!lambda_ready) {   // s + 1 == T: build lambda^T first
             if ((rc = advance(si, s, s + 1)) || (rc = terminal())) return rc;
         }
-        return adjoint_step(s, slot_state(si));
+        return adjoint_step(s, slot_state(si), slot_ev[si]);
     }
 
     int take_slot()
@@ -257,8 +311,8 @@ struct Adjoint {
                     if ((rc = advance(si, s, o.nsteps)) || (rc = terminal())) return rc;
                 }
                 if (j == s) {
-                    if ((rc = adjoint_step(j, slot_state(si)))) return rc;
-                } else if ((rc = advance(si, s, j)) || (rc = adjoint_step(j, ctx_state()))) {
+                    if ((rc = adjoint_step(j, slot_state(si), slot_ev[si]))) return rc;
+                } else if ((rc = advance(si, s, j)) || (rc = adjoint_step(j, ctx_state(), ctx_ev))) {
                     return rc;
                 }
             }
@@ -279,6 +333,14 @@ struct Adjoint {
     void release()
     {
         cudaStreamSynchronize(c->stream);
+        if (side) {
+            cudaStreamSynchronize(side);
+            cudaStreamDestroy(side);
+        }
+        for (cudaEvent_t x : slot_ev)
+            if (x) cudaEventDestroy(x);
+        for (cudaEvent_t x : {ctx_ev, side_done, buf_free[0], buf_free[1]})
+            if (x) cudaEventDestroy(x);
         void *p[] = {phi, lam[0], lam[1], lst[0], lst[1], lsrc, phi0, mom_save, partials, dgrav, ab, acc, slots};
         for (void *q : p) cudaFree(q);
     }
@@ -344,7 +406,7 @@ extern "C" int lbm_objective(lbm_ctx *c, const lbm_adjoint_opts *o, double *J)
     if (!rc) rc = A.forward(A.first_source);
     for (long long k = A.first_source; !rc && k <= o->nsteps; k++) {
         const lbm::NativeState st = A.ctx_state();
-        rc = A.prepare(st);
+        rc = A.prepare(st, A.phi, c->stream);
         if (!rc) {
             e = lbm::launch_objective(c->box, o->objective, c->d.phiStar, A.scale, c->q, st, A.phi, A.partials, A.ab,
                                       A.acc, c->stream);
@@ -381,7 +443,7 @@ extern "C" int lbm_step_adjoint(lbm_ctx *c, const lbm_adjoint_opts *o, lbm_adjoi
     auto alloc = [&](void **p, size_t bytes) {
         if (e == cudaSuccess) e = cudaMalloc(p, bytes);
     };
-    alloc((void **)&A.phi, sizeof(float) * n);
+    alloc((void **)&A.phi, sizeof(float) * 2 * n);
     alloc((void **)&A.lam[0], sizeof(float) * (lbm::kQf + lbm::kQg) * n);
     alloc((void **)&A.lam[1], sizeof(float) * (lbm::kQf + lbm::kQg) * n);
     alloc((void **)&A.lst[0], sizeof(float) * n);
@@ -391,7 +453,7 @@ extern "C" int lbm_step_adjoint(lbm_ctx *c, const lbm_adjoint_opts *o, lbm_adjoi
     alloc((void **)&A.mom_save, sizeof(float) * 5 * n);
     alloc((void **)&A.partials, sizeof(double) * 2 * nblocks);
     alloc((void **)&A.dgrav, sizeof(double) * nblocks);
-    alloc((void **)&A.ab, sizeof(double) * 4);
+    alloc((void **)&A.ab, sizeof(double) * 8);
     alloc((void **)&A.acc, sizeof(double) * 2);
     if (e != cudaSuccess) {
         A.release();
@@ -426,6 +488,7 @@ extern "C" int lbm_step_adjoint(lbm_ctx *c, const lbm_adjoint_opts *o, lbm_adjoi
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(A.mom_save, c->st.mom, sizeof(float) * 5 * n, cudaMemcpyDeviceToDevice, c->stream);
     if (e != cudaSuccess) rc = cuda_fail(e, "lbm_step_adjoint: setup");
+    if (!rc) rc = A.create_streams((int)nslots);
     if (!rc) rc = A.save(0, 0);
     if (!rc) rc = A.revolve(0, o->nsteps, 0, (int)(nslots - 1));
     // lambda^0 -> dJ/dphi0 through the initial equilibrium (output in the
