@@ -1,9 +1,12 @@
 // zsc_stats.cu -- statistics of the phi, rho, u arrays in FP64.
 //
 // Replaces the host loops of src/stats.c:39-58 and the pressure part of
-// src/logsave.c:63-150.  One pass over the five arrays: per-thread FP64
-// accumulators, warp-shuffle reductions per block into a partials array, then
-// one block folds the partials in a fixed order (deterministic for a given box).
+// src/logsave.c:63-150.  One pass over the five arrays: per-thread
+// compensated float sums (a float pair hi + lo updated with Knuth's two-sum,
+// products split exactly with an FMA), which hold ~48 bits like an FP64 sum
+// at FP32 throughput (GB300's FP64 rate is a small fraction of its FP32 rate);
+// FP64 warp-shuffle reductions per block into a partials array, then one block
+// folds the partials in a fixed order (deterministic for a given box).
 //
 // Partial / result layout (doubles):
 //   0 max |u|^2 (compat)    1 #phi>=0 (compat)   2..4 sum u over phi>=0 (compat)
@@ -64,17 +67,39 @@ __device__ void block_reduce(double (&acc)[kStatsValues], double *out)
     }
 }
 
+// Compensated float accumulator: the sum is hi + lo.  The _rn intrinsics keep
+// the compiler from contracting the two-sum's operations into FMAs, which
+// would break the exact error terms.
+struct Sum2 {
+    float hi = 0.f, lo = 0.f;
+    __device__ __forceinline__ void add(float x)
+    {
+        const float s = __fadd_rn(hi, x);
+        const float bp = __fsub_rn(s, hi);
+        lo = __fadd_rn(lo, __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bp)), __fsub_rn(x, bp)));
+        hi = s;
+    }
+    // a * b exactly (the product's rounding error from an FMA)
+    __device__ __forceinline__ void add_product(float a, float b)
+    {
+        const float p = __fmul_rn(a, b);
+        add(p);
+        lo = __fadd_rn(lo, fmaf(a, b, -p));
+    }
+    __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
+
 // One block works on whole x-rows (row r = y + ny z, grid-stride over rows);
-// the pressure is evaluated in float as the reference does
-// (src/logsave.c:94-137), every sum is accumulated in FP64.
+// |u|^2 and the pressure are evaluated in float as the reference does
+// (src/stats.c:45, src/logsave.c:94-137); sums are compensated, counts exact.
 __global__ void __launch_bounds__(kThreads) stats_kernel(Box b, StatsConst c, const float *__restrict__ phi,
                                                          const float *__restrict__ rho, const float *__restrict__ ux,
                                                          const float *__restrict__ uy, const float *__restrict__ uz,
                                                          double *__restrict__ partials)
 {
-    double acc[kStatsValues];
-#pragma unroll
-    for (int v = 0; v < kStatsValues; v++) acc[v] = 0.0;
+    Sum2 sum[kStatsValues];
+    unsigned cnt_in = 0, cnt_all = 0, cnt_bad = 0;
+    float umax_c = 0.f, umax_all = 0.f;
 
     const int nx = b.nx, ny = b.ny, nz = b.nz;
     const int rows = ny * nz;
@@ -92,19 +117,19 @@ __global__ void __launch_bounds__(kThreads) stats_kernel(Box b, StatsConst c, co
             const size_t t = row_c + i;
             const float ph = phi[t], rh = rho[t], vx = ux[t], vy = uy[t], vz = uz[t];
             if (!(isfinite(ph) && isfinite(rh) && isfinite(vx) && isfinite(vy) && isfinite(vz))) {
-                acc[14] += 1.0;
+                cnt_bad++;
                 continue;
             }
-            const double u2 = (double)vx * vx + (double)vy * vy + (double)vz * vz;
-            acc[7] += ph;
-            acc[8] += rh;
-            acc[9] += (double)rh * vx;
-            acc[10] += (double)rh * vy;
-            acc[11] += (double)rh * vz;
-            if (ph >= 0.f) acc[12] += 1.0;
-            acc[13] = fmax(acc[13], u2);
+            const float u2 = vx * vx + vy * vy + vz * vz;
+            sum[7].add(ph);
+            sum[8].add(rh);
+            sum[9].add_product(rh, vx);
+            sum[10].add_product(rh, vy);
+            sum[11].add_product(rh, vz);
+            if (ph >= 0.f) cnt_all++;
+            umax_all = fmaxf(umax_all, u2);
             if (!row_in || i < 1 || i > nx - 2) continue;
-            acc[0] = fmax(acc[0], u2);
+            umax_c = fmaxf(umax_c, u2);
 
             const int ie = i == nx - 1 ? 0 : i + 1, iw = i == 0 ? nx - 1 : i - 1;
             const float p01 = phi[row_c + ie], p02 = phi[row_c + iw], p03 = phi[row_n + i], p04 = phi[row_s + i];
@@ -121,16 +146,25 @@ __global__ void __launch_bounds__(kThreads) stats_kernel(Box b, StatsConst c, co
             const float pres = c.alpha * (ph2 * (3.f * ph2 - 2.f * c.phiStarSq) - c.phiStarSq * c.phiStarSq)
                                - c.kappa * (ph * lap - 0.5f * (gx * gx + gy * gy + gz * gz)) + kCsSq * rh;
             if (ph >= 0.f) {
-                acc[1] += 1.0;
-                acc[2] += vx;
-                acc[3] += vy;
-                acc[4] += vz;
-                acc[5] += pres;
+                cnt_in++;
+                sum[2].add(vx);
+                sum[3].add(vy);
+                sum[4].add(vz);
+                sum[5].add(pres);
             } else {
-                acc[6] += pres;
+                sum[6].add(pres);
             }
         }
     }
+    double acc[kStatsValues];
+#pragma unroll
+    for (int v = 0; v < kStatsValues; v++) acc[v] = sum[v].value();
+    acc[0] = umax_c;
+    acc[1] = cnt_in;
+    acc[12] = cnt_all;
+    acc[13] = umax_all;
+    acc[14] = cnt_bad;
+    acc[15] = 0.0;
     block_reduce(acc, partials + (size_t)blockIdx.x * kStatsValues);
 }
 
