@@ -46,13 +46,24 @@ int validate(const lbm_params *p)
     return LBM_OK;
 }
 
-void identity_quant(lbm::Quant &q)
+// The derived coefficients of the storage map (see lbm::Quant).
+void finish_quant(lbm::Quant &q, float eta)
+{
+    for (int a = 0; a < lbm::kQf - 1; a++) {
+        q.f_eta[a] = eta * q.f_inv[a];
+        q.f_eta2[a] = (1.f - eta) * q.f_inv[a];
+    }
+    for (int i = 0; i < lbm::kQg; i++) q.g_sshift[i] = -q.g_shift[i] * q.g_scale[i];
+}
+
+void identity_quant(lbm::Quant &q, float eta)
 {
     for (int a = 0; a < lbm::kQf - 1; a++) q.f_scale[a] = q.f_inv[a] = 1.f;
     for (int i = 0; i < lbm::kQg; i++) {
         q.g_scale[i] = q.g_inv[i] = 1.f;
         q.g_shift[i] = 0.f;
     }
+    finish_quant(q, eta);
 }
 
 // Allocate a context and its buffers; the state is left uninitialised.
@@ -71,7 +82,7 @@ int create(lbm_ctx **out, const lbm_params *p)
         c->d.gravity = 0.f;
         c->d.grav = 0.f;
     }
-    identity_quant(c->q);
+    identity_quant(c->q, c->d.eta);
     c->esz = lbm::storage_bytes(p->storage);
     c->box.nx = p->nx;
     c->box.ny = p->ny;
@@ -116,7 +127,7 @@ int reduce_stats(lbm_ctx *c)
 // c->st.mom must already hold the fields (for the mean density).
 int load_state(lbm_ctx *c, const float *tf, const float *tg)
 {
-    identity_quant(c->q);
+    identity_quant(c->q, c->d.eta);
     if (c->p.storage != LBM_STORAGE_FP32) {
         int rc = reduce_stats(c);
         if (rc) return rc;
@@ -162,6 +173,7 @@ int load_state(lbm_ctx *c, const float *tf, const float *tg)
             c->q.g_scale[i] = pick(m, 0.3 * kW[i] * std::fabs(rho_mean));
             c->q.g_inv[i] = 1.f / c->q.g_scale[i];
         }
+        finish_quant(c->q, c->d.eta);
     }
     lbm::StepView v = view(c, 0);
     LBM_CUDA(lbm::launch_quantize(c->box, c->q, c->p.storage, tf, tg, c->st.f0, const_cast<void *>(v.fq_in),

@@ -40,6 +40,9 @@ struct Box {
 struct Quant {
     float f_scale[kQf - 1], f_inv[kQf - 1];          // f_1 .. f_6
     float g_scale[kQg], g_inv[kQg], g_shift[kQg];
+    // derived, so that the step applies the map with one FMA per value:
+    float g_sshift[kQg];                             // -shift * scale (exact: scale is a power of two)
+    float f_eta[kQf - 1], f_eta2[kQf - 1];           // eta * f_inv, (1 - eta) * f_inv
 };
 
 // Device buffers of one context (element type of fq and g: the storage type,

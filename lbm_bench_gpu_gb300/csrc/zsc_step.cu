@@ -280,9 +280,20 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Quan
         const int c0 = lx + 3;          // f_0 column: x - (x0 - 4)
         const int cq = lx - 1 + E;      // f_1..f_6 column: x - (x0 - E)
         unsigned char *S1 = fstage(p);
+        auto raw = [&](unsigned char *S, int a, int rr, int cc) {
+            return Fm::load(fqpart(S)[(a * FR + rr) * W + cc]);
+        };
         auto fq = [&](unsigned char *S, int a, int rr, int cc) {
-            const float v = Fm::load(fqpart(S)[(a * FR + rr) * W + cc]);
+            const float v = raw(S, a, rr, cc);
             if constexpr (Fm::kMapped) return v * q.f_inv[a]; else return v;
+        };
+        // eta P(x - c) + (1 - eta) P(x); 16-bit storage folds the map's 1/scale
+        // into the two weights
+        auto blend = [&](unsigned char *Su, int a, int ru, int cu) {
+            if constexpr (Fm::kMapped)
+                return q.f_eta[a] * raw(Su, a, ru, cu) + q.f_eta2[a] * raw(S1, a, row, cq);
+            else
+                return c.eta * raw(Su, a, ru, cu) + c.eta2 * raw(S1, a, row, cq);
         };
         f[0] = f0part(S1)[row * W0 + c0];
         if (STREAMED) {
@@ -290,13 +301,12 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Quan
             for (int a = 0; a < kQf - 1; a++) f[a + 1] = fq(S1, a, row, cq);
         } else {
             unsigned char *S0 = fstage(p - 1), *S2 = fstage(p + 1);
-            const float eta = c.eta, eta2 = c.eta2;
-            f[1] = eta * fq(S1, 0, row, cq - 1) + eta2 * fq(S1, 0, row, cq);
-            f[2] = eta * fq(S1, 1, row, cq + 1) + eta2 * fq(S1, 1, row, cq);
-            f[3] = eta * fq(S1, 2, row - 1, cq) + eta2 * fq(S1, 2, row, cq);
-            f[4] = eta * fq(S1, 3, row + 1, cq) + eta2 * fq(S1, 3, row, cq);
-            f[5] = eta * fq(S0, 4, row, cq) + eta2 * fq(S1, 4, row, cq);
-            f[6] = eta * fq(S2, 5, row, cq) + eta2 * fq(S1, 5, row, cq);
+            f[1] = blend(S1, 0, row, cq - 1);
+            f[2] = blend(S1, 1, row, cq + 1);
+            f[3] = blend(S1, 2, row - 1, cq);
+            f[4] = blend(S1, 3, row + 1, cq);
+            f[5] = blend(S0, 4, row, cq);
+            f[6] = blend(S2, 5, row, cq);
         }
         return f[0] + f[1] + f[2] + f[3] + f[4] + f[5] + f[6];
     };
@@ -372,9 +382,13 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Quan
         const float lap = (pen + pws + pes + pwn + pet + pwb + peb + pwt + pnt + psb + pnb + pst
                            + 2.f * (pe + pw + pn + ps + pt + pb - 12.f * pc)) * kInv6;
         const float mu = c.alpha4 * pc * (pc * pc - c.phiStarSq) - c.kappa * lap;
-        const float Fx = mu * (2.f * (pe - pw) + pen - pws + pes - pwn + pet - pwb + peb - pwt) * kInv12;
-        const float Fy = mu * (2.f * (pn - ps) + pen - pws + pwn - pes + pnt - psb + pnb - pst) * kInv12;
-        float Fz = mu * (2.f * (pt - pb) + pet - pwb + pwt - peb + pnt - psb + pst - pnb) * kInv12;
+        // the edge differences each gradient component shares with another
+        const float d_en = pen - pws, d_es = pes - pwn, d_et = pet - pwb, d_eb = peb - pwt;
+        const float d_nt = pnt - psb, d_nb = pnb - pst;
+        const float mu12 = mu * kInv12;
+        const float Fx = mu12 * (2.f * (pe - pw) + d_en + d_es + d_et + d_eb);
+        const float Fy = mu12 * (2.f * (pn - ps) + d_en - d_es + d_nt + d_nb);
+        float Fz = mu12 * (2.f * (pt - pb) + d_et - d_eb + d_nt - d_nb);
         if (pc > 0.f) Fz += c.grav;
 
         // D3Q19 values of this node from the staged rows (AA pattern)
@@ -391,9 +405,12 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Quan
 #pragma unroll
         for (int i = 1; i < kQg; i++) rho += g[i];
         const float invRho = 1.0f / rho;
-        const float ux = (g[1] - g[2] + g[7] - g[8] + g[9] - g[10] + g[11] - g[12] + g[13] - g[14]) * invRho;
-        const float uy = (g[3] - g[4] + g[7] - g[8] - g[9] + g[10] + g[15] - g[16] + g[17] - g[18]) * invRho;
-        const float uz = (g[5] - g[6] + g[11] - g[12] - g[13] + g[14] + g[15] - g[16] - g[17] + g[18]) * invRho;
+        // momentum from the pair differences each component shares
+        const float d7 = g[7] - g[8], d9 = g[9] - g[10], d11 = g[11] - g[12], d13 = g[13] - g[14];
+        const float d15 = g[15] - g[16], d17 = g[17] - g[18];
+        const float ux = ((g[1] - g[2]) + d7 + d9 + d11 + d13) * invRho;
+        const float uy = ((g[3] - g[4]) + d7 - d9 + d15 + d17) * invRho;
+        const float uz = ((g[5] - g[6]) + d11 - d13 + d15 - d17) * invRho;
         const unsigned id = node_index(b, x, y, z);
         if (write_moments) {
             P.mom[0][id] = pc;
@@ -438,25 +455,26 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Quan
             float qv[kQg];
             qv[0] = bb * g[0] + c.K0 * (rho - 6.f * pc * mu - rho * vsq6) - c.KC0 * UF;
             {
-                const float K1r = K1 * rho;
-                float eq1 = temp1 + K1r * vx * vx * 0.5f + KC1 * (vx * Fx - UF);
+                const float K1r = K1 * rho, hK1r = 0.5f * K1r;
+                const float t1 = temp1 - KC1 * UF;
+                float eq1 = t1 + hK1r * vx * vx + KC1 * (vx * Fx);
                 float eq2 = vx * (K1r + KC1 * Fx);
                 qv[1] = bb * g[1] + eq1 + eq2;
                 qv[2] = bb * g[2] + eq1 - eq2;
-                eq1 = temp1 + K1r * vy * 0.5f * vy + KC1 * (vy * Fy - UF);
+                eq1 = t1 + hK1r * vy * vy + KC1 * (vy * Fy);
                 eq2 = vy * (K1r + KC1 * Fy);
                 qv[3] = bb * g[3] + eq1 + eq2;
                 qv[4] = bb * g[4] + eq1 - eq2;
-                eq1 = temp1 + K1r * vz * 0.5f * vz + KC1 * (vz * Fz - UF);
+                eq1 = t1 + hK1r * vz * vz + KC1 * (vz * Fz);
                 eq2 = vz * (K1r + KC1 * Fz);
                 qv[5] = bb * g[5] + eq1 + eq2;
                 qv[6] = bb * g[6] + eq1 - eq2;
             }
             {
-                const float K2r = K2 * rho;
-                const float temp2 = K2 * (phimu3 + rho * (1.f - vsq6));
+                const float K2r = K2 * rho, hK2r = 0.5f * K2r;
+                const float t2 = K2 * (phimu3 + rho * (1.f - vsq6)) - KC2 * UF;
                 auto pair = [&](float w, float Gf, int ip, int im) {
-                    const float eq1 = temp2 + K2r * w * 0.5f * w + KC2 * (w * Gf - UF);
+                    const float eq1 = t2 + hK2r * w * w + KC2 * (w * Gf);
                     const float eq2 = K2r * w + KC2 * Gf;
                     qv[ip] = bb * g[ip] + eq1 + eq2;
                     qv[im] = bb * g[im] + eq1 - eq2;
@@ -469,7 +487,7 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Quan
                 pair(vy - vz, Fy - Fz, 17, 18);
             }
             auto enc = [&](int i, float v) -> ST {
-                if constexpr (Fm::kMapped) return Fm::store((v - q.g_shift[i]) * q.g_scale[i]);
+                if constexpr (Fm::kMapped) return Fm::store(fmaf(v, q.g_scale[i], q.g_sshift[i]));
                 else return v;
             };
             if (!ODD) {
