@@ -62,6 +62,8 @@ def oracle_lib() -> C.CDLL:
         lib.zo_adjoint_run.restype = C.c_double
         lib.zo_objective_run.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_int, C.c_int]
         lib.zo_objective_run.restype = C.c_double
+        lib.zo_adjoint_apply.argtypes = [C.c_void_p, C.c_double, _D, _D, _D, _D, C.POINTER(C.c_double)]
+        lib.zo_adjoint_apply.restype = C.c_int
         lib.zo_heavy_mask.argtypes = [C.c_void_p, C.c_int, C.c_long]
         lib.zo_heavy_mask.restype = C.c_int
         lib.zo_init_adjoint.argtypes = [C.c_void_p, _D, _D, _D, _D, _D]
@@ -164,6 +166,18 @@ class Oracle:
 
     def objective(self, T: int, grav: float, objective: str = "light_uz_mean", window: int = 1) -> float:
         return float(self.lib.zo_objective_run(self.h, int(T), float(grav), self.OBJECTIVES[objective], int(window)))
+
+    def adjoint_apply(self, grav: float, lf, lg):
+        """J^T (lf, lg) for one step at the current streamed state, and dJ/dgrav's
+        term sum lambda_Fz H(phi > 0)."""
+        lf = np.ascontiguousarray(lf, np.float64)
+        lg = np.ascontiguousarray(lg, np.float64)
+        of = np.empty_like(lf)
+        og = np.empty_like(lg)
+        dg = C.c_double(0.0)
+        if self.lib.zo_adjoint_apply(self.h, float(grav), _dptr(lf), _dptr(lg), _dptr(of), _dptr(og), C.byref(dg)):
+            raise MemoryError("zo_adjoint_apply")
+        return of, og, dg.value
 
     def heavy_mask(self, mode: str, steps: int = 0) -> None:
         """Heavy-node log: "record" H(phi > 0) of the next `steps` collisions

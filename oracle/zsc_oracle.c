@@ -931,3 +931,34 @@ int zo_heavy_mask(zo_ctx *s, int mode, long steps)
     }
     return -1;
 }
+
+/* One adjoint step at the current streamed state s^n: (lf_out, lg_out) =
+ * J^T (lf_in, lg_in), J the derivative of the step s^n -> s^{n+1}
+ * (zo_adjoint_step, no objective source); *dgrav receives
+ * sum lambda_{F_z} H(phi > 0).  Test aid for the per-step dot-product check
+ * <J v, w> = <v, J^T w>.  Arrays: 7 x N (f) and 19 x N (g).  Returns 0, or
+ * -1 when the scratch cannot be allocated. */
+int zo_adjoint_apply(zo_ctx *s, double grav, const double *lf_in, const double *lg_in, double *lf_out,
+                     double *lg_out, double *dgrav)
+{
+    const long N = s->n;
+    double *work = (double *)calloc((size_t)5 * N, sizeof(double));
+    if (!work) return -1;
+    const double *fk[7], *gk[19], *la[26];
+    double *lb[26];
+    for (int i = 0; i < 7; i++) {
+        fk[i] = s->f[i];
+        la[i] = lf_in + (long)i * N;
+        lb[i] = lf_out + (long)i * N;
+    }
+    for (int i = 0; i < 19; i++) {
+        gk[i] = s->g[i];
+        la[7 + i] = lg_in + (long)i * N;
+        lb[7 + i] = lg_out + (long)i * N;
+    }
+    *dgrav = 0.0;
+    zo_adjoint_step(s, fk, gk, (const double *const *)la, (const double *const *)(la + 7), grav, lb, lb + 7, dgrav,
+                    work, work + N, work + 2 * N, work + 3 * N, work + 4 * N);
+    free(work);
+    return 0;
+}

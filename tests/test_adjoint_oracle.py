@@ -52,3 +52,39 @@ def test_oracle_adjoint_matches_fd(setup, objective, window):
         fd = (jp - jm) / (2 * hp)
         # FD roundoff ~1e-16 |J| / h limits the comparison at ~1e-4 relative
         assert abs(lphi[node] - fd) <= 3e-4 * abs(fd) + 1e-16 * abs(J) / hp, node
+
+
+def test_adjoint_step_dot_product(setup):
+    """One step of the FP64 adjoint is the transpose of the step's Jacobian:
+    <J v, w> = <v, J^T w> for random v, w at a moving state with gravity.
+    J v is the central difference of the FP64 step (eps = 1e-4 on v ~ 1e-3: a
+    1e-7 perturbation keeps both the truncation error, ~1e-14, and the
+    roundoff, ~1e-16 * 0.05 / 1e-7, far below the bar; the heavy set
+    H(phi > 0) of the base state is replayed, so the map is smooth); bar 1e-9
+    relative."""
+    o, phi0, rho0 = setup
+    grav = -3e-5
+    o.init(phi0, rho0)
+    o.step(5, grav)
+    f, g = o.dist()
+    rng = np.random.default_rng(11)
+    vf, vg = rng.standard_normal(f.shape) * 1e-3, rng.standard_normal(g.shape) * 1e-3
+    wf, wg = rng.standard_normal(f.shape), rng.standard_normal(g.shape)
+    eps = 1e-4
+    o.heavy_mask("record", 1)
+    o.set_dist(f, g)
+    o.step(1, grav)
+    out = []
+    for sgn in (1, -1):
+        o.heavy_mask("replay")
+        o.set_dist(f + sgn * eps * vf, g + sgn * eps * vg)
+        o.step(1, grav)
+        out.append(o.dist())
+    o.heavy_mask("off")
+    jvf = (out[0][0] - out[1][0]) / (2 * eps)
+    jvg = (out[0][1] - out[1][1]) / (2 * eps)
+    lhs = float((jvf * wf).sum() + (jvg * wg).sum())
+    o.set_dist(f, g)
+    lf, lg, _ = o.adjoint_apply(grav, wf, wg)
+    rhs = float((vf * lf).sum() + (vg * lg).sum())
+    assert rhs == pytest.approx(lhs, rel=1e-9)
