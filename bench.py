@@ -201,6 +201,19 @@ def cpu_baseline(inp, budget_s: float = 15.0):
                       f"({dt:.1f} s)"}
 
 
+def max_over_ranks(x: float, local: int = 0) -> float:
+    """The largest x over the ranks of the process group (x itself without one):
+    the job's time is its slowest replica's."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    dev = f"cuda:{local}" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], device=dev, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def time_storage(inp, storage, local, K, W, sampler=None):
     """Device time (ms) of K fused steps on resident state, CUDA events on the
     context's stream."""
@@ -229,11 +242,7 @@ def time_storage(inp, storage, local, K, W, sampler=None):
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
-    ms = e0.elapsed_time(e1)
-    if world > 1:
-        t = torch.tensor([ms], device=f"cuda:{local}", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(e0.elapsed_time(e1), local)
     s, _ = lat.stats()
     lat.close()
     if s["nonfinite"]:
