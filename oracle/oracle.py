@@ -1,11 +1,11 @@
-"""ctypes front-ends of the two CPU checkers (test infrastructure only).
+"""ctypes front-ends of the two CPU oracles (test infrastructure only).
 
 * ``Oracle``  -- the FP64 restatement in zsc_oracle.c.
 * ``RefCPU``  -- the reference's own kernels compiled for the host CPU
   (oracle/_ref/libzsc_ref.so, see oracle/build.py).
 
 Only tests, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline and
-reference legs use this module, and only as the checker or the timed CPU
+reference legs use this module, and only as the oracle or the timed CPU
 baseline -- never as the thing measured on the GPU.
 """
 from __future__ import annotations

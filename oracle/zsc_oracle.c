@@ -2,7 +2,7 @@
  * zsc_oracle.c -- FP64 CPU oracle for the Zheng-Shu-Chew (ZSC) free-energy
  * multiphase lattice Boltzmann step (D3Q7 order parameter f + D3Q19 momentum g).
  *
- * TEST INFRASTRUCTURE ONLY.  This file is the checker: the parity tests, the
+ * TEST INFRASTRUCTURE ONLY.  This file is the oracle: the parity tests, the
  * smoke check and the CPU-baseline leg of bench.py call it; the product path
  * (liblbm_gb300.so) never links or calls it.
  *

@@ -52,7 +52,9 @@ def test_read_inputs_matches_reference_parser(golden_manifest, tmp_path):
 
 def test_read_inputs_reference_sample():
     """The reference's own Input/ directory, where the checkout is present."""
-    src = Path("/root/reference/Input")
+    import os
+    from oracle.build import DEFAULT_REFERENCE_SRC
+    src = Path(os.environ.get("LBM_REFERENCE_SRC", DEFAULT_REFERENCE_SRC)).parent / "Input"
     if not (src / "properties.in").exists():
         pytest.skip("reference checkout not present")
     from lbm_bench_gpu_gb300 import capi

@@ -8,7 +8,8 @@ boxes of the benchmark take the FP64 oracle hours for 10 000 steps.
 Reported per format: phi L2 error (||phi - phi_ref||_2 / ||phi_ref||_2 and the
 RMS), relative drift of sum(phi) and sum(rho) against the oracle, and the
 largest distance between matching heavy-phase (phi > 0) centroids.  The
-report goes to gpurun_out/precision_study.json when that folder exists.
+report is also written to $LBM_REPORT_DIR/precision_study.json when that
+variable names a directory.
 Bar: relative phi L2 error <= 1e-3 for FP32 and FP16 storage.  BF16 (8-bit
 mantissa) is reported, with a looser sanity bound: its phi error after 10 000
 steps is ~2e-2 relative, driven by the rounding of f_1..f_6."""
@@ -72,8 +73,8 @@ def test_storage_precision_10k_steps(lib):
             "centroid_err_max": cerr,
             "bubbles": int(len(cg)),
         }
-    out = Path("gpurun_out")
-    if out.is_dir():
+    out = Path(os.environ.get("LBM_REPORT_DIR", ""))
+    if os.environ.get("LBM_REPORT_DIR") and out.is_dir():
         (out / "precision_study.json").write_text(json.dumps(report, indent=1))
     print(json.dumps(report))
     for storage, r in report["formats"].items():
@@ -103,8 +104,8 @@ def test_laplace_jump_by_storage(lib):
         report[storage] = {"p_dif": s["p_dif"], "p_err": s["p_err"],
                            "p_dif_rel_err": abs(s["p_dif"] - ref["p_dif"]) / abs(ref["p_dif"])}
     print(json.dumps(report))
-    out = Path("gpurun_out")
-    if out.is_dir():
+    out = Path(os.environ.get("LBM_REPORT_DIR", ""))
+    if os.environ.get("LBM_REPORT_DIR") and out.is_dir():
         (out / "laplace_by_storage.json").write_text(json.dumps(report, indent=1))
     assert report["fp32"]["p_dif_rel_err"] <= 1e-3
     assert report["fp16"]["p_dif_rel_err"] <= 1e-3
