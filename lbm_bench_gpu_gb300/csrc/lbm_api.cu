@@ -99,6 +99,8 @@ int create(lbm_ctx **out, const lbm_params *p)
     if (e == cudaSuccess) e = cudaMalloc(&c->partials, sizeof(double) * lbm::kStatsValues * c->partial_count);
     if (e == cudaSuccess) e = cudaMalloc(&c->result, sizeof(double) * lbm::kStatsValues);
     if (e == cudaSuccess) e = cudaMallocHost(&c->result_host, sizeof(double) * lbm::kStatsValues);
+    if (e == cudaSuccess) e = cudaMalloc(&c->err, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->err, 0, sizeof(int), c->stream);
     if (e != cudaSuccess) {
         lbm_destroy(c);
         return cuda_fail(e, "context allocation");
@@ -199,6 +201,15 @@ int init_from_mom(lbm_ctx *c, const float *ghost_lo, const float *ghost_hi)
     cudaFree(tmp);
     c->st.steps = 0;
     return rc;
+}
+
+// LBM_ETIMEOUT when a step kernel gave up a bounded wait (the flag stays set).
+int device_error(lbm_ctx *c)
+{
+    int flag = 0;
+    LBM_CUDA(cudaMemcpy(&flag, c->err, sizeof(int), cudaMemcpyDeviceToHost), "error flag");
+    if (flag) return fail(LBM_ETIMEOUT, "a step kernel timed out waiting for its staged data");
+    return LBM_OK;
 }
 
 // lbm_stats_out from the 16 raw stats values (the reference's formulas of
@@ -327,6 +338,7 @@ extern "C" int lbm_stats(lbm_ctx *c, lbm_stats_out *s, float *phi, float *rho, f
             LBM_CUDA(cudaMemcpyAsync(dst[a], c->st.mom + a * n, bytes, cudaMemcpyDeviceToHost, c->stream),
                      "field copy");
     LBM_CUDA(cudaStreamSynchronize(c->stream), "lbm_stats");
+    if (int rc = device_error(c)) return rc;
     if (!s) return LBM_OK;
     return fill_stats(c, c->result_host, s);
 }
@@ -457,7 +469,7 @@ extern "C" int lbm_sync(lbm_ctx *c)
 {
     if (!c) return fail(LBM_EINVAL, "context is NULL");
     LBM_CUDA(cudaStreamSynchronize(c->stream), "lbm_sync");
-    return LBM_OK;
+    return device_error(c);
 }
 
 extern "C" void lbm_destroy(lbm_ctx *c)
@@ -471,6 +483,7 @@ extern "C" void lbm_destroy(lbm_ctx *c)
     cudaFree(c->st.mom);
     cudaFree(c->partials);
     cudaFree(c->result);
+    cudaFree(c->err);
     if (c->result_host) cudaFreeHost(c->result_host);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;

@@ -74,6 +74,7 @@ struct StepView {
     void *g;                  // 19 arrays of n elements, written (and read when g_in is NULL)
     const void *g_in;         // g read by the step when it is not g (a checkpoint), else NULL
     float *mom;
+    int *err;                 // device flag a kernel sets when a bounded wait gives up
 };
 
 size_t storage_bytes(int storage);   // bytes per element of fq / g
@@ -171,6 +172,7 @@ struct lbm_ctx {
     size_t partial_count = 0;
     double *result = nullptr;      // stats result (device)
     double *result_host = nullptr; // pinned copy
+    int *err = nullptr;            // device error flag of the kernels (0 = none)
 };
 
 namespace lbm {
@@ -189,6 +191,7 @@ inline StepView state_view(lbm_ctx *c, int in)
     v.g = c->st.g;
     v.g_in = nullptr;
     v.mom = c->st.mom;
+    v.err = c->err;
     return v;
 }
 int fail(int code, const std::string &msg);

@@ -28,17 +28,27 @@
 // staged in shared memory on the tile plus two halo rows and one 16-byte
 // chunk of halo columns on each side.
 //
-// Memory pipeline: every global read goes through cp.async (16-byte chunks,
-// L2-cached, no registers held while in flight) into shared-memory stages:
+// Memory pipeline: the global reads go through asynchronous copies into
+// shared-memory stages (L2-cached, no registers held while in flight):
 //   - the 19 g rows of the next plane (2 stages; odd steps stage one extra
 //     chunk per row so the +-x shifted reads stay 16-byte aligned),
 //   - the 7 P_f planes three planes ahead (4 stages),
 // so a block always has about one plane of the step's input in flight while it
-// computes the current plane.  Warps 0-3 queue P_f, warps 4-7 queue g, each
-// thread with chunk coordinates fixed for the whole block.  Periodic wrap is
-// applied per chunk: with nx a multiple of 32 no chunk straddles the seam.
+// computes the current plane.  The P_f planes (tile + ragged halo, periodic
+// wrap) and the odd step's shifted g rows are cp.async 16-byte chunks: warps
+// 0-3 queue P_f, warps 4-7 queue g, each thread with chunk coordinates fixed
+// for the whole block; with nx a multiple of 32 no chunk straddles the seam.
+// The even step's g rows are the tile itself in all 19 fields, which one
+// thread fetches with a single TMA tensor copy per plane (a 4-d tensor map
+// x, y, z, field; box 32 x 8 x 1 x 19) completing on an mbarrier; the waits
+// on it are bounded and report a timeout through an error flag.
+#include <cuda.h>   // CUtensorMap (the encoder is fetched from the driver at run time)
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
+
+#include <cstdint>
+#include <cstring>
+#include <type_traits>
 
 #include "lattice.cuh"
 
@@ -63,6 +73,11 @@ static_assert(RING <= NT, "one ring node per thread at most");
 static_assert(TX == 32 && TY == 8, "issuer roles assume a 32 x 8 tile");
 
 constexpr float kInv6 = 0.16666666666666666667f;
+
+#ifndef ZSC_TMA_G
+#define ZSC_TMA_G 1
+#endif
+constexpr bool kUseTma = ZSC_TMA_G != 0;
 constexpr float kInv12 = 0.08333333333333333333f;
 
 template <int I>
@@ -84,10 +99,14 @@ struct Geo {
     static constexpr int G_OFF = 0;
     static constexpr int F_OFF = NG * G_STAGE;
     static constexpr int PHI_OFF = F_OFF + NF * F_STAGE;
-    static constexpr int SMEM = PHI_OFF + NPHI * PHI_STAGE;
+    static constexpr int MBAR_OFF = PHI_OFF + NPHI * PHI_STAGE;   // two mbarriers (even-step g stages)
+    static constexpr int SMEM = MBAR_OFF + 16;
+    static constexpr int G_TMA_BYTES = kQg * TY * TX * (int)sizeof(ST);   // one plane's tile, 19 fields
     static constexpr int TPD = TY * CM;              // g issuer threads per direction
     static constexpr int D = (NT / 2) / TPD;         // directions per pass of the g issuers
     static_assert(G_STAGE % 16 == 0 && F_STAGE % 16 == 0 && F0_BYTES % 16 == 0, "16-byte aligned stages");
+    static_assert(G_STAGE % 128 == 0 && G_TMA_BYTES <= G_STAGE, "TMA destinations: 128-byte aligned, inside a stage");
+    static_assert(MBAR_OFF % 8 == 0, "8-byte aligned mbarriers");
     static_assert(FR * (W0 / 4) <= NT / 2 && FR * CR <= NT / 2, "P_f issuers fit in warps 0-3");
     static_assert(D * TPD == NT / 2, "g issuers cover whole directions");
 };
@@ -101,6 +120,7 @@ struct StepPtrs {
     const ST *gin[kQg];       // g read (== g for the in-place AA update)
     ST *g[kQg];               // g written
     float *mom[5];
+    int *err;                 // set when a bounded wait gives up
 };
 
 __device__ __forceinline__ unsigned node_index(const Box &b, int x, int y, int z)
@@ -119,6 +139,50 @@ __device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
+// ---- mbarrier + TMA (bulk tensor copy) ----
+__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_init_fence() { asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory"); }
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, unsigned bytes)
+{
+    asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n}\n" ::"r"(smem_u32(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned phase)
+{
+    unsigned done;
+    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+                 : "=r"(done)
+                 : "r"(smem_u32(bar)), "r"(phase)
+                 : "memory");
+    return done != 0;
+}
+// Bounded wait for phase `phase` of an mbarrier: false after kWaitLimit polls
+// (each poll may suspend the thread for a hardware-defined time).
+constexpr unsigned kWaitLimit = 1u << 22;
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned phase)
+{
+    for (unsigned it = 0; it < kWaitLimit; ++it)
+        if (mbar_try_wait(bar, phase)) return true;
+    return false;
+}
+// Order this thread's earlier generic-proxy shared-memory accesses (made
+// visible to it by a barrier) before a following TMA write to the same bytes.
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
+__device__ __forceinline__ void tma_load_4d(void *dst, const CUtensorMap *map, int c0, int c1, int c2, int c3,
+                                            uint64_t *bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+        "[%6];\n" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(bar))
+        : "memory");
+}
+
 // f(Dir<i>) for i = I, I + D, I + 2D, ... < 19
 template <int I, int D, typename F>
 __device__ __forceinline__ void for_dirs_from(F &&f)
@@ -129,15 +193,18 @@ __device__ __forceinline__ void for_dirs_from(F &&f)
     }
 }
 
-template <typename ST, bool STREAMED, bool ODD>
+// TMA: the even step's g rows come by one tensor copy per plane (gmap), in the
+// dense layout [field][TY][TX]; otherwise gmap is unused.
+template <typename ST, bool STREAMED, bool ODD, bool TMA>
 __global__ void __launch_bounds__(NT, Fmt<ST>::kMinBlocks)
 zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Quant q, const int tz,
-                const int write_moments)
+                const int write_moments, const __grid_constant__ CUtensorMap gmap)
 {
+    static_assert(!(TMA && ODD), "the odd step's g rows are shifted per direction: cp.async");
     using Gm = Geo<ST>;
     using Fm = Fmt<ST>;
     constexpr int E = Gm::E, W = Gm::W, CR = Gm::CR, CM = Gm::CM;
-    extern __shared__ __align__(16) unsigned char smem[];
+    extern __shared__ __align__(128) unsigned char smem[];
     ST *const G = reinterpret_cast<ST *>(smem + Gm::G_OFF);            // [NG][19][TY][W]
     unsigned char *const F = smem + Gm::F_OFF;                          // [NF]{f0 [FR][W0]; fq [6][FR][W]}
     float *const PHI = reinterpret_cast<float *>(smem + Gm::PHI_OFF);   // [NPHI][RH][RW]
@@ -155,6 +222,22 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Quan
     const int nzc = min(tz, b.nz - z0);       // planes of this chunk
     const int x0 = bx * TX, y0 = by * TY;
     const int x = x0 + tx, y = y0 + ty;
+
+    uint64_t *const mbar = reinterpret_cast<uint64_t *>(smem + Gm::MBAR_OFF);
+    if constexpr (TMA) {
+        // a TMA destination must be 128-byte aligned (uniform check: every
+        // thread returns before any wait or barrier)
+        if (smem_u32(G) & 127u) {
+            if (tid == 0) atomicOr(P.err, 2);
+            return;
+        }
+        if (tid == 0) {
+            mbar_init(&mbar[0], 1);
+            mbar_init(&mbar[1], 1);
+            mbar_init_fence();
+        }
+        __syncthreads();
+    }
 
     // Halo ring node handled by this thread (if any): top row, bottom row,
     // left column, right column of the (TX+2) x (TY+2) phi tile.
@@ -243,6 +326,14 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Quan
     // steps read the node's own slots; odd steps read direction i of node x
     // from the reversed slot of x - c_i (AA pattern).
     auto issue_g = [&](int z, int s) {
+        if constexpr (TMA) {
+            if (tid == 0) {
+                fence_proxy_async();
+                mbar_expect_tx(&mbar[s], (unsigned)Gm::G_TMA_BYTES);
+                tma_load_4d(G + s * G_ELEMS, &gmap, x0, y0, z, 0, &mbar[s]);
+            }
+            return;
+        }
         if (!g_issuer) return;
         ST *dst = G + s * G_ELEMS + g_r * W;
         if (!ODD) {
@@ -358,7 +449,18 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Quan
         }
         cp_async_commit();
         build_plane(z + 1, (j + 2) & 3, fnext);
-        __syncthreads();
+        if constexpr (TMA) {
+            // g of plane z: stage j & 1, its (j >> 1)-th use
+            const bool late = !mbar_wait(&mbar[j & 1], (unsigned)(j >> 1) & 1u);
+            if (__syncthreads_or(late)) {
+                if (tid == 0) atomicOr(P.err, 1);
+                // the copy of plane z + 1 may still be in flight: wait for it (bounded)
+                if (j + 1 < nzc) mbar_wait(&mbar[(j + 1) & 1], (unsigned)((j + 1) >> 1) & 1u);
+                return;
+            }
+        } else {
+            __syncthreads();
+        }
 
         const float *S0 = PHI + (j & 3) * (RH * RW);        // plane z - 1
         const float *S1 = PHI + ((j + 1) & 3) * (RH * RW);  // plane z
@@ -396,7 +498,7 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Quan
         float g[kQg];
 #pragma unroll
         for (int i = 0; i < kQg; i++) {
-            const float v = Fm::load(Gs[(i * TY + ty) * W + E + tx - (ODD ? kCx(i) : 0)]);
+            const float v = Fm::load(TMA ? Gs[(i * TY + ty) * TX + tx] : Gs[(i * TY + ty) * W + E + tx - (ODD ? kCx(i) : 0)]);
             if constexpr (Fm::kMapped) g[i] = v * q.g_inv[i] + q.g_shift[i]; else g[i] = v;
         }
 
@@ -512,15 +614,59 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Quan
     }
 }
 
-template <typename ST, bool S, bool O>
+template <typename ST, bool S, bool O, bool T>
 cudaError_t configure()
 {
     static bool done = false;   // per template instance, per process
     if (done) return cudaSuccess;
-    const cudaError_t e = cudaFuncSetAttribute(zsc_step_kernel<ST, S, O>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                               Geo<ST>::SMEM);
+    const cudaError_t e = cudaFuncSetAttribute(zsc_step_kernel<ST, S, O, T>,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize, Geo<ST>::SMEM);
     if (e == cudaSuccess) done = true;
     return e;
+}
+
+// cuTensorMapEncodeTiled from the driver (no link-time dependency on it).
+using EncodeTiled = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                 const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiled tensor_map_encoder()
+{
+    static const EncodeTiled fn = [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &p, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            return EncodeTiled(nullptr);
+        return reinterpret_cast<EncodeTiled>(p);
+    }();
+    return fn;
+}
+
+template <typename ST>
+constexpr CUtensorMapDataType tensor_type()
+{
+    if constexpr (std::is_same<ST, float>::value) return CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+    else if constexpr (std::is_same<ST, __half>::value) return CU_TENSOR_MAP_DATA_TYPE_FLOAT16;
+    else return CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
+}
+
+// The 19 g arrays at g (n elements each) as one 4-d tensor (x, y, z, field)
+// read in boxes of one plane's tile: 32 x 8 x 1 x 19.  Strides are multiples of
+// 16 bytes (nx is a multiple of 32) and the base is a cudaMalloc pointer.
+template <typename ST>
+bool encode_g_map(const Box &b, const ST *g, CUtensorMap *map)
+{
+    const EncodeTiled encode = tensor_map_encoder();
+    if (!encode) return false;
+    const cuuint64_t es = sizeof(ST);
+    const cuuint64_t dims[4] = {(cuuint64_t)b.nx, (cuuint64_t)b.ny, (cuuint64_t)b.nz, (cuuint64_t)kQg};
+    const cuuint64_t strides[3] = {(cuuint64_t)b.nx * es, (cuuint64_t)b.nxy * es, (cuuint64_t)b.n * es};
+    const cuuint32_t box[4] = {(cuuint32_t)TX, (cuuint32_t)TY, 1u, (cuuint32_t)kQg};
+    const cuuint32_t elem[4] = {1u, 1u, 1u, 1u};
+    if ((reinterpret_cast<uintptr_t>(g) & 15u) != 0) return false;
+    return encode(map, tensor_type<ST>(), 4, const_cast<ST *>(g), dims, strides, box, elem,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 // Planes per block.  The blocks of one launch all march the same number of
@@ -536,7 +682,8 @@ int choose_tz(const Box &b)
         int dev = 0, sms = 0, per_sm = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, zsc_step_kernel<ST, false, false>, NT, Geo<ST>::SMEM);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, zsc_step_kernel<ST, false, false, false>, NT,
+                                                      Geo<ST>::SMEM);
         slots = sms * per_sm > 0 ? sms * per_sm : 1;
     }
     const long long tiles = (long long)(b.nx / TX) * (b.ny / TY);
@@ -575,10 +722,17 @@ cudaError_t launch_typed(const Box &b, const StepConst &c, const Quant &q, const
         P.g[i] = g + (size_t)i * b.n;
     }
     for (int i = 0; i < 5; i++) P.mom[i] = v.mom + (size_t)i * b.n;
-    cudaError_t e = configure<ST, true, false>();
-    if (e == cudaSuccess) e = configure<ST, false, true>();
-    if (e == cudaSuccess) e = configure<ST, false, false>();
+    P.err = v.err;
+    cudaError_t e = configure<ST, true, false, false>();
+    if (e == cudaSuccess) e = configure<ST, false, true, false>();
+    if (e == cudaSuccess) e = configure<ST, false, false, false>();
+    if (e == cudaSuccess) e = configure<ST, true, false, true>();
+    if (e == cudaSuccess) e = configure<ST, false, false, true>();
     if (e != cudaSuccess) return e;
+    // even steps: the g tile by TMA when the driver encodes the map
+    CUtensorMap gmap;
+    std::memset(&gmap, 0, sizeof(gmap));
+    const bool tma = kUseTma && !odd && encode_g_map<ST>(b, gin, &gmap);
     const int tz = choose_tz<ST>(b);
     const int nchunks = (b.nz + tz - 1) / tz;
     const unsigned nblocks = (unsigned)((b.nx / TX) * (b.ny / TY) * nchunks);
@@ -587,11 +741,16 @@ cudaError_t launch_typed(const Box &b, const StepConst &c, const Quant &q, const
     constexpr int smem = Geo<ST>::SMEM;
     if (f_streamed) {
         if (odd) return cudaErrorInvalidValue;  // the streamed initial state is always read by an even step
-        zsc_step_kernel<ST, true, false><<<nblocks, block, smem, s>>>(P, b, c, q, tz, wm);
+        if (tma)
+            zsc_step_kernel<ST, true, false, true><<<nblocks, block, smem, s>>>(P, b, c, q, tz, wm, gmap);
+        else
+            zsc_step_kernel<ST, true, false, false><<<nblocks, block, smem, s>>>(P, b, c, q, tz, wm, gmap);
     } else if (odd) {
-        zsc_step_kernel<ST, false, true><<<nblocks, block, smem, s>>>(P, b, c, q, tz, wm);
+        zsc_step_kernel<ST, false, true, false><<<nblocks, block, smem, s>>>(P, b, c, q, tz, wm, gmap);
+    } else if (tma) {
+        zsc_step_kernel<ST, false, false, true><<<nblocks, block, smem, s>>>(P, b, c, q, tz, wm, gmap);
     } else {
-        zsc_step_kernel<ST, false, false><<<nblocks, block, smem, s>>>(P, b, c, q, tz, wm);
+        zsc_step_kernel<ST, false, false, false><<<nblocks, block, smem, s>>>(P, b, c, q, tz, wm, gmap);
     }
     return cudaGetLastError();
 }

@@ -70,9 +70,10 @@ def test_adjoint_needs_initial_state(lib):
 
 
 def test_objective_alone_matches_adjoint_J(lib):
-    """lbm_objective runs the same forward states as lbm_step_adjoint, so J is
-    bit-identical; central differences of it agree with dJ/dgrav to FP32
-    trajectory noise (5e-3 relative at h = 1e-5 on a 16 x 32 x 32 box)."""
+    """lbm_objective runs the same forward states as lbm_step_adjoint, so J
+    agrees to the rounding of its FP64 sum (the adjoint adds the window's terms
+    in reverse step order); central differences of it agree with dJ/dgrav to
+    FP32 trajectory noise (5e-3 relative at h = 1e-5 on a 16 x 32 x 32 box)."""
     from lbm_bench_gpu_gb300 import capi
     phi0, rho0 = fields()
     p = capi.make_params(32, 32, 16, **KW)
@@ -83,5 +84,5 @@ def test_objective_alone_matches_adjoint_J(lib):
         h = 1e-5
         fd = (lat.objective(12, grav + h, "light_uz_mean", 5) - lat.objective(12, grav - h, "light_uz_mean", 5)) / (2 * h)
         assert lat.steps == 0
-    assert J == r["J"]
+    assert J == pytest.approx(r["J"], rel=1e-14)
     assert fd == pytest.approx(r["dJ_dgrav"], rel=5e-3)
