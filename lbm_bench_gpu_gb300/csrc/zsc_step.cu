@@ -38,10 +38,14 @@
 // wrap) and the odd step's shifted g rows are cp.async 16-byte chunks: warps
 // 0-3 queue P_f, warps 4-7 queue g, each thread with chunk coordinates fixed
 // for the whole block; with nx a multiple of 32 no chunk straddles the seam.
-// The even step's g rows are the tile itself in all 19 fields, which one
-// thread fetches with a single TMA tensor copy per plane (a 4-d tensor map
-// x, y, z, field; box 32 x 8 x 1 x 19) completing on an mbarrier; the waits
-// on it are bounded and report a timeout through an error flag.
+// The g rows go by TMA tensor copies (4-d tensor map x, y, z, field)
+// completing on an mbarrier: in the even step the tile itself in all 19
+// fields, one copy per plane (box 32 x 8 x 1 x 19); in the odd step, on tiles
+// whose shifted rows stay inside the box (no periodic wrap, which TMA's fill
+// cannot express), one copy per direction (box W x 8 x 1 x 1 at the shifted
+// origin, W = 32 + 2E as the cp.async rows); the other odd tiles keep
+// cp.async.  The mbarrier waits are bounded and report a timeout through an
+// error flag.
 #include <cuda.h>   // CUtensorMap (the encoder is fetched from the driver at run time)
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
@@ -77,7 +81,23 @@ constexpr float kInv6 = 0.16666666666666666667f;
 #ifndef ZSC_TMA_G
 #define ZSC_TMA_G 1
 #endif
+// odd steps by TMA too (19 per-direction copies per plane on interior tiles):
+// measured slower than cp.async (FP16 33.7k vs 36.2k MLUPS at 256^3), so off
+#ifndef ZSC_TMA_ODD
+#define ZSC_TMA_ODD 0
+#endif
+// the P_f planes by TMA on interior tiles (f_0 box W0 x FR, f_1..f_6 box
+// W x FR x 6), for the 16-bit formats: measured at 256^3 (same GPU, 500
+// steps), FP16 36 250 -> 37 060 MLUPS, while FP32 drops 27 110 -> 26 560 with
+// it (its per-thread cp.async spreads the twice larger planes better)
+#ifndef ZSC_TMA_F
+#define ZSC_TMA_F 1
+#endif
 constexpr bool kUseTma = ZSC_TMA_G != 0;
+constexpr bool kUseTmaOdd = ZSC_TMA_ODD != 0;
+constexpr bool kUseTmaF = ZSC_TMA_F != 0;
+template <typename ST>
+constexpr bool use_tma_f() { return kUseTmaF && sizeof(ST) == 2; }
 constexpr float kInv12 = 0.08333333333333333333f;
 
 template <int I>
@@ -99,14 +119,15 @@ struct Geo {
     static constexpr int G_OFF = 0;
     static constexpr int F_OFF = NG * G_STAGE;
     static constexpr int PHI_OFF = F_OFF + NF * F_STAGE;
-    static constexpr int MBAR_OFF = PHI_OFF + NPHI * PHI_STAGE;   // two mbarriers (even-step g stages)
-    static constexpr int SMEM = MBAR_OFF + 16;
+    static constexpr int MBAR_OFF = PHI_OFF + NPHI * PHI_STAGE;   // mbarriers: 2 g stages, then NF P_f stages
+    static constexpr int SMEM = MBAR_OFF + 8 * (NG + NF);
     static constexpr int G_TMA_BYTES = kQg * TY * TX * (int)sizeof(ST);   // one plane's tile, 19 fields
     static constexpr int TPD = TY * CM;              // g issuer threads per direction
     static constexpr int D = (NT / 2) / TPD;         // directions per pass of the g issuers
     static_assert(G_STAGE % 16 == 0 && F_STAGE % 16 == 0 && F0_BYTES % 16 == 0, "16-byte aligned stages");
     static_assert(G_STAGE % 128 == 0 && G_TMA_BYTES <= G_STAGE, "TMA destinations: 128-byte aligned, inside a stage");
     static_assert(MBAR_OFF % 8 == 0, "8-byte aligned mbarriers");
+    static_assert(F_OFF % 128 == 0 && F_STAGE % 128 == 0 && F0_BYTES % 128 == 0, "P_f TMA destinations 128-byte aligned");
     static_assert(FR * (W0 / 4) <= NT / 2 && FR * CR <= NT / 2, "P_f issuers fit in warps 0-3");
     static_assert(D * TPD == NT / 2, "g issuers cover whole directions");
 };
@@ -173,6 +194,14 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned phase)
 // Order this thread's earlier generic-proxy shared-memory accesses (made
 // visible to it by a barrier) before a following TMA write to the same bytes.
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
+__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, int c0, int c1, int c2, uint64_t *bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];\n" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
+        : "memory");
+}
 __device__ __forceinline__ void tma_load_4d(void *dst, const CUtensorMap *map, int c0, int c1, int c2, int c3,
                                             uint64_t *bar)
 {
@@ -193,14 +222,15 @@ __device__ __forceinline__ void for_dirs_from(F &&f)
     }
 }
 
-// TMA: the even step's g rows come by one tensor copy per plane (gmap), in the
-// dense layout [field][TY][TX]; otherwise gmap is unused.
+// TMA: the g rows come by tensor copies (gmap): even steps one copy per plane
+// in the dense layout [field][TY][TX]; odd steps, on interior tiles, one copy
+// per direction into the [dir][TY][W] rows.  Without TMA gmap is unused.
 template <typename ST, bool STREAMED, bool ODD, bool TMA>
 __global__ void __launch_bounds__(NT, Fmt<ST>::kMinBlocks)
 zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Quant q, const int tz,
-                const int write_moments, const __grid_constant__ CUtensorMap gmap)
+                const int write_moments, const __grid_constant__ CUtensorMap gmap,
+                const __grid_constant__ CUtensorMap f0map, const __grid_constant__ CUtensorMap fqmap)
 {
-    static_assert(!(TMA && ODD), "the odd step's g rows are shifted per direction: cp.async");
     using Gm = Geo<ST>;
     using Fm = Fmt<ST>;
     constexpr int E = Gm::E, W = Gm::W, CR = Gm::CR, CM = Gm::CM;
@@ -224,6 +254,14 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Quan
     const int x = x0 + tx, y = y0 + ty;
 
     uint64_t *const mbar = reinterpret_cast<uint64_t *>(smem + Gm::MBAR_OFF);
+    // odd step: the rows y0 - 1 .. y0 + TY and columns x0 - E .. x0 + TX + E - 1
+    // must lie inside the box for the shifted tensor copies (uniform per block)
+    const bool tile_tma =
+        TMA && (!ODD || (kUseTmaOdd && x0 - E >= 0 && x0 + TX + E <= b.nx && y0 - 1 >= 0 && y0 + TY + 1 <= b.ny));
+    // P_f planes by TMA: the staged rows y0 - 2 .. y0 + TY + 1 and columns
+    // x0 - 4 .. x0 + TX + 3 (f_0) / x0 - E .. x0 + TX + E - 1 (f_1..f_6) inside the box
+    const bool tile_tma_f = TMA && use_tma_f<ST>() && x0 - 4 >= 0 && x0 - E >= 0 && x0 + TX + 4 <= b.nx &&
+                            x0 + TX + E <= b.nx && y0 - 2 >= 0 && y0 + TY + 2 <= b.ny;
     if constexpr (TMA) {
         // a TMA destination must be 128-byte aligned (uniform check: every
         // thread returns before any wait or barrier)
@@ -232,8 +270,7 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Quan
             return;
         }
         if (tid == 0) {
-            mbar_init(&mbar[0], 1);
-            mbar_init(&mbar[1], 1);
+            for (int k = 0; k < NG + NF; k++) mbar_init(&mbar[k], 1);
             mbar_init_fence();
         }
         __syncthreads();
@@ -294,8 +331,24 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Quan
         g_x_wrap = wrap(x0 + TX, b.nx);                // c_x = -1 also needs x0 + TX
     }
 
+    // P_f stage p's mbarrier and the phase of plane p's use of it (planes
+    // z0 - 2 + m go to stage (m + 2) & 3 for their (m >> 2)-th use)
+    auto fbar = [&](int p) { return &mbar[NG + ((p - z0 + 4) & (NF - 1))]; };
+    auto fphase = [&](int p) { return (unsigned)((p - z0 + 2) >> 2) & 1u; };
+
     // Queue the 7 P_f planes of plane p (tile + halo) into its stage.
     auto issue_f = [&](int p) {
+        if (tile_tma_f) {
+            if (tid == 32) {   // lane 0 of warp 1 (warp 0 issues the g copies)
+                unsigned char *st = fstage(p);
+                const int zp = wrap(p, b.nz);
+                fence_proxy_async();
+                mbar_expect_tx(fbar(p), (unsigned)Gm::F_STAGE);
+                tma_load_3d(f0part(st), &f0map, x0 - 4, y0 - 2, zp, fbar(p));
+                tma_load_4d(fqpart(st), &fqmap, x0 - E, y0 - 2, zp, 0, fbar(p));
+            }
+            return;
+        }
         const unsigned zb = (unsigned)wrap(p, b.nz) * (unsigned)b.nxy;
         unsigned char *st = fstage(p);
         if (f0_issuer) cp_async16(f0part(st) + f0_dst, P.f0in + (zb + (unsigned)f0_xy));
@@ -326,11 +379,29 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Quan
     // steps read the node's own slots; odd steps read direction i of node x
     // from the reversed slot of x - c_i (AA pattern).
     auto issue_g = [&](int z, int s) {
-        if constexpr (TMA) {
+        if constexpr (TMA && !ODD) {
             if (tid == 0) {
                 fence_proxy_async();
                 mbar_expect_tx(&mbar[s], (unsigned)Gm::G_TMA_BYTES);
                 tma_load_4d(G + s * G_ELEMS, &gmap, x0, y0, z, 0, &mbar[s]);
+            }
+            return;
+        }
+        if (tile_tma) {
+            // odd step, interior tile: lane i of warp 0 copies direction i, the
+            // reversed slot of the upstream rows x - c_i (columns from x0 - E)
+            if (tid < 32) {
+                if (tid == 0) {
+                    fence_proxy_async();
+                    mbar_expect_tx(&mbar[s], (unsigned)Gm::G_STAGE);
+                }
+                __syncwarp();
+                if (tid < kQg) {
+                    const int i = tid;
+                    const int zc = wrap(z - kCz(i), b.nz);
+                    fence_proxy_async();
+                    tma_load_4d(G + s * G_ELEMS + i * TY * W, &gmap, x0 - E, y0 - kCy(i), zc, kOpp(i), &mbar[s]);
+                }
             }
             return;
         }
@@ -429,6 +500,10 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Quan
     issue_g(z0, 0);
     cp_async_commit();
     cp_async_wait_all();
+    bool late = false;
+    if (tile_tma_f) {
+        for (int p = z0 - 2; p <= z0 + 1; p++) late |= !mbar_wait(fbar(p), fphase(p));
+    }
     __syncthreads();
     {
         float tmp[kQf];
@@ -448,14 +523,19 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Quan
             issue_f(z + 3);
         }
         cp_async_commit();
+        // P_f plane z + 2 is first read here (a late copy only spoils values:
+        // the uniform exit below comes before anything is stored)
+        if (tile_tma_f) late |= !mbar_wait(fbar(z + 2), fphase(z + 2));
         build_plane(z + 1, (j + 2) & 3, fnext);
         if constexpr (TMA) {
-            // g of plane z: stage j & 1, its (j >> 1)-th use
-            const bool late = !mbar_wait(&mbar[j & 1], (unsigned)(j >> 1) & 1u);
+            // g of plane z: stage j & 1, its (j >> 1)-th use (cp.async tiles
+            // were complete at the barrier above)
+            if (tile_tma) late |= !mbar_wait(&mbar[j & 1], (unsigned)(j >> 1) & 1u);
             if (__syncthreads_or(late)) {
                 if (tid == 0) atomicOr(P.err, 1);
-                // the copy of plane z + 1 may still be in flight: wait for it (bounded)
-                if (j + 1 < nzc) mbar_wait(&mbar[(j + 1) & 1], (unsigned)((j + 1) >> 1) & 1u);
+                // copies still in flight: wait for them (bounded) before leaving
+                if (tile_tma && j + 1 < nzc) mbar_wait(&mbar[(j + 1) & 1], (unsigned)((j + 1) >> 1) & 1u);
+                if (tile_tma_f && j + 1 < nzc) mbar_wait(fbar(z + 3), fphase(z + 3));
                 return;
             }
         } else {
@@ -498,7 +578,8 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Quan
         float g[kQg];
 #pragma unroll
         for (int i = 0; i < kQg; i++) {
-            const float v = Fm::load(TMA ? Gs[(i * TY + ty) * TX + tx] : Gs[(i * TY + ty) * W + E + tx - (ODD ? kCx(i) : 0)]);
+            const float v = Fm::load((TMA && !ODD) ? Gs[(i * TY + ty) * TX + tx]
+                                                   : Gs[(i * TY + ty) * W + E + tx - (ODD ? kCx(i) : 0)]);
             if constexpr (Fm::kMapped) g[i] = v * q.g_inv[i] + q.g_shift[i]; else g[i] = v;
         }
 
@@ -634,7 +715,8 @@ EncodeTiled tensor_map_encoder()
     static const EncodeTiled fn = [] {
         void *p = nullptr;
         cudaDriverEntryPointQueryResult q{};
-        if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &p, cudaEnableDefault, &q) != cudaSuccess ||
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
             q != cudaDriverEntryPointSuccess)
             return EncodeTiled(nullptr);
         return reinterpret_cast<EncodeTiled>(p);
@@ -650,21 +732,50 @@ constexpr CUtensorMapDataType tensor_type()
     else return CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
 }
 
-// The 19 g arrays at g (n elements each) as one 4-d tensor (x, y, z, field)
-// read in boxes of one plane's tile: 32 x 8 x 1 x 19.  Strides are multiples of
-// 16 bytes (nx is a multiple of 32) and the base is a cudaMalloc pointer.
+// The 19 g arrays at g (n elements each) as one 4-d tensor (x, y, z, field),
+// read in boxes of one plane's tile in all fields (even steps: 32 x 8 x 1 x 19)
+// or of one field's W-wide rows (odd steps: W x 8 x 1 x 1).  Strides are
+// multiples of 16 bytes (nx is a multiple of 32); the base must be 16-byte
+// aligned (a cudaMalloc pointer, or a checkpoint slot offset by whole fields).
 template <typename ST>
-bool encode_g_map(const Box &b, const ST *g, CUtensorMap *map)
+bool encode_g_map(const Box &b, const ST *g, bool odd, CUtensorMap *map)
 {
     const EncodeTiled encode = tensor_map_encoder();
     if (!encode) return false;
     const cuuint64_t es = sizeof(ST);
     const cuuint64_t dims[4] = {(cuuint64_t)b.nx, (cuuint64_t)b.ny, (cuuint64_t)b.nz, (cuuint64_t)kQg};
     const cuuint64_t strides[3] = {(cuuint64_t)b.nx * es, (cuuint64_t)b.nxy * es, (cuuint64_t)b.n * es};
-    const cuuint32_t box[4] = {(cuuint32_t)TX, (cuuint32_t)TY, 1u, (cuuint32_t)kQg};
+    const cuuint32_t box[4] = {odd ? (cuuint32_t)Geo<ST>::W : (cuuint32_t)TX, (cuuint32_t)TY, 1u,
+                               odd ? 1u : (cuuint32_t)kQg};
     const cuuint32_t elem[4] = {1u, 1u, 1u, 1u};
     if ((reinterpret_cast<uintptr_t>(g) & 15u) != 0) return false;
     return encode(map, tensor_type<ST>(), 4, const_cast<ST *>(g), dims, strides, box, elem,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// The P_f planes: f_0 (FP32) as a 3-d tensor read in W0 x FR boxes, f_1..f_6
+// (six consecutive arrays) as a 4-d tensor (x, y, z, field) read in
+// W x FR x 1 x 6 boxes, both from x0 - 4 / x0 - E and y0 - 2.
+template <typename ST>
+bool encode_f_maps(const Box &b, const float *f0, const ST *fq, CUtensorMap *f0map, CUtensorMap *fqmap)
+{
+    const EncodeTiled encode = tensor_map_encoder();
+    if (!encode) return false;
+    if ((reinterpret_cast<uintptr_t>(f0) & 15u) != 0 || (reinterpret_cast<uintptr_t>(fq) & 15u) != 0) return false;
+    const cuuint32_t elem[4] = {1u, 1u, 1u, 1u};
+    const cuuint64_t dims0[3] = {(cuuint64_t)b.nx, (cuuint64_t)b.ny, (cuuint64_t)b.nz};
+    const cuuint64_t strides0[2] = {(cuuint64_t)b.nx * 4, (cuuint64_t)b.nxy * 4};
+    const cuuint32_t box0[3] = {(cuuint32_t)W0, (cuuint32_t)FR, 1u};
+    if (encode(f0map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float *>(f0), dims0, strides0, box0, elem,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return false;
+    const cuuint64_t es = sizeof(ST);
+    const cuuint64_t dims[4] = {(cuuint64_t)b.nx, (cuuint64_t)b.ny, (cuuint64_t)b.nz, (cuuint64_t)(kQf - 1)};
+    const cuuint64_t strides[3] = {(cuuint64_t)b.nx * es, (cuuint64_t)b.nxy * es, (cuuint64_t)b.n * es};
+    const cuuint32_t box[4] = {(cuuint32_t)Geo<ST>::W, (cuuint32_t)FR, 1u, (cuuint32_t)(kQf - 1)};
+    return encode(fqmap, tensor_type<ST>(), 4, const_cast<ST *>(fq), dims, strides, box, elem,
                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
@@ -728,11 +839,18 @@ cudaError_t launch_typed(const Box &b, const StepConst &c, const Quant &q, const
     if (e == cudaSuccess) e = configure<ST, false, false, false>();
     if (e == cudaSuccess) e = configure<ST, true, false, true>();
     if (e == cudaSuccess) e = configure<ST, false, false, true>();
+    if (e == cudaSuccess) e = configure<ST, false, true, true>();
     if (e != cudaSuccess) return e;
-    // even steps: the g tile by TMA when the driver encodes the map
-    CUtensorMap gmap;
+    // staging by TMA when the driver encodes every map the step needs: the g
+    // rows (even steps, and odd ones if enabled) and the P_f planes (if enabled)
+    CUtensorMap gmap, f0map, fqmap;
     std::memset(&gmap, 0, sizeof(gmap));
-    const bool tma = kUseTma && !odd && encode_g_map<ST>(b, gin, &gmap);
+    std::memset(&f0map, 0, sizeof(f0map));
+    std::memset(&fqmap, 0, sizeof(fqmap));
+    const bool need_g = !odd || kUseTmaOdd;
+    bool tma = kUseTma && (need_g || use_tma_f<ST>());
+    if (tma && need_g) tma = encode_g_map<ST>(b, gin, odd, &gmap);
+    if (tma && use_tma_f<ST>()) tma = encode_f_maps<ST>(b, P.f0in, fin, &f0map, &fqmap);
     const int tz = choose_tz<ST>(b);
     const int nchunks = (b.nz + tz - 1) / tz;
     const unsigned nblocks = (unsigned)((b.nx / TX) * (b.ny / TY) * nchunks);
@@ -742,15 +860,18 @@ cudaError_t launch_typed(const Box &b, const StepConst &c, const Quant &q, const
     if (f_streamed) {
         if (odd) return cudaErrorInvalidValue;  // the streamed initial state is always read by an even step
         if (tma)
-            zsc_step_kernel<ST, true, false, true><<<nblocks, block, smem, s>>>(P, b, c, q, tz, wm, gmap);
+            zsc_step_kernel<ST, true, false, true><<<nblocks, block, smem, s>>>(P, b, c, q, tz, wm, gmap, f0map, fqmap);
         else
-            zsc_step_kernel<ST, true, false, false><<<nblocks, block, smem, s>>>(P, b, c, q, tz, wm, gmap);
+            zsc_step_kernel<ST, true, false, false><<<nblocks, block, smem, s>>>(P, b, c, q, tz, wm, gmap, f0map, fqmap);
     } else if (odd) {
-        zsc_step_kernel<ST, false, true, false><<<nblocks, block, smem, s>>>(P, b, c, q, tz, wm, gmap);
+        if (tma)
+            zsc_step_kernel<ST, false, true, true><<<nblocks, block, smem, s>>>(P, b, c, q, tz, wm, gmap, f0map, fqmap);
+        else
+            zsc_step_kernel<ST, false, true, false><<<nblocks, block, smem, s>>>(P, b, c, q, tz, wm, gmap, f0map, fqmap);
     } else if (tma) {
-        zsc_step_kernel<ST, false, false, true><<<nblocks, block, smem, s>>>(P, b, c, q, tz, wm, gmap);
+        zsc_step_kernel<ST, false, false, true><<<nblocks, block, smem, s>>>(P, b, c, q, tz, wm, gmap, f0map, fqmap);
     } else {
-        zsc_step_kernel<ST, false, false, false><<<nblocks, block, smem, s>>>(P, b, c, q, tz, wm, gmap);
+        zsc_step_kernel<ST, false, false, false><<<nblocks, block, smem, s>>>(P, b, c, q, tz, wm, gmap, f0map, fqmap);
     }
     return cudaGetLastError();
 }
