@@ -201,7 +201,11 @@ typedef struct lbm_adjoint_out {
  * counterpart in the reference.  The context must hold its initial state
  * (lbm_init / lbm_init_bubbles / lbm_set_dist, no step taken); the gradient
  * with respect to phi0 passes through the initial equilibrium with periodic
- * z.  On return the context holds the initial state again.  Synchronises. */
+ * z.  On return the context holds the initial state again.  Synchronises.
+ * The work buffers and the checkpoint pool stay allocated in the context for
+ * the next call (a pool larger than the next budget is reused, not shrunk)
+ * until lbm_adjoint_release or lbm_destroy; checkpoint_bytes <= 0 counts the
+ * cached pool as free memory. */
 int lbm_step_adjoint(lbm_ctx *c, const lbm_adjoint_opts *o, lbm_adjoint_out *out);
 
 /* The objective of lbm_step_adjoint alone (forward run, no gradient), e.g.
@@ -210,6 +214,11 @@ int lbm_step_adjoint(lbm_ctx *c, const lbm_adjoint_opts *o, lbm_adjoint_out *out
  * Same preconditions; on return the context holds the initial state again.
  * Synchronises. */
 int lbm_objective(lbm_ctx *c, const lbm_adjoint_opts *o, double *J);
+
+/* Free the adjoint work buffers and checkpoint pool that lbm_step_adjoint and
+ * lbm_objective keep in the context.  No counterpart in the reference.
+ * Synchronises the context's stream. */
+int lbm_adjoint_release(lbm_ctx *c);
 
 /* Largest box lbm_stats_noalloc accepts: 512^3 nodes. */
 #define LBM_NOALLOC_MAX_NODES 134217728LL

@@ -23,7 +23,7 @@ EXPORTS = [
     "lbm_read_inputs", "lbm_derive", "lbm_init", "lbm_init_bubbles", "lbm_step", "lbm_stats",
     "lbm_get_dist", "lbm_set_dist", "lbm_steps_done", "lbm_stream", "lbm_sync", "lbm_destroy",
     "lbm_strerror", "lbm_last_error", "lbm_stats_noalloc", "lbm_step_adjoint",
-    "lbm_objective", "lbm_stats_fields", "lbm_pressure", "lbm_device_name",
+    "lbm_objective", "lbm_stats_fields", "lbm_pressure", "lbm_device_name", "lbm_adjoint_release",
 ]
 OBJECTIVES = {"light_uz_mean": 0, "light_z_centroid": 1}
 
@@ -109,6 +109,7 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
                                       C.c_void_p, C.c_void_p, C.c_void_p]
     lib.lbm_step_adjoint.argtypes = [C.c_void_p, C.POINTER(AdjointOpts), C.POINTER(AdjointOut)]
     lib.lbm_objective.argtypes = [C.c_void_p, C.POINTER(AdjointOpts), C.POINTER(C.c_double)]
+    lib.lbm_adjoint_release.argtypes = [C.c_void_p]
     lib.lbm_stats_fields.argtypes = [C.c_void_p, C.POINTER(StatsOut), _F, _F, _F, _F, _F]
     lib.lbm_pressure.argtypes = [C.c_void_p, _F]
     lib.lbm_device_name.argtypes = [C.c_int, C.c_char_p, C.c_int, C.POINTER(C.c_double)]
@@ -264,6 +265,10 @@ class Lattice:
         J = C.c_double()
         check(load().lbm_objective(self._h, C.byref(o), C.byref(J)), "lbm_objective")
         return float(J.value)
+
+    def adjoint_release(self) -> None:
+        """lbm_adjoint_release: free the adjoint workspace and checkpoint pool kept in the context."""
+        check(load().lbm_adjoint_release(self._h), "lbm_adjoint_release")
 
     @property
     def steps(self) -> int:

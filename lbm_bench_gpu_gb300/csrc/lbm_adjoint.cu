@@ -36,6 +36,21 @@ double beta(int c, int r)
     return v;
 }
 
+// Sub-buffers of one allocation, 256-byte aligned; with base == nullptr only
+// the size is counted.
+struct Carver {
+    unsigned char *base;
+    size_t off = 0;
+    template <typename T>
+    T *take(size_t count)
+    {
+        off = (off + 255) & ~(size_t)255;
+        T *p = base ? reinterpret_cast<T *>(base + off) : nullptr;
+        off += sizeof(T) * count;
+        return p;
+    }
+};
+
 struct Snapshot {
     long long step = -1;
     bool f_streamed = false, g_odd_next = false;
@@ -54,7 +69,7 @@ struct Adjoint {
     float4 *lsrc = nullptr;
     float *phi0 = nullptr, *mom_save = nullptr;
     double *partials = nullptr, *dgrav = nullptr, *ab = nullptr, *acc = nullptr;
-    unsigned char *slots = nullptr;
+    unsigned char *slots = nullptr;   // the context's checkpoint pool
     std::vector<Snapshot> snaps;
     std::vector<int> free_slots;
     int cur = 0;                 // lam[cur] holds lambda^{k+1}
@@ -341,10 +356,57 @@ struct Adjoint {
             if (x) cudaEventDestroy(x);
         for (cudaEvent_t x : {ctx_ev, side_done, buf_free[0], buf_free[1]})
             if (x) cudaEventDestroy(x);
-        void *p[] = {phi, lam[0], lam[1], lst[0], lst[1], lsrc, phi0, mom_save, partials, dgrav, ab, acc, slots};
-        for (void *q : p) cudaFree(q);
+    }
+
+    // the work buffers, carved from the context's arena; the objective alone
+    // needs only phi, mom_save and the sums
+    void carve(Carver &w, bool gradient, size_t nblocks)
+    {
+        phi = w.take<float>(2 * n);
+        mom_save = w.take<float>(5 * n);
+        partials = w.take<double>(2 * nblocks);
+        ab = w.take<double>(8);
+        acc = w.take<double>(2);
+        if (!gradient) return;
+        lam[0] = w.take<float>((size_t)(lbm::kQf + lbm::kQg) * n);
+        lam[1] = w.take<float>((size_t)(lbm::kQf + lbm::kQg) * n);
+        lst[0] = w.take<float>(n);
+        lst[1] = w.take<float>(n);
+        lsrc = w.take<float4>(n);
+        phi0 = w.take<float>(n);
+        dgrav = w.take<double>(nblocks);
     }
 };
+
+// Grow a cached device buffer to `need` bytes (a larger one is kept).
+int ensure(void *&p, size_t &have, size_t need, const char *what)
+{
+    if (have >= need) return LBM_OK;
+    cudaFree(p);
+    p = nullptr;
+    have = 0;
+    cudaError_t e = cudaMalloc(&p, need);
+    if (e != cudaSuccess) {
+        p = nullptr;
+        return cuda_fail(e, what);
+    }
+    have = need;
+    return LBM_OK;
+}
+
+// The arena and the pool for one call: work buffers carved from
+// c->adj_work, `slot_need` bytes of checkpoints in c->adj_slots.
+int workspace(lbm_ctx *c, Adjoint &A, bool gradient, const char *fn)
+{
+    const size_t nblocks = lbm::adjoint_blocks(c->box);
+    Carver dry{nullptr};
+    A.carve(dry, gradient, nblocks);
+    int rc = ensure(c->adj_work, c->adj_work_bytes, dry.off, fn);
+    if (rc) return rc;
+    Carver w{static_cast<unsigned char *>(c->adj_work)};
+    A.carve(w, gradient, nblocks);
+    return LBM_OK;
+}
 
 }  // namespace
 
@@ -386,19 +448,13 @@ extern "C" int lbm_objective(lbm_ctx *c, const lbm_adjoint_opts *o, double *J)
     if (rc) return rc;
     Adjoint A;
     setup(A, c, o);
-    const size_t n = A.n, nblocks = lbm::adjoint_blocks(c->box);
-    cudaError_t e = cudaMalloc((void **)&A.phi, sizeof(float) * n);
-    if (e == cudaSuccess) e = cudaMalloc((void **)&A.mom_save, sizeof(float) * 5 * n);
-    if (e == cudaSuccess) e = cudaMalloc((void **)&A.partials, sizeof(double) * 2 * nblocks);
-    if (e == cudaSuccess) e = cudaMalloc((void **)&A.ab, sizeof(double) * 4);
-    if (e == cudaSuccess) e = cudaMalloc((void **)&A.acc, sizeof(double) * 2);
-    if (e == cudaSuccess) e = cudaMalloc((void **)&A.slots, A.snap_bytes);
-    if (e != cudaSuccess) {
-        A.release();
-        return cuda_fail(e, "lbm_objective: buffers");
-    }
+    const size_t n = A.n;
+    if ((rc = workspace(c, A, false, "lbm_objective: work buffers")) ||
+        (rc = ensure(c->adj_slots, c->adj_slot_bytes, A.snap_bytes, "lbm_objective: snapshot")))
+        return rc;
+    A.slots = static_cast<unsigned char *>(c->adj_slots);
     A.snaps.assign(1, Snapshot());
-    e = cudaMemsetAsync(A.acc, 0, sizeof(double) * 2, c->stream);
+    cudaError_t e = cudaMemsetAsync(A.acc, 0, sizeof(double) * 2, c->stream);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(A.mom_save, c->st.mom, sizeof(float) * 5 * n, cudaMemcpyDeviceToDevice, c->stream);
     if (e != cudaSuccess) rc = cuda_fail(e, "lbm_objective: setup");
@@ -439,49 +495,27 @@ extern "C" int lbm_step_adjoint(lbm_ctx *c, const lbm_adjoint_opts *o, lbm_adjoi
     setup(A, c, o);
     const size_t n = A.n;
     const size_t nblocks = lbm::adjoint_blocks(c->box);
-
-    auto alloc = [&](void **p, size_t bytes) {
-        if (e == cudaSuccess) e = cudaMalloc(p, bytes);
-    };
-    alloc((void **)&A.phi, sizeof(float) * 2 * n);
-    alloc((void **)&A.lam[0], sizeof(float) * (lbm::kQf + lbm::kQg) * n);
-    alloc((void **)&A.lam[1], sizeof(float) * (lbm::kQf + lbm::kQg) * n);
-    alloc((void **)&A.lst[0], sizeof(float) * n);
-    alloc((void **)&A.lst[1], sizeof(float) * n);
-    alloc((void **)&A.lsrc, sizeof(float4) * n);
-    alloc((void **)&A.phi0, sizeof(float) * n);
-    alloc((void **)&A.mom_save, sizeof(float) * 5 * n);
-    alloc((void **)&A.partials, sizeof(double) * 2 * nblocks);
-    alloc((void **)&A.dgrav, sizeof(double) * nblocks);
-    alloc((void **)&A.ab, sizeof(double) * 8);
-    alloc((void **)&A.acc, sizeof(double) * 2);
-    if (e != cudaSuccess) {
-        A.release();
-        return cuda_fail(e, "lbm_step_adjoint: work buffers");
-    }
-    // checkpoint pool
+    int rc = workspace(c, A, true, "lbm_step_adjoint: work buffers");
+    if (rc) return rc;
+    // checkpoint pool (a cached pool counts as free for the default budget)
     double budget = o->checkpoint_bytes;
     if (!(budget > 0)) {
         size_t fr = 0, tot = 0;
         cudaMemGetInfo(&fr, &tot);
-        budget = 0.5 * (double)fr;
+        budget = 0.5 * ((double)fr + (double)c->adj_slot_bytes);
     }
     long long nslots = (long long)(budget / (double)A.snap_bytes);
     nslots = std::min<long long>(nslots, (long long)o->nsteps + 1);
-    if (nslots < 1) {
-        A.release();
+    if (nslots < 1)
         return fail(LBM_ENOMEM, "lbm_step_adjoint: checkpoint budget below one snapshot (" +
                                     std::to_string(A.snap_bytes) + " bytes)");
-    }
-    e = cudaMalloc(&A.slots, (size_t)nslots * A.snap_bytes);
-    if (e != cudaSuccess) {
-        A.release();
-        return cuda_fail(e, "lbm_step_adjoint: checkpoint pool");
-    }
+    if ((rc = ensure(c->adj_slots, c->adj_slot_bytes, (size_t)nslots * A.snap_bytes,
+                     "lbm_step_adjoint: checkpoint pool")))
+        return rc;
+    A.slots = static_cast<unsigned char *>(c->adj_slots);
     A.snaps.assign((size_t)nslots, Snapshot());
     for (long long s = nslots - 1; s >= 1; s--) A.free_slots.push_back((int)s);
 
-    int rc = LBM_OK;
     e = cudaMemsetAsync(A.acc, 0, sizeof(double) * 2, c->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(A.dgrav, 0, sizeof(double) * nblocks, c->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(A.phi0, c->st.mom, sizeof(float) * n, cudaMemcpyDeviceToDevice, c->stream);
@@ -522,5 +556,18 @@ extern "C" int lbm_step_adjoint(lbm_ctx *c, const lbm_adjoint_opts *o, lbm_adjoi
     out->adjoint_steps = A.adj_steps;
     out->checkpoint_bytes_used = (double)nslots * (double)A.snap_bytes;
     out->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return LBM_OK;
+}
+
+extern "C" int lbm_adjoint_release(lbm_ctx *c)
+{
+    if (!c) return fail(LBM_EINVAL, "lbm_adjoint_release: NULL context");
+    cudaError_t e = cudaSetDevice(c->p.device);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "lbm_adjoint_release");
+    cudaFree(c->adj_work);
+    cudaFree(c->adj_slots);
+    c->adj_work = c->adj_slots = nullptr;
+    c->adj_work_bytes = c->adj_slot_bytes = 0;
     return LBM_OK;
 }

@@ -46,24 +46,10 @@ int validate(const lbm_params *p)
     return LBM_OK;
 }
 
-// The derived coefficients of the storage map (see lbm::Quant).
-void finish_quant(lbm::Quant &q, float eta)
+void identity_quant(lbm::Quant &q)
 {
-    for (int a = 0; a < lbm::kQf - 1; a++) {
-        q.f_eta[a] = eta * q.f_inv[a];
-        q.f_eta2[a] = (1.f - eta) * q.f_inv[a];
-    }
-    for (int i = 0; i < lbm::kQg; i++) q.g_sshift[i] = -q.g_shift[i] * q.g_scale[i];
-}
-
-void identity_quant(lbm::Quant &q, float eta)
-{
-    for (int a = 0; a < lbm::kQf - 1; a++) q.f_scale[a] = q.f_inv[a] = 1.f;
-    for (int i = 0; i < lbm::kQg; i++) {
-        q.g_scale[i] = q.g_inv[i] = 1.f;
-        q.g_shift[i] = 0.f;
-    }
-    finish_quant(q, eta);
+    q.f_scale = q.f_inv = q.g_scale = q.g_inv = 1.f;
+    for (int i = 0; i < lbm::kQg; i++) q.g_shift[i] = 0.f;
 }
 
 // Allocate a context and its buffers; the state is left uninitialised.
@@ -82,7 +68,7 @@ int create(lbm_ctx **out, const lbm_params *p)
         c->d.gravity = 0.f;
         c->d.grav = 0.f;
     }
-    identity_quant(c->q, c->d.eta);
+    identity_quant(c->q);
     c->esz = lbm::storage_bytes(p->storage);
     c->box.nx = p->nx;
     c->box.ny = p->ny;
@@ -129,7 +115,7 @@ int reduce_stats(lbm_ctx *c)
 // c->st.mom must already hold the fields (for the mean density).
 int load_state(lbm_ctx *c, const float *tf, const float *tg)
 {
-    identity_quant(c->q, c->d.eta);
+    identity_quant(c->q);
     if (c->p.storage != LBM_STORAGE_FP32) {
         int rc = reduce_stats(c);
         if (rc) return rc;
@@ -153,6 +139,8 @@ int load_state(lbm_ctx *c, const float *tf, const float *tg)
         // covers the flow developing later: |u| up to 0.1 moves g_i by about
         // 3 w_i rho |u| and f_i by about phiStar |u| / (tauPhi (1 - eta)).
         // BF16 has the FP32 exponent range and keeps scale 1.
+        // One scale per set, the smallest of its fields' (scaling by a power
+        // of two changes no rounding of normal FP16 numbers).
         const bool fp16 = c->p.storage == LBM_STORAGE_FP16;
         auto pick = [&](float maxabs, double bound) -> float {
             double m = std::max((double)maxabs, bound);
@@ -162,20 +150,22 @@ int load_state(lbm_ctx *c, const float *tf, const float *tg)
             return std::ldexp(1.f, ex);
         };
         const double fbound = 0.1 * std::fabs((double)c->d.phiStar) * c->d.invTauPhi * c->d.invEta2;
+        float fs = INFINITY, gs = INFINITY;
         for (int a = 0; a < lbm::kQf - 1; a++) {
             float m;
             std::memcpy(&m, &bits[a + 1], sizeof(float));
-            c->q.f_scale[a] = pick(m, fbound);
-            c->q.f_inv[a] = 1.f / c->q.f_scale[a];
+            fs = std::min(fs, pick(m, fbound));
         }
         for (int i = 0; i < lbm::kQg; i++) {
             float m;
             std::memcpy(&m, &bits[lbm::kQf + i], sizeof(float));
             c->q.g_shift[i] = shift[i];
-            c->q.g_scale[i] = pick(m, 0.3 * kW[i] * std::fabs(rho_mean));
-            c->q.g_inv[i] = 1.f / c->q.g_scale[i];
+            gs = std::min(gs, pick(m, 0.3 * kW[i] * std::fabs(rho_mean)));
         }
-        finish_quant(c->q, c->d.eta);
+        c->q.f_scale = fs;
+        c->q.f_inv = 1.f / fs;
+        c->q.g_scale = gs;
+        c->q.g_inv = 1.f / gs;
     }
     lbm::StepView v = view(c, 0);
     LBM_CUDA(lbm::launch_quantize(c->box, c->q, c->p.storage, tf, tg, c->st.f0, const_cast<void *>(v.fq_in),
@@ -484,6 +474,8 @@ extern "C" void lbm_destroy(lbm_ctx *c)
     cudaFree(c->partials);
     cudaFree(c->result);
     cudaFree(c->err);
+    cudaFree(c->adj_work);
+    cudaFree(c->adj_slots);
     if (c->result_host) cudaFreeHost(c->result_host);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;

@@ -33,16 +33,16 @@ struct Box {
     long long nxy, n;
 };
 
-// Per-field affine map of the 16-bit storage formats:
-//   stored = (value - shift) * scale,   value = stored * inv + shift.
-// scale is a power of two (exact); shift is w_i * mean(rho) for g and 0 for f.
-// For FP32 storage the map is the identity and is not applied.
+// Affine map of the 16-bit storage formats, one power-of-two scale per set:
+//   stored f_k = f_k * f_scale                   (k = 1..6; f_0 stays FP32)
+//   stored g_i = (g_i - g_shift[i]) * g_scale     (g_shift[i] = w_i * mean rho)
+// A power of two makes the map exact, and one scale per set lets the step
+// fold it into its collision constants.  For FP32 storage the map is the
+// identity and is not applied.
 struct Quant {
-    float f_scale[kQf - 1], f_inv[kQf - 1];          // f_1 .. f_6
-    float g_scale[kQg], g_inv[kQg], g_shift[kQg];
-    // derived, so that the step applies the map with one FMA per value:
-    float g_sshift[kQg];                             // -shift * scale (exact: scale is a power of two)
-    float f_eta[kQf - 1], f_eta2[kQf - 1];           // eta * f_inv, (1 - eta) * f_inv
+    float f_scale, f_inv;
+    float g_scale, g_inv;
+    float g_shift[kQg];
 };
 
 // Device buffers of one context (element type of fq and g: the storage type,
@@ -173,6 +173,13 @@ struct lbm_ctx {
     double *result = nullptr;      // stats result (device)
     double *result_host = nullptr; // pinned copy
     int *err = nullptr;            // device error flag of the kernels (0 = none)
+    // adjoint workspace, kept between lbm_step_adjoint / lbm_objective calls
+    // (freeing tens of GB costs ~0.4 ms per GB) until lbm_adjoint_release or
+    // lbm_destroy: the work buffers as one arena, and the checkpoint pool
+    void *adj_work = nullptr;
+    size_t adj_work_bytes = 0;
+    void *adj_slots = nullptr;
+    size_t adj_slot_bytes = 0;
 };
 
 namespace lbm {

@@ -102,7 +102,7 @@ __device__ __forceinline__ float g_streamed(const ST *__restrict__ g, unsigned n
 {
     const ST v = ODD ? g[kOpp(i) * n + dir_at(p, i, -1)] : g[i * n + p.at(0, 0, 0)];
     if constexpr (Fmt<ST>::kMapped)
-        return Fmt<ST>::load(v) * q.g_inv[i] + q.g_shift[i];
+        return Fmt<ST>::load(v) * q.g_inv + q.g_shift[i];
     else
         return Fmt<ST>::load(v);
 }
@@ -156,7 +156,7 @@ __global__ void __launch_bounds__(NTA) adjoint_phi_kernel(Box b, float eta, Quan
 #pragma unroll
         for (int i = 1; i < kQf; i++) {
             const ST *a = fq + (i - 1) * n;
-            const float inv = Fmt<ST>::kMapped ? q.f_inv[i - 1] : 1.f;
+            const float inv = Fmt<ST>::kMapped ? q.f_inv : 1.f;
             const float here = Fmt<ST>::load(a[t]) * inv;
             s += f_streamed ? here : eta * (Fmt<ST>::load(a[dir_at(p, i, -1)]) * inv) + eta2 * here;
         }
@@ -298,6 +298,40 @@ struct AdjIn {
     int objective, add_source;
 };
 
+// L2 prefetch of the block's tile rows of plane z in every field the local
+// kernel reads (lambda_g, lambda_f, lst, g, phi): one bulk prefetch per row
+// (128 B of floats, 32 storage elements of g), about 1.5 per thread.  The
+// kernel is latency-bound on its neighbour gathers; with the rows already on
+// their way to L2 they hit there.  The blocks of neighbouring tiles and planes
+// (which run at the same time) prefetch the halo rows.
+template <typename ST>
+__device__ __forceinline__ void prefetch_plane(const Box &b, const AdjIn &a, int z)
+{
+    constexpr int kFields = kQg + kQf + 1 + kQg + 1;
+    const unsigned n = (unsigned)b.n;
+    const int tid = threadIdx.y * TXA + threadIdx.x;
+    for (int r = tid; r < kFields * TYA; r += NTA) {
+        const int field = r / TYA;
+        const unsigned node =
+            (unsigned)z * (unsigned)b.nxy + (blockIdx.y * TYA + (unsigned)(r % TYA)) * (unsigned)b.nx + blockIdx.x * TXA;
+        const void *src;
+        unsigned bytes = TXA * sizeof(float);
+        if (field < kQg) {
+            src = a.lg + field * n + node;
+        } else if (field < kQg + kQf) {
+            src = a.lf + (field - kQg) * n + node;
+        } else if (field == kQg + kQf) {
+            src = a.lst + node;
+        } else if (field < 2 * kQg + kQf + 1) {
+            src = static_cast<const ST *>(a.g) + (field - kQg - kQf - 1) * n + node;
+            bytes = TXA * sizeof(ST);
+        } else {
+            src = a.phi + node;
+        }
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;\n" ::"l"(src), "r"(bytes) : "memory");
+    }
+}
+
 // The local part of one adjoint step (see the file comment).
 template <typename ST, bool ODD>
 __global__ void __launch_bounds__(NTA, ZSC_ADJ_MIN_BLOCKS) adjoint_local_kernel(Box b, StepConst c, float phiStar, Quant q, AdjIn a)
@@ -307,7 +341,9 @@ __global__ void __launch_bounds__(NTA, ZSC_ADJ_MIN_BLOCKS) adjoint_local_kernel(
     const ST *__restrict__ g = static_cast<const ST *>(a.g);
     double dg = 0.0;
     const int x = blockIdx.x * TXA + threadIdx.x, y = blockIdx.y * TYA + threadIdx.y;
+    if (blockIdx.z < (unsigned)b.nz) prefetch_plane<ST>(b, a, blockIdx.z);
     for (int z = blockIdx.z; z < b.nz; z += gridDim.z) {
+        if (z + (int)gridDim.z < b.nz) prefetch_plane<ST>(b, a, z + gridDim.z);
         const Nb p = neighbourhood(b, x, y, z);
         const unsigned t = p.at(0, 0, 0);
         float lap, gr[3];

@@ -63,7 +63,7 @@ __global__ void stream_out_kernel(Box b, float eta, Quant q, const float *__rest
         if (fo) {
             fo[t] = f0[t];
             for (int i = 1; i < kQf; i++) {
-                const float inv = q.f_inv[i - 1];
+                const float inv = q.f_inv;
                 const ST *a = fq + (i - 1) * b.n;
                 if (f_streamed) {
                     fo[i * b.n + t] = to_f(a[t]) * inv;
@@ -82,7 +82,7 @@ __global__ void stream_out_kernel(Box b, float eta, Quant q, const float *__rest
                     const long long up = shifted(b, x, y, z, -kCg[i][0], -kCg[i][1], -kCg[i][2]);
                     v = to_f(g[kOpp[i] * b.n + up]);
                 }
-                go[i * b.n + t] = v * q.g_inv[i] + q.g_shift[i];
+                go[i * b.n + t] = v * q.g_inv + q.g_shift[i];
             }
         }
     }
@@ -95,8 +95,8 @@ __global__ void quantize_kernel(Box b, Quant q, const float *__restrict__ f, con
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < b.n;
          t += (long long)gridDim.x * blockDim.x) {
         f0[t] = f[t];
-        for (int i = 1; i < kQf; i++) fq[(i - 1) * b.n + t] = from_f<ST>(f[i * b.n + t] * q.f_scale[i - 1]);
-        for (int i = 0; i < kQg; i++) gq[i * b.n + t] = from_f<ST>((g[i * b.n + t] - q.g_shift[i]) * q.g_scale[i]);
+        for (int i = 1; i < kQf; i++) fq[(i - 1) * b.n + t] = from_f<ST>(f[i * b.n + t] * q.f_scale);
+        for (int i = 0; i < kQg; i++) gq[i * b.n + t] = from_f<ST>((g[i * b.n + t] - q.g_shift[i]) * q.g_scale);
     }
 }
 

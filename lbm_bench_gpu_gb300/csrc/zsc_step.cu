@@ -222,12 +222,51 @@ __device__ __forceinline__ void for_dirs_from(F &&f)
     }
 }
 
+// The 16-bit storage map folded into the step's constants.  The step works on
+// stored values: a stored f_k is f_k f_scale, so phi = f_0 + f_inv sum_k f_k
+// and the outputs f_scale P_k come from f_scale-scaled collision terms; a
+// stored g_i is (g_i - shift_i) g_scale, so rho = g_inv sum_i s_i + sum_i
+// shift_i (the shifts cancel in the momentum's opposite-pair differences),
+// and with bb = 1 - 1/tauRho the stored output is
+//   (bb g_i + eq_i - shift_i) g_scale = bb s_i + g_scale eq_i + (bb - 1) shift_i g_scale,
+// i.e. the FP32 collision with g_scale-scaled constants plus one constant per
+// weight class (g_scale g_inv = 1 exactly: both are powers of two).
+struct StepMap {
+    float f_inv, Af, Cf;                  // f_inv; f_scale Gamma / (2 tauPhi); f_scale invTauPhi invEta2
+    float g_inv, rho_shift;               // g_inv; sum of the shifts
+    float K0, K1, K2, KC0, KC1, KC2;      // g_scale x the collision constants
+    float k0, k1, k2;                     // (bb - 1) shift g_scale: rest, face, edge classes
+};
+
+StepMap step_map(const StepConst &c, const Quant &q)
+{
+    StepMap m;
+    m.f_inv = q.f_inv;
+    m.Af = 0.5f * c.Gamma * c.invTauPhi * q.f_scale;
+    m.Cf = c.invTauPhi * c.invEta2 * q.f_scale;
+    m.g_inv = q.g_inv;
+    float rs = 0.f;
+    for (int i = 0; i < kQg; i++) rs += q.g_shift[i];
+    m.rho_shift = rs;
+    m.K0 = c.K0 * q.g_scale;
+    m.K1 = c.K1 * q.g_scale;
+    m.K2 = c.K2 * q.g_scale;
+    m.KC0 = c.KC0 * q.g_scale;
+    m.KC1 = c.KC1 * q.g_scale;
+    m.KC2 = c.KC2 * q.g_scale;
+    const float bm1 = c.invTauRhoOne - 1.f;
+    m.k0 = bm1 * q.g_shift[0] * q.g_scale;
+    m.k1 = bm1 * q.g_shift[1] * q.g_scale;
+    m.k2 = bm1 * q.g_shift[7] * q.g_scale;
+    return m;
+}
+
 // TMA: the g rows come by tensor copies (gmap): even steps one copy per plane
 // in the dense layout [field][TY][TX]; odd steps, on interior tiles, one copy
 // per direction into the [dir][TY][W] rows.  Without TMA gmap is unused.
 template <typename ST, bool STREAMED, bool ODD, bool TMA>
 __global__ void __launch_bounds__(NT, Fmt<ST>::kMinBlocks)
-zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Quant q, const int tz,
+zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const StepMap m, const int tz,
                 const int write_moments, const __grid_constant__ CUtensorMap gmap,
                 const __grid_constant__ CUtensorMap f0map, const __grid_constant__ CUtensorMap fqmap)
 {
@@ -435,8 +474,8 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Quan
         }
     };
 
-    // Streamed D3Q7 values at ring-tile position (lx, ly) of plane p and their
-    // sum phi (src/update_phi.cu:42-43), from the staged planes.
+    // Streamed D3Q7 values at ring-tile position (lx, ly) of plane p (f_1..f_6
+    // in stored units) and phi (src/update_phi.cu:42-43), from the staged planes.
     auto phi_at = [&](int p, int lx, int ly, float(&f)[kQf]) -> float {
         const int row = ly + 1;
         const int c0 = lx + 3;          // f_0 column: x - (x0 - 4)
@@ -445,22 +484,14 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Quan
         auto raw = [&](unsigned char *S, int a, int rr, int cc) {
             return Fm::load(fqpart(S)[(a * FR + rr) * W + cc]);
         };
-        auto fq = [&](unsigned char *S, int a, int rr, int cc) {
-            const float v = raw(S, a, rr, cc);
-            if constexpr (Fm::kMapped) return v * q.f_inv[a]; else return v;
-        };
-        // eta P(x - c) + (1 - eta) P(x); 16-bit storage folds the map's 1/scale
-        // into the two weights
+        // eta P(x - c) + (1 - eta) P(x), in stored units
         auto blend = [&](unsigned char *Su, int a, int ru, int cu) {
-            if constexpr (Fm::kMapped)
-                return q.f_eta[a] * raw(Su, a, ru, cu) + q.f_eta2[a] * raw(S1, a, row, cq);
-            else
-                return c.eta * raw(Su, a, ru, cu) + c.eta2 * raw(S1, a, row, cq);
+            return c.eta * raw(Su, a, ru, cu) + c.eta2 * raw(S1, a, row, cq);
         };
         f[0] = f0part(S1)[row * W0 + c0];
         if (STREAMED) {
 #pragma unroll
-            for (int a = 0; a < kQf - 1; a++) f[a + 1] = fq(S1, a, row, cq);
+            for (int a = 0; a < kQf - 1; a++) f[a + 1] = raw(S1, a, row, cq);
         } else {
             unsigned char *S0 = fstage(p - 1), *S2 = fstage(p + 1);
             f[1] = blend(S1, 0, row, cq - 1);
@@ -470,7 +501,8 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Quan
             f[5] = blend(S0, 4, row, cq);
             f[6] = blend(S2, 5, row, cq);
         }
-        return f[0] + f[1] + f[2] + f[3] + f[4] + f[5] + f[6];
+        if constexpr (Fm::kMapped) return fmaf(m.f_inv, f[1] + f[2] + f[3] + f[4] + f[5] + f[6], f[0]);
+        else return f[0] + f[1] + f[2] + f[3] + f[4] + f[5] + f[6];
     };
 
     // phi of plane p on the tile + ring into phi slot s; the streamed f of the
@@ -573,27 +605,29 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Quan
         float Fz = mu12 * (2.f * (pt - pb) + d_et - d_eb + d_nt - d_nb);
         if (pc > 0.f) Fz += c.grav;
 
-        // D3Q19 values of this node from the staged rows (AA pattern)
+        // D3Q19 values of this node from the staged rows (AA pattern), in
+        // stored units
         const ST *Gs = G + (j & 1) * G_ELEMS;
         float g[kQg];
 #pragma unroll
-        for (int i = 0; i < kQg; i++) {
-            const float v = Fm::load((TMA && !ODD) ? Gs[(i * TY + ty) * TX + tx]
-                                                   : Gs[(i * TY + ty) * W + E + tx - (ODD ? kCx(i) : 0)]);
-            if constexpr (Fm::kMapped) g[i] = v * q.g_inv[i] + q.g_shift[i]; else g[i] = v;
-        }
+        for (int i = 0; i < kQg; i++)
+            g[i] = Fm::load((TMA && !ODD) ? Gs[(i * TY + ty) * TX + tx]
+                                          : Gs[(i * TY + ty) * W + E + tx - (ODD ? kCx(i) : 0)]);
 
         // moments: src/update_rho.cu:46-50, src/update_velocity.cu:47-59
         float rho = g[0];
 #pragma unroll
         for (int i = 1; i < kQg; i++) rho += g[i];
+        if constexpr (Fm::kMapped) rho = fmaf(m.g_inv, rho, m.rho_shift);
         const float invRho = 1.0f / rho;
+        float invRhoG = invRho;   // 1 / rho on physical momentum differences
+        if constexpr (Fm::kMapped) invRhoG = invRho * m.g_inv;
         // momentum from the pair differences each component shares
         const float d7 = g[7] - g[8], d9 = g[9] - g[10], d11 = g[11] - g[12], d13 = g[13] - g[14];
         const float d15 = g[15] - g[16], d17 = g[17] - g[18];
-        const float ux = ((g[1] - g[2]) + d7 + d9 + d11 + d13) * invRho;
-        const float uy = ((g[3] - g[4]) + d7 - d9 + d15 + d17) * invRho;
-        const float uz = ((g[5] - g[6]) + d11 - d13 + d15 - d17) * invRho;
+        const float ux = ((g[1] - g[2]) + d7 + d9 + d11 + d13) * invRhoG;
+        const float uy = ((g[3] - g[4]) + d7 - d9 + d15 + d17) * invRhoG;
+        const float uz = ((g[5] - g[6]) + d11 - d13 + d15 - d17) * invRhoG;
         const unsigned id = node_index(b, x, y, z);
         if (write_moments) {
             P.mom[0][id] = pc;
@@ -611,35 +645,38 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Quan
         // D3Q7 collision, src/collision_f.cu:105-114 (A/B store)
         {
             const float Af = 0.5f * c.Gamma * c.invTauPhi * mu;
-            const float Cf = c.invTauPhi * c.invEta2 * pc;
             const float a = c.invTauPhiOne;
-            auto put = [&](int k, float v) {
-                if constexpr (Fm::kMapped) P.fout[k][id] = Fm::store(v * q.f_scale[k]);
-                else P.fout[k][id] = v;
-            };
             P.f0out[id] = a * fcur[0] - 6.0f * Af + c.invTauPhi * pc;
-            put(0, a * fcur[1] + Af + Cf * usx);
-            put(1, a * fcur[2] + Af - Cf * usx);
-            put(2, a * fcur[3] + Af + Cf * usy);
-            put(3, a * fcur[4] + Af - Cf * usy);
-            put(4, a * fcur[5] + Af + Cf * usz);
-            put(5, a * fcur[6] + Af - Cf * usz);
+            // f_1..f_6 in stored units: terms scaled by f_scale
+            const float Afk = Fm::kMapped ? m.Af * mu : Af;
+            const float Cf = (Fm::kMapped ? m.Cf : c.invTauPhi * c.invEta2) * pc;
+            auto put = [&](int k, float v) { P.fout[k][id] = Fm::store(v); };
+            put(0, a * fcur[1] + Afk + Cf * usx);
+            put(1, a * fcur[2] + Afk - Cf * usx);
+            put(2, a * fcur[3] + Afk + Cf * usy);
+            put(3, a * fcur[4] + Afk - Cf * usy);
+            put(4, a * fcur[5] + Afk + Cf * usz);
+            put(5, a * fcur[6] + Afk - Cf * usz);
         }
 
-        // D3Q19 collision with forcing, src/collision_g.cu:111-196
+        // D3Q19 collision with forcing, src/collision_g.cu:111-196; in stored
+        // units for 16-bit storage (StepMap)
         {
+            constexpr bool M = Fm::kMapped;
             const float bb = c.invTauRhoOne;
-            const float K1 = c.K1, K2 = c.K2, KC1 = c.KC1, KC2 = c.KC2;
+            const float K1 = M ? m.K1 : c.K1, K2 = M ? m.K2 : c.K2, KC1 = M ? m.KC1 : c.KC1, KC2 = M ? m.KC2 : c.KC2;
             const float phimu3 = 3.f * pc * mu;
             const float temp1 = K1 * (phimu3 + rho * (1.f - 1.5f * (usx * usx + usy * usy + usz * usz)));
             const float UF = usx * Fx + usy * Fy + usz * Fz;
             const float vx = usx * 3.f, vy = usy * 3.f, vz = usz * 3.f;
             const float vsq6 = (vx * vx + vy * vy + vz * vz) * kInv6;
             float qv[kQg];
-            qv[0] = bb * g[0] + c.K0 * (rho - 6.f * pc * mu - rho * vsq6) - c.KC0 * UF;
+            qv[0] = bb * g[0] + (M ? m.K0 : c.K0) * (rho - 6.f * pc * mu - rho * vsq6) - (M ? m.KC0 : c.KC0) * UF;
+            if constexpr (M) qv[0] += m.k0;
             {
                 const float K1r = K1 * rho, hK1r = 0.5f * K1r;
-                const float t1 = temp1 - KC1 * UF;
+                float t1 = temp1 - KC1 * UF;
+                if constexpr (M) t1 += m.k1;
                 float eq1 = t1 + hK1r * vx * vx + KC1 * (vx * Fx);
                 float eq2 = vx * (K1r + KC1 * Fx);
                 qv[1] = bb * g[1] + eq1 + eq2;
@@ -655,7 +692,8 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Quan
             }
             {
                 const float K2r = K2 * rho, hK2r = 0.5f * K2r;
-                const float t2 = K2 * (phimu3 + rho * (1.f - vsq6)) - KC2 * UF;
+                float t2 = K2 * (phimu3 + rho * (1.f - vsq6)) - KC2 * UF;
+                if constexpr (M) t2 += m.k2;
                 auto pair = [&](float w, float Gf, int ip, int im) {
                     const float eq1 = t2 + hK2r * w * w + KC2 * (w * Gf);
                     const float eq2 = K2r * w + KC2 * Gf;
@@ -669,10 +707,7 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Quan
                 pair(vy + vz, Fy + Fz, 15, 16);
                 pair(vy - vz, Fy - Fz, 17, 18);
             }
-            auto enc = [&](int i, float v) -> ST {
-                if constexpr (Fm::kMapped) return Fm::store(fmaf(v, q.g_scale[i], q.g_sshift[i]));
-                else return v;
-            };
+            auto enc = [&](int, float v) -> ST { return Fm::store(v); };
             if (!ODD) {
                 // even: own node, reversed slots
 #pragma unroll
@@ -817,6 +852,7 @@ template <typename ST>
 cudaError_t launch_typed(const Box &b, const StepConst &c, const Quant &q, const StepView &v, bool f_streamed,
                          bool odd, bool write_moments, cudaStream_t s)
 {
+    const StepMap m = step_map(c, q);
     StepPtrs<ST> P;
     P.f0in = v.f0_in;
     P.f0out = v.f0_out;
@@ -860,18 +896,18 @@ cudaError_t launch_typed(const Box &b, const StepConst &c, const Quant &q, const
     if (f_streamed) {
         if (odd) return cudaErrorInvalidValue;  // the streamed initial state is always read by an even step
         if (tma)
-            zsc_step_kernel<ST, true, false, true><<<nblocks, block, smem, s>>>(P, b, c, q, tz, wm, gmap, f0map, fqmap);
+            zsc_step_kernel<ST, true, false, true><<<nblocks, block, smem, s>>>(P, b, c, m, tz, wm, gmap, f0map, fqmap);
         else
-            zsc_step_kernel<ST, true, false, false><<<nblocks, block, smem, s>>>(P, b, c, q, tz, wm, gmap, f0map, fqmap);
+            zsc_step_kernel<ST, true, false, false><<<nblocks, block, smem, s>>>(P, b, c, m, tz, wm, gmap, f0map, fqmap);
     } else if (odd) {
         if (tma)
-            zsc_step_kernel<ST, false, true, true><<<nblocks, block, smem, s>>>(P, b, c, q, tz, wm, gmap, f0map, fqmap);
+            zsc_step_kernel<ST, false, true, true><<<nblocks, block, smem, s>>>(P, b, c, m, tz, wm, gmap, f0map, fqmap);
         else
-            zsc_step_kernel<ST, false, true, false><<<nblocks, block, smem, s>>>(P, b, c, q, tz, wm, gmap, f0map, fqmap);
+            zsc_step_kernel<ST, false, true, false><<<nblocks, block, smem, s>>>(P, b, c, m, tz, wm, gmap, f0map, fqmap);
     } else if (tma) {
-        zsc_step_kernel<ST, false, false, true><<<nblocks, block, smem, s>>>(P, b, c, q, tz, wm, gmap, f0map, fqmap);
+        zsc_step_kernel<ST, false, false, true><<<nblocks, block, smem, s>>>(P, b, c, m, tz, wm, gmap, f0map, fqmap);
     } else {
-        zsc_step_kernel<ST, false, false, false><<<nblocks, block, smem, s>>>(P, b, c, q, tz, wm, gmap, f0map, fqmap);
+        zsc_step_kernel<ST, false, false, false><<<nblocks, block, smem, s>>>(P, b, c, m, tz, wm, gmap, f0map, fqmap);
     }
     return cudaGetLastError();
 }

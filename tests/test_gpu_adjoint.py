@@ -86,3 +86,32 @@ def test_objective_alone_matches_adjoint_J(lib):
         assert lat.steps == 0
     assert J == pytest.approx(r["J"], rel=1e-14)
     assert fd == pytest.approx(r["dJ_dgrav"], rel=5e-3)
+
+
+def test_workspace_is_kept_between_calls_and_released(lib):
+    """The context keeps the adjoint workspace and checkpoint pool: a call with
+    a smaller budget after a larger one reuses the larger pool and gives the
+    same results as on a fresh pool; lbm_adjoint_release returns the memory."""
+    import torch
+    from lbm_bench_gpu_gb300 import capi
+    phi0, rho0 = fields()
+    p = capi.make_params(32, 32, 16, **KW)
+    snap = 26 * 4 * 32 * 32 * 16
+    with capi.Lattice.from_fields(p, phi0.astype(np.float32), rho0.astype(np.float32)) as lat:
+        tight = lat.adjoint(20, -3e-5, "light_uz_mean", 6, checkpoint_bytes=3.5 * snap)
+        full = lat.adjoint(20, -3e-5, "light_uz_mean", 6)
+        held = torch.cuda.mem_get_info()[0]
+        again = lat.adjoint(20, -3e-5, "light_uz_mean", 6, checkpoint_bytes=3.5 * snap)
+        assert torch.cuda.mem_get_info()[0] == held     # nothing allocated
+        J = lat.objective(20, -3e-5, "light_uz_mean", 6)
+        assert torch.cuda.mem_get_info()[0] == held
+        lat.adjoint_release()
+        assert torch.cuda.mem_get_info()[0] - held >= 21 * snap
+        after = lat.adjoint(20, -3e-5, "light_uz_mean", 6, checkpoint_bytes=3.5 * snap)
+        assert lat.steps == 0
+    assert tight["slots"] == again["slots"] == after["slots"] == 3 and full["slots"] == 21
+    for r in (again, after):
+        assert r["forward_steps"] == tight["forward_steps"]
+        assert r["J"] == tight["J"] and r["dJ_dgrav"] == tight["dJ_dgrav"]
+        assert np.array_equal(r["dJ_dphi0"], tight["dJ_dphi0"])
+    assert J == pytest.approx(tight["J"], rel=1e-14)
