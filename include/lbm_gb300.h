@@ -262,8 +262,18 @@ long long lbm_steps_done(const lbm_ctx *c);
  * work around lbm_step. */
 void *lbm_stream(const lbm_ctx *c);
 
-/* Wait for all work queued on the context. */
+/* Wait for all work queued on the context.  LBM_ETIMEOUT if a step kernel gave
+ * up one of its bounded waits for staged data (the step's results are then
+ * not valid; the context's error flag stays set). */
 int lbm_sync(lbm_ctx *c);
+
+/* Failure-path self-test, no counterpart in the reference: one block waits,
+ * with the step kernel's bounded wait, on a barrier that nothing completes; the
+ * wait gives up, sets the context's error flag, and the error reaches the host
+ * as it would from a step.  Returns LBM_ETIMEOUT (the expected outcome) after
+ * clearing the flag, so the context stays usable; LBM_ESTATE if the wait did
+ * not give up.  Synchronises. */
+int lbm_wait_selftest(lbm_ctx *c);
 
 /* Release the context and all its device memory.  NULL is a no-op. */
 void lbm_destroy(lbm_ctx *c);

@@ -24,6 +24,7 @@ EXPORTS = [
     "lbm_get_dist", "lbm_set_dist", "lbm_steps_done", "lbm_stream", "lbm_sync", "lbm_destroy",
     "lbm_strerror", "lbm_last_error", "lbm_stats_noalloc", "lbm_step_adjoint",
     "lbm_objective", "lbm_stats_fields", "lbm_pressure", "lbm_device_name", "lbm_adjoint_release",
+    "lbm_wait_selftest",
 ]
 OBJECTIVES = {"light_uz_mean": 0, "light_z_centroid": 1}
 
@@ -110,6 +111,7 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.lbm_step_adjoint.argtypes = [C.c_void_p, C.POINTER(AdjointOpts), C.POINTER(AdjointOut)]
     lib.lbm_objective.argtypes = [C.c_void_p, C.POINTER(AdjointOpts), C.POINTER(C.c_double)]
     lib.lbm_adjoint_release.argtypes = [C.c_void_p]
+    lib.lbm_wait_selftest.argtypes = [C.c_void_p]
     lib.lbm_stats_fields.argtypes = [C.c_void_p, C.POINTER(StatsOut), _F, _F, _F, _F, _F]
     lib.lbm_pressure.argtypes = [C.c_void_p, _F]
     lib.lbm_device_name.argtypes = [C.c_int, C.c_char_p, C.c_int, C.POINTER(C.c_double)]
@@ -265,6 +267,10 @@ class Lattice:
         J = C.c_double()
         check(load().lbm_objective(self._h, C.byref(o), C.byref(J)), "lbm_objective")
         return float(J.value)
+
+    def wait_selftest(self) -> int:
+        """lbm_wait_selftest: the status code a timed-out bounded wait reports (LBM_ETIMEOUT)."""
+        return int(load().lbm_wait_selftest(self._h))
 
     def adjoint_release(self) -> None:
         """lbm_adjoint_release: free the adjoint workspace and checkpoint pool kept in the context."""

@@ -462,6 +462,20 @@ extern "C" int lbm_sync(lbm_ctx *c)
     return device_error(c);
 }
 
+extern "C" int lbm_wait_selftest(lbm_ctx *c)
+{
+    if (!c) return fail(LBM_EINVAL, "context is NULL");
+    LBM_CUDA(cudaSetDevice(c->p.device), "cudaSetDevice");
+    if (int rc = lbm_sync(c)) return rc;
+    LBM_CUDA(lbm::launch_wait_selftest(c->err, c->stream), "wait self-test launch");
+    LBM_CUDA(cudaStreamSynchronize(c->stream), "wait self-test");
+    const int rc = device_error(c);
+    LBM_CUDA(cudaMemsetAsync(c->err, 0, sizeof(int), c->stream), "clear error flag");
+    LBM_CUDA(cudaStreamSynchronize(c->stream), "clear error flag");
+    if (rc == LBM_OK) return fail(LBM_ESTATE, "lbm_wait_selftest: the bounded wait did not give up");
+    return rc;
+}
+
 extern "C" void lbm_destroy(lbm_ctx *c)
 {
     if (!c) return;

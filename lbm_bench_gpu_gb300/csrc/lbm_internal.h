@@ -117,6 +117,8 @@ cudaError_t launch_equilibrium(const Box &b, const lbm_derived &d, float Gamma, 
 cudaError_t launch_fill(float *p, long long n, float v, cudaStream_t s);
 cudaError_t launch_step(const Box &b, const StepConst &c, const Quant &q, const StepView &v, bool f_streamed,
                         bool odd, bool write_moments, cudaStream_t s);
+// One block whose bounded mbarrier wait gives up and sets *err (the step's wait).
+cudaError_t launch_wait_selftest(int *err, cudaStream_t s);
 // State (post-collision / AA layout, any storage) -> streamed FP32 f (7 x n) and g (19 x n).
 cudaError_t launch_stream_out(const Box &b, float eta, const Quant &q, const StepView &v, bool f_streamed, bool odd,
                               float *f_out, float *g_out, cudaStream_t s);

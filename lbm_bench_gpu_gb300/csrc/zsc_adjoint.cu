@@ -29,11 +29,15 @@
 //   adjoint_stencil_kernel float4 -> lst                        ~20 B/node
 // All per-node arithmetic is FP32; the objective sums and dJ/dgrav are FP64.
 // Every kernel runs on one grid: 32 x 8 column tiles, each block marching
-// kPlanes consecutive z planes (so the z neighbours of one plane are the
+// kPlanes (4) consecutive z planes (so the z neighbours of one plane are the
 // block's previous and next planes, mostly L1 hits), except the local kernel,
-// whose blocks take planes gridDim.z apart (with consecutive planes the
-// compiler keeps more values live across iterations and spills; measured 1%
-// slower).  32-bit node indices (n * 19 < 2^32 is checked at init).
+// whose blocks take kLocalPlanes (2) planes gridDim.z apart (with consecutive
+// planes the compiler keeps more values live across iterations and spills),
+// with the next plane's rows prefetched into L2.  Measured at 128^3 (T = 2000,
+// 40 GB): 1, 2, 4 local planes -> adjoint/forward 4.06, 3.99, 4.09; 8 and 16
+// stencil planes are slower.  32-bit node indices (n * 19 < 2^32 is checked at
+// init).
+#include <algorithm>
 #include <type_traits>
 
 #include "lattice.cuh"
@@ -48,7 +52,11 @@ constexpr int TXA = 32, TYA = 8, NTA = TXA * TYA;
 #ifndef ZSC_ADJ_MIN_BLOCKS
 #define ZSC_ADJ_MIN_BLOCKS 3
 #endif
+#ifndef ZSC_ADJ_LOCAL_PLANES
+#define ZSC_ADJ_LOCAL_PLANES 2
+#endif
 constexpr int kPlanes = ZSC_ADJ_PLANES;
+constexpr int kLocalPlanes = ZSC_ADJ_LOCAL_PLANES;   // planes per block of the local kernel
 constexpr float kInv6 = 0.16666666666666666667f;
 constexpr float kInv12 = 0.08333333333333333333f;
 constexpr float kW0 = 0.33333333333333333333f, kW1 = 0.05555555555555555556f, kW2 = 0.02777777777777777778f;
@@ -605,6 +613,14 @@ dim3 adjoint_grid(const Box &b)
     return dim3((unsigned)(b.nx / TXA), (unsigned)(b.ny / TYA), (unsigned)((b.nz + kPlanes - 1) / kPlanes));
 }
 
+// the local kernel's grid (its blocks take planes gridDim.z apart)
+dim3 local_grid(const Box &b)
+{
+    return dim3((unsigned)(b.nx / TXA), (unsigned)(b.ny / TYA), (unsigned)((b.nz + kLocalPlanes - 1) / kLocalPlanes));
+}
+
+size_t blocks_of(const dim3 &g) { return (size_t)g.x * g.y * g.z; }
+
 const dim3 kBlock(TXA, TYA);
 
 // fn(ST{}, std::integral_constant<bool, ODD>{}) for the state's storage type and g layout.
@@ -624,8 +640,7 @@ cudaError_t dispatch(const NativeState &st, Fn &&fn)
 
 size_t adjoint_blocks(const Box &b)
 {
-    const dim3 g = adjoint_grid(b);
-    return (size_t)g.x * g.y * g.z;
+    return std::max(blocks_of(adjoint_grid(b)), blocks_of(local_grid(b)));
 }
 
 cudaError_t launch_adjoint_phi(const Box &b, float eta, const Quant &q, const NativeState &st, float *phi,
@@ -652,7 +667,7 @@ cudaError_t launch_objective(const Box &b, int objective, float phiStar, double 
         return cudaGetLastError();
     });
     if (e != cudaSuccess) return e;
-    objective_fold_kernel<<<1, kBlock, 0, s>>>(partials, (int)adjoint_blocks(b), scale, ab, acc);
+    objective_fold_kernel<<<1, kBlock, 0, s>>>(partials, (int)blocks_of(adjoint_grid(b)), scale, ab, acc);
     return cudaGetLastError();
 }
 
@@ -688,7 +703,7 @@ cudaError_t launch_adjoint_step(const Box &b, const StepConst &c, float phiStar,
     in.add_source = add_source ? 1 : 0;
     cudaError_t e = dispatch(st, [&](auto tag, auto odd) {
         adjoint_local_kernel<decltype(tag), decltype(odd)::value>
-            <<<adjoint_grid(b), kBlock, 0, s>>>(b, c, phiStar, q, in);
+            <<<local_grid(b), kBlock, 0, s>>>(b, c, phiStar, q, in);
         return cudaGetLastError();
     });
     if (e != cudaSuccess) return e;
@@ -698,7 +713,7 @@ cudaError_t launch_adjoint_step(const Box &b, const StepConst &c, float phiStar,
 
 cudaError_t launch_dgrav_fold(const Box &b, const double *dgrav, double *acc, cudaStream_t s)
 {
-    dgrav_fold_kernel<<<1, kBlock, 0, s>>>(dgrav, (int)adjoint_blocks(b), acc);
+    dgrav_fold_kernel<<<1, kBlock, 0, s>>>(dgrav, (int)blocks_of(local_grid(b)), acc);
     return cudaGetLastError();
 }
 

@@ -185,11 +185,26 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned phase)
 // Bounded wait for phase `phase` of an mbarrier: false after kWaitLimit polls
 // (each poll may suspend the thread for a hardware-defined time).
 constexpr unsigned kWaitLimit = 1u << 22;
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned phase)
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned phase, unsigned limit = kWaitLimit)
 {
-    for (unsigned it = 0; it < kWaitLimit; ++it)
+    for (unsigned it = 0; it < limit; ++it)
         if (mbar_try_wait(bar, phase)) return true;
     return false;
+}
+
+// One warp waits, bounded, on a fresh mbarrier that nothing arrives at (no
+// copy is issued against it, so nothing is in flight when the block exits):
+// the wait gives up and the error flag is set as in the step kernel.
+__global__ void wait_selftest_kernel(int *err, unsigned limit)
+{
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        mbar_init_fence();
+    }
+    __syncthreads();
+    const bool done = mbar_wait(&bar, 0, limit);
+    if (__syncthreads_or(!done) && threadIdx.x == 0) atomicOr(err, 1);
 }
 // Order this thread's earlier generic-proxy shared-memory accesses (made
 // visible to it by a barrier) before a following TMA write to the same bytes.
@@ -913,6 +928,12 @@ cudaError_t launch_typed(const Box &b, const StepConst &c, const Quant &q, const
 }
 
 }  // namespace
+
+cudaError_t launch_wait_selftest(int *err, cudaStream_t s)
+{
+    wait_selftest_kernel<<<1, 32, 0, s>>>(err, 1u << 14);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_step(const Box &b, const StepConst &c, const Quant &q, const StepView &v, bool f_streamed,
                         bool odd, bool write_moments, cudaStream_t s)

@@ -201,6 +201,22 @@ def test_nan_is_reported(lib):
         assert s["nonfinite"] > 0
 
 
+def test_timed_out_wait_is_reported_and_context_stays_usable(lib):
+    """Failure detection on the device without a fault: a bounded wait on a
+    barrier that nothing completes gives up (the step kernel's wait and error
+    flag), the host reads LBM_ETIMEOUT, and the same context then steps and
+    matches the oracle."""
+    from lbm_bench_gpu_gb300 import capi
+    p = make(32, 32, 32)
+    with capi.Lattice.from_bubbles(p, BUB32) as lat:
+        assert lat.wait_selftest() == capi.LBM_ETIMEOUT
+        lat.sync()                                    # the flag was cleared
+        lat.step(3, -2e-5)
+        o = oracle_for(p, BUB32)
+        o.step(3, -2e-5)
+        assert_fields_close(lat.fields(), o.moments(), what="after the self-test")
+
+
 def test_full_size_conservation(lib):
     """256^3, 64 bubbles (the bench workload): sum phi and sum rho stay put."""
     from lbm_bench_gpu_gb300 import capi, inputs
