@@ -45,15 +45,30 @@ template <>
 struct Fmt<__half> {
     static constexpr int kMinBlocks = 3;
     static constexpr bool kMapped = true;
+    using T2 = __half2;   // two adjacent nodes, one 32-bit word
     __device__ static float load(__half v) { return __half2float(v); }
     __device__ static __half store(float v) { return __float2half_rn(v); }
+    __device__ static float2 load2(__half2 v) { return __half22float2(v); }
+    __device__ static __half2 store2(float2 v) { return __float22half2_rn(v); }
 };
 template <>
 struct Fmt<__nv_bfloat16> {
     static constexpr int kMinBlocks = 3;
     static constexpr bool kMapped = true;
+    using T2 = __nv_bfloat162;
     __device__ static float load(__nv_bfloat16 v) { return __bfloat162float(v); }
     __device__ static __nv_bfloat16 store(float v) { return __float2bfloat16_rn(v); }
+    __device__ static float2 load2(__nv_bfloat162 v) { return __bfloat1622float2(v); }
+    __device__ static __nv_bfloat162 store2(float2 v) { return __float22bfloat162_rn(v); }
 };
+
+// Packed FP32 (f32x2): two lanes per instruction, each rounded as FP32.
+namespace pk {
+__device__ __forceinline__ float2 splat(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 add(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 sub(float2 a, float2 b) { return __ffma2_rn(b, splat(-1.f), a); }
+}  // namespace pk
 
 }  // namespace lbm

@@ -78,6 +78,18 @@ static_assert(TX == 32 && TY == 8, "issuer roles assume a 32 x 8 tile");
 
 constexpr float kInv6 = 0.16666666666666666667f;
 
+// 16-bit storage: two adjacent x nodes per thread (128 threads per 32 x 8
+// tile), all FP32 arithmetic in packed f32x2 pairs (node A in .x, node B in .y),
+// both nodes' 16-bit values converted and stored as one 32-bit word.
+#ifndef ZSC_PAIR
+#define ZSC_PAIR 1
+#endif
+constexpr bool kUsePair = ZSC_PAIR != 0;
+template <typename ST>
+constexpr bool use_pair() { return kUsePair && sizeof(ST) == 2; }
+template <typename ST>
+constexpr int threads_of() { return use_pair<ST>() ? NT / 2 : NT; }
+
 // Packed FP32 (f32x2: two lanes per instruction, each rounded as FP32) in the
 // D3Q19 collision: 32-36 fewer warp instructions per 32 nodes, FP16 storage
 // 38.6k -> 39.6k MLUPS at 256^3.  (Packing the eta-blends, the stencil sums
@@ -293,7 +305,7 @@ StepMap step_map(const StepConst &c, const Quant &q)
 // in the dense layout [field][TY][TX]; odd steps, on interior tiles, one copy
 // per direction into the [dir][TY][W] rows.  Without TMA gmap is unused.
 template <typename ST, bool STREAMED, bool ODD, bool TMA>
-__global__ void __launch_bounds__(NT, Fmt<ST>::kMinBlocks)
+__global__ void __launch_bounds__(threads_of<ST>(), Fmt<ST>::kMinBlocks)
 zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const StepMap m, const int tz,
                 const int write_moments, const __grid_constant__ CUtensorMap gmap,
                 const __grid_constant__ CUtensorMap f0map, const __grid_constant__ CUtensorMap fqmap)
@@ -307,8 +319,10 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
     float *const PHI = reinterpret_cast<float *>(smem + Gm::PHI_OFF);   // [NPHI][RH][RW]
     constexpr int G_ELEMS = kQg * TY * W;                               // per stage
 
+    constexpr bool PAIR = use_pair<ST>();
+    constexpr int XPT = PAIR ? 2 : 1;          // x nodes per thread (block TX / XPT x TY)
     const int tx = threadIdx.x, ty = threadIdx.y;
-    const int tid = ty * TX + tx;
+    const int tid = ty * (TX / XPT) + tx;
     int bid = blockIdx.x;
     const int ntx = b.nx / TX, nty = b.ny / TY;
     const int bx = bid % ntx;
@@ -318,7 +332,7 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
     const int z0 = bid * tz;
     const int nzc = min(tz, b.nz - z0);       // planes of this chunk
     const int x0 = bx * TX, y0 = by * TY;
-    const int x = x0 + tx, y = y0 + ty;
+    const int x = x0 + XPT * tx, y = y0 + ty;   // (first) node of the thread
 
     uint64_t *const mbar = reinterpret_cast<uint64_t *>(smem + Gm::MBAR_OFF);
     // odd step: the rows y0 - 1 .. y0 + TY and columns x0 - E .. x0 + TX + E - 1
@@ -384,7 +398,7 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
     }
     // Warps 4-7 queue the g rows: thread owns row g_r, chunk g_k of every D-th
     // direction starting at g_q (uniform per warp).
-    const int gt = tid - NT / 2;
+    const int gt = PAIR ? tid : tid - NT / 2;   // with 128 threads every thread also queues g
     const bool g_issuer = gt >= 0;
     const int g_q = gt / Gm::TPD;
     const int g_r = (gt % Gm::TPD) / CM, g_k = gt % CM;
@@ -534,10 +548,12 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
     };
 
     // phi of plane p on the tile + ring into phi slot s; the streamed f of the
-    // thread's own node is returned in fo.
-    auto build_plane = [&](int p, int s, float(&fo)[kQf]) {
+    // thread's own node(s) is returned in fo.
+    auto build_plane = [&](int p, int s, float(&fo)[XPT][kQf]) {
         float *ph = PHI + s * (RH * RW);
-        ph[(ty + 1) * RW + tx + 1] = phi_at(p, tx + 1, ty + 1, fo);
+#pragma unroll
+        for (int k = 0; k < XPT; k++)
+            ph[(ty + 1) * RW + XPT * tx + k + 1] = phi_at(p, XPT * tx + k + 1, ty + 1, fo[k]);
         if (has_ring) {
             float tmp[kQf];
             ph[rly * RW + rlx] = phi_at(p, rlx, rly, tmp);
@@ -550,7 +566,7 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
     const int o_ym = (y == 0) ? (b.ny - 1) * b.nx : -b.nx;
     const int o_yp = (y == b.ny - 1) ? -(b.ny - 1) * b.nx : b.nx;
 
-    float fcur[kQf], fnext[kQf];
+    float fcur[XPT][kQf], fnext[XPT][kQf];
 
     // prologue: P_f planes z0-2 .. z0+1, g of plane z0; phi of z0-1 and z0
     issue_f(z0 - 2);
@@ -566,7 +582,7 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
     }
     __syncthreads();
     {
-        float tmp[kQf];
+        float tmp[XPT][kQf];
         build_plane(z0 - 1, 0, tmp);
     }
     build_plane(z0, 1, fcur);
@@ -605,6 +621,7 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
         const float *S0 = PHI + (j & 3) * (RH * RW);        // plane z - 1
         const float *S1 = PHI + ((j + 1) & 3) * (RH * RW);  // plane z
         const float *S2 = PHI + ((j + 2) & 3) * (RH * RW);  // plane z + 1
+        if constexpr (!PAIR) {
         const int lx = tx + 1, ly = ty + 1;
         auto at = [&](const float *S, int yy, int xx) { return S[yy * RW + xx]; };
 
@@ -674,17 +691,17 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
         {
             const float Af = 0.5f * c.Gamma * c.invTauPhi * mu;
             const float a = c.invTauPhiOne;
-            P.f0out[id] = a * fcur[0] - 6.0f * Af + c.invTauPhi * pc;
+            P.f0out[id] = a * fcur[0][0] - 6.0f * Af + c.invTauPhi * pc;
             // f_1..f_6 in stored units: terms scaled by f_scale
             const float Afk = Fm::kMapped ? m.Af * mu : Af;
             const float Cf = (Fm::kMapped ? m.Cf : c.invTauPhi * c.invEta2) * pc;
             auto put = [&](int k, float v) { P.fout[k][id] = Fm::store(v); };
-            put(0, a * fcur[1] + Afk + Cf * usx);
-            put(1, a * fcur[2] + Afk - Cf * usx);
-            put(2, a * fcur[3] + Afk + Cf * usy);
-            put(3, a * fcur[4] + Afk - Cf * usy);
-            put(4, a * fcur[5] + Afk + Cf * usz);
-            put(5, a * fcur[6] + Afk - Cf * usz);
+            put(0, a * fcur[0][1] + Afk + Cf * usx);
+            put(1, a * fcur[0][2] + Afk - Cf * usx);
+            put(2, a * fcur[0][3] + Afk + Cf * usy);
+            put(3, a * fcur[0][4] + Afk - Cf * usy);
+            put(4, a * fcur[0][5] + Afk + Cf * usz);
+            put(5, a * fcur[0][6] + Afk - Cf * usz);
         }
 
         // D3Q19 collision with forcing, src/collision_g.cu:111-196; in stored
@@ -802,8 +819,176 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
             }
         }
 
+        } else {
+            // Two nodes per thread: A = (x, y, z) in the .x lanes, B = (x + 1, y, z)
+            // in the .y lanes of packed FP32; 16-bit storage only, so g and f_1..f_6
+            // are in stored units (StepMap) and each store writes both nodes.
+            using namespace pk;
+            using T2 = typename Fm::T2;
+            const int lx = 2 * tx + 1, ly = ty + 1;   // ring-tile column of A
+            // phi at columns lx - 1 .. lx + 2 of row yy of a plane: two aligned float2
+            auto row4 = [&](const float *S, int yy, float2 &lo, float2 &hi) {
+                const float2 *r = reinterpret_cast<const float2 *>(S + yy * RW + lx - 1);
+                lo = r[0];
+                hi = r[1];
+            };
+            auto col = [&](const float *S, int yy) { return make_float2(S[yy * RW + lx], S[yy * RW + lx + 1]); };
+            float2 cl, ch, nl, nh, sl, sh, tl, th, bl, bh;
+            row4(S1, ly, cl, ch);
+            row4(S1, ly + 1, nl, nh);
+            row4(S1, ly - 1, sl, sh);
+            row4(S2, ly, tl, th);
+            row4(S0, ly, bl, bh);
+            // the same points as the one-node stencil (lo = x - 1, hi = x + 1)
+            const float2 pc = make_float2(cl.y, ch.x), pe = ch, pw = cl;
+            const float2 pn = make_float2(nl.y, nh.x), ps = make_float2(sl.y, sh.x);
+            const float2 pt = make_float2(tl.y, th.x), pb = make_float2(bl.y, bh.x);
+            const float2 pen = nh, pwn = nl, pes = sh, pws = sl, pet = th, pwt = tl, peb = bh, pwb = bl;
+            const float2 pnt = col(S2, ly + 1), psb = col(S0, ly - 1), pnb = col(S0, ly + 1), pst = col(S2, ly - 1);
+
+            float2 se = add(add(add(pen, pws), add(pes, pwn)), add(add(pet, pwb), add(peb, pwt)));
+            se = add(se, add(add(pnt, psb), add(pnb, pst)));
+            const float2 sf = add(add(add(pe, pw), add(pn, ps)), add(pt, pb));
+            const float2 lap = mul(fma(splat(2.f), fma(splat(-12.f), pc, sf), se), splat(kInv6));
+            const float2 mu =
+                fma(splat(-c.kappa), lap, mul(mul(splat(c.alpha4), pc), add(mul(pc, pc), splat(-c.phiStarSq))));
+            const float2 d_en = sub(pen, pws), d_es = sub(pes, pwn), d_et = sub(pet, pwb), d_eb = sub(peb, pwt);
+            const float2 d_nt = sub(pnt, psb), d_nb = sub(pnb, pst);
+            const float2 mu12 = mul(mu, splat(kInv12));
+            const float2 Fx = mul(mu12, add(add(fma(splat(2.f), sub(pe, pw), d_en), add(d_es, d_et)), d_eb));
+            const float2 Fy = mul(mu12, add(add(fma(splat(2.f), sub(pn, ps), d_en), sub(d_nt, d_es)), d_nb));
+            float2 Fz = mul(mu12, sub(add(fma(splat(2.f), sub(pt, pb), d_et), sub(d_nt, d_eb)), d_nb));
+            if (pc.x > 0.f) Fz.x += c.grav;
+            if (pc.y > 0.f) Fz.y += c.grav;
+
+            // D3Q19 values of both nodes from the staged rows (AA pattern)
+            const ST *Gs = G + (j & 1) * G_ELEMS;
+            float2 g[kQg];
 #pragma unroll
-        for (int i = 0; i < kQf; i++) fcur[i] = fnext[i];
+            for (int i = 0; i < kQg; i++) {
+                if (TMA && !ODD) {
+                    g[i] = Fm::load2(*reinterpret_cast<const T2 *>(Gs + (i * TY + ty) * TX + 2 * tx));
+                } else if (!ODD || kCx(i) == 0) {
+                    g[i] = Fm::load2(*reinterpret_cast<const T2 *>(Gs + (i * TY + ty) * W + E + 2 * tx));
+                } else {
+                    const ST *r = Gs + (i * TY + ty) * W + E + 2 * tx - kCx(i);
+                    g[i] = make_float2(Fm::load(r[0]), Fm::load(r[1]));
+                }
+            }
+
+            // moments (stored units: rho = g_inv sum + sum of shifts)
+            float2 rho = g[0];
+#pragma unroll
+            for (int i = 1; i < kQg; i++) rho = add(rho, g[i]);
+            rho = fma(splat(m.g_inv), rho, splat(m.rho_shift));
+            const float2 invRho = make_float2(1.0f / rho.x, 1.0f / rho.y);
+            const float2 invRhoG = mul(invRho, splat(m.g_inv));
+            const float2 d7 = sub(g[7], g[8]), d9 = sub(g[9], g[10]), d11 = sub(g[11], g[12]);
+            const float2 d13 = sub(g[13], g[14]), d15 = sub(g[15], g[16]), d17 = sub(g[17], g[18]);
+            const float2 ux = mul(add(add(add(add(sub(g[1], g[2]), d7), d9), d11), d13), invRhoG);
+            const float2 uy = mul(add(add(sub(add(sub(g[3], g[4]), d7), d9), d15), d17), invRhoG);
+            const float2 uz = mul(sub(add(sub(add(sub(g[5], g[6]), d11), d13), d15), d17), invRhoG);
+            const unsigned id = node_index(b, x, y, z);   // node A (even: 8-byte aligned pairs)
+            if (write_moments) {
+                *reinterpret_cast<float2 *>(P.mom[0] + id) = pc;
+                *reinterpret_cast<float2 *>(P.mom[1] + id) = rho;
+                *reinterpret_cast<float2 *>(P.mom[2] + id) = ux;
+                *reinterpret_cast<float2 *>(P.mom[3] + id) = uy;
+                *reinterpret_cast<float2 *>(P.mom[4] + id) = uz;
+            }
+            const float2 hinv = mul(splat(0.5f), invRho);
+            const float2 usx = fma(Fx, hinv, ux), usy = fma(Fy, hinv, uy), usz = fma(Fz, hinv, uz);
+
+            // D3Q7 collision (A/B store), f_1..f_6 in stored units
+            {
+                const float2 a2 = splat(c.invTauPhiOne);
+                auto fc = [&](int k) { return make_float2(fcur[0][k], fcur[1][k]); };
+                const float2 Af = mul(splat(0.5f * c.Gamma * c.invTauPhi), mu);
+                *reinterpret_cast<float2 *>(P.f0out + id) =
+                    fma(a2, fc(0), fma(splat(-6.f), Af, mul(splat(c.invTauPhi), pc)));
+                const float2 Afk = mul(splat(m.Af), mu), Cf = mul(splat(m.Cf), pc);
+                const float2 cux = mul(Cf, usx), cuy = mul(Cf, usy), cuz = mul(Cf, usz);
+                auto put2 = [&](int k, float2 v) { *reinterpret_cast<T2 *>(P.fout[k] + id) = Fm::store2(v); };
+                put2(0, fma(a2, fc(1), add(Afk, cux)));
+                put2(1, fma(a2, fc(2), sub(Afk, cux)));
+                put2(2, fma(a2, fc(3), add(Afk, cuy)));
+                put2(3, fma(a2, fc(4), sub(Afk, cuy)));
+                put2(4, fma(a2, fc(5), add(Afk, cuz)));
+                put2(5, fma(a2, fc(6), sub(Afk, cuz)));
+            }
+
+            // D3Q19 collision with forcing (the one-node formulas, StepMap constants)
+            {
+                const float2 bb = splat(c.invTauRhoOne);
+                const float2 phimu3 = mul(mul(splat(3.f), pc), mu);
+                const float2 usq = fma(usx, usx, fma(usy, usy, mul(usz, usz)));
+                const float2 temp1 = mul(splat(m.K1), fma(rho, fma(splat(-1.5f), usq, splat(1.f)), phimu3));
+                const float2 UF = fma(usx, Fx, fma(usy, Fy, mul(usz, Fz)));
+                const float2 vx = mul(usx, splat(3.f)), vy = mul(usy, splat(3.f)), vz = mul(usz, splat(3.f));
+                const float2 vsq6 = mul(fma(vx, vx, fma(vy, vy, mul(vz, vz))), splat(kInv6));
+                float2 qv[kQg];
+                qv[0] = fma(bb, g[0],
+                            fma(splat(m.K0), sub(fma(splat(-6.f), mul(pc, mu), rho), mul(rho, vsq6)),
+                                fma(splat(-m.KC0), UF, splat(m.k0))));
+                const float2 K1r = mul(splat(m.K1), rho), hK1r = mul(splat(0.5f), K1r);
+                const float2 t1 = fma(splat(-m.KC1), UF, add(temp1, splat(m.k1)));
+                auto face = [&](float2 w, float2 Gf, int ip, int im) {
+                    const float2 eq1 = fma(splat(m.KC1), mul(w, Gf), fma(mul(hK1r, w), w, t1));
+                    const float2 eq2 = mul(w, fma(splat(m.KC1), Gf, K1r));
+                    qv[ip] = add(fma(bb, g[ip], eq1), eq2);
+                    qv[im] = sub(fma(bb, g[im], eq1), eq2);
+                };
+                face(vx, Fx, 1, 2);
+                face(vy, Fy, 3, 4);
+                face(vz, Fz, 5, 6);
+                const float2 K2r = mul(splat(m.K2), rho), hK2r = mul(splat(0.5f), K2r);
+                const float2 t2 =
+                    fma(splat(-m.KC2), UF, fma(splat(m.K2), fma(rho, sub(splat(1.f), vsq6), phimu3), splat(m.k2)));
+                auto edge = [&](float2 w, float2 Gf, int ip, int im) {
+                    const float2 eq1 = fma(splat(m.KC2), mul(w, Gf), fma(mul(hK2r, w), w, t2));
+                    const float2 eq2 = fma(K2r, w, mul(splat(m.KC2), Gf));
+                    qv[ip] = add(fma(bb, g[ip], eq1), eq2);
+                    qv[im] = sub(fma(bb, g[im], eq1), eq2);
+                };
+                edge(add(vx, vy), add(Fx, Fy), 7, 8);
+                edge(sub(vx, vy), sub(Fx, Fy), 9, 10);
+                edge(add(vx, vz), add(Fx, Fz), 11, 12);
+                edge(sub(vx, vz), sub(Fx, Fz), 13, 14);
+                edge(add(vy, vz), add(Fy, Fz), 15, 16);
+                edge(sub(vy, vz), sub(Fy, Fz), 17, 18);
+                if (!ODD) {
+                    // even: own nodes, reversed slots
+#pragma unroll
+                    for (int i = 0; i < kQg; i++) *reinterpret_cast<T2 *>(P.g[kOpp(i)] + id) = Fm::store2(qv[i]);
+                } else {
+                    // odd: downstream neighbours x + c_i, natural slot i; a pair
+                    // moved along x is not 32-bit aligned, so those directions
+                    // store the two 16-bit values apart (A = x is even: only its
+                    // -x neighbour wraps; only B's +x neighbour wraps)
+                    const int o_zm = (z == 0) ? (b.nz - 1) * (int)b.nxy : -(int)b.nxy;
+                    const int o_zp = (z == b.nz - 1) ? -(b.nz - 1) * (int)b.nxy : (int)b.nxy;
+                    const int oA_xm = (x == 0) ? b.nx - 1 : -1;
+                    const int oB_xp = (x + 1 == b.nx - 1) ? -(b.nx - 1) : 1;
+#pragma unroll
+                    for (int i = 0; i < kQg; i++) {
+                        const int oyz = (kCy(i) > 0 ? o_yp : kCy(i) < 0 ? o_ym : 0) +
+                                        (kCz(i) > 0 ? o_zp : kCz(i) < 0 ? o_zm : 0);
+                        const T2 h = Fm::store2(qv[i]);
+                        if (kCx(i) == 0) {
+                            *reinterpret_cast<T2 *>(P.g[i] + id + oyz) = h;
+                        } else {
+                            P.g[i][id + oyz + (kCx(i) > 0 ? 1 : oA_xm)] = h.x;
+                            P.g[i][id + 1 + oyz + (kCx(i) > 0 ? oB_xp : -1)] = h.y;
+                        }
+                    }
+                }
+            }
+        }
+
+#pragma unroll
+        for (int k = 0; k < XPT; k++)
+#pragma unroll
+            for (int i = 0; i < kQf; i++) fcur[k][i] = fnext[k][i];
     }
 }
 
@@ -905,8 +1090,8 @@ int choose_tz(const Box &b)
         int dev = 0, sms = 0, per_sm = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, zsc_step_kernel<ST, false, false, false>, NT,
-                                                      Geo<ST>::SMEM);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, zsc_step_kernel<ST, false, false, false>,
+                                                      threads_of<ST>(), Geo<ST>::SMEM);
         slots = sms * per_sm > 0 ? sms * per_sm : 1;
     }
     const long long tiles = (long long)(b.nx / TX) * (b.ny / TY);
@@ -967,7 +1152,7 @@ cudaError_t launch_typed(const Box &b, const StepConst &c, const Quant &q, const
     const int tz = choose_tz<ST>(b);
     const int nchunks = (b.nz + tz - 1) / tz;
     const unsigned nblocks = (unsigned)((b.nx / TX) * (b.ny / TY) * nchunks);
-    const dim3 block(TX, TY, 1);
+    const dim3 block(TX / (use_pair<ST>() ? 2 : 1), TY, 1);
     const int wm = write_moments ? 1 : 0;
     constexpr int smem = Geo<ST>::SMEM;
     if (f_streamed) {
