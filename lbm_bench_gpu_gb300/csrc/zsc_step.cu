@@ -102,14 +102,16 @@ constexpr int threads_of() { return use_pair<ST>() ? NT / 2 : NT; }
 #define ZSC_TMA_G 1
 #endif
 // odd steps by TMA too (19 per-direction copies per plane on interior tiles):
-// measured slower than cp.async (FP16 33.7k vs 36.2k MLUPS at 256^3), so off
+// measured slower than cp.async (256^3: FP16 one node per thread 33.7k vs 36.2k,
+// two nodes per thread 39.5k vs 41.9k; FP32 26.7k vs 27.2k MLUPS), so off
 #ifndef ZSC_TMA_ODD
 #define ZSC_TMA_ODD 0
 #endif
 // the P_f planes by TMA on interior tiles (f_0 box W0 x FR, f_1..f_6 box
 // W x FR x 6), for the 16-bit formats: measured at 256^3 (same GPU, 500
 // steps), FP16 36 250 -> 37 060 MLUPS, while FP32 drops 27 110 -> 26 560 with
-// it (its per-thread cp.async spreads the twice larger planes better)
+// it (its per-thread cp.async spreads the twice larger planes better; again
+// 27 200 -> 26 640 with the current kernel); 2 = all formats
 #ifndef ZSC_TMA_F
 #define ZSC_TMA_F 1
 #endif
@@ -117,7 +119,7 @@ constexpr bool kUseTma = ZSC_TMA_G != 0;
 constexpr bool kUseTmaOdd = ZSC_TMA_ODD != 0;
 constexpr bool kUseTmaF = ZSC_TMA_F != 0;
 template <typename ST>
-constexpr bool use_tma_f() { return kUseTmaF && sizeof(ST) == 2; }
+constexpr bool use_tma_f() { return kUseTmaF && (sizeof(ST) == 2 || ZSC_TMA_F == 2); }
 constexpr float kInv12 = 0.08333333333333333333f;
 
 template <int I>
