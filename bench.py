@@ -196,9 +196,43 @@ def cpu_baseline(inp, budget_s: float = 15.0):
     dt = time.perf_counter() - t0
     nodes = inp.nx * inp.ny * inp.nz
     o.close()
-    return {"value": nodes * n / dt / 1e6, "unit": "MLUPS", "cores": Oracle.threads(), "kind": "port",
-            "sample": f"FP64 oracle, full {inp.nx}x{inp.ny}x{inp.nz} box, {n} steps after 1 untimed step "
-                      f"({dt:.1f} s)"}
+    out = {"value": nodes * n / dt / 1e6, "unit": "MLUPS", "cores": Oracle.threads(), "kind": "port",
+           "cpu_model": cpu_model(),
+           "sample": f"FP64 oracle, full {inp.nx}x{inp.ny}x{inp.nz} box, {n} steps after 1 untimed step "
+                     f"({dt:.1f} s)"}
+    # the static-bubble case in full: 64^3, one bubble R = 12, 1000 relaxation steps
+    from lbm_bench_gpu_gb300 import inputs
+    s1 = inputs.static_bubble()
+    o = Oracle.from_params(params_for(s1))
+    o.init_bubbles(s1.bubbles)
+    t0 = time.perf_counter()
+    o.step(1000, 0.0)
+    dt1 = time.perf_counter() - t0
+    o.close()
+    out["static_bubble_64"] = {"value": s1.nx * s1.ny * s1.nz * 1000 / dt1 / 1e6, "unit": "MLUPS",
+                               "seconds": round(dt1, 2), "sample": "64^3, one bubble R = 12, 1000 steps, in full"}
+    return out
+
+
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu, else /proc/cpuinfo, else the architecture)."""
+    import platform
+    import subprocess
+    try:
+        r = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10)
+        for line in r.stdout.splitlines():
+            if line.strip().lower().startswith("model name"):
+                return line.split(":", 1)[1].strip() + f" ({platform.machine()})"
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith(("model name", "cpu model")):
+                    return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return platform.machine()
 
 
 def max_over_ranks(x: float, local: int = 0) -> float:
