@@ -493,7 +493,10 @@ __global__ void __launch_bounds__(NTA, ZSC_ADJ_MIN_BLOCKS) adjoint_local_kernel(
 // float4 source in shared memory, each on the tile plus a one-node ring
 // (34 x 10), split into its four components so that a node reads the 49
 // scalars it needs (lambda_lap at 19 points, each gradient component at the
-// 10 points with c_k != 0) without bank conflicts.
+// 10 points with c_k != 0) without bank conflicts.  Plane z + 2 is read into
+// registers before plane z is computed (its loads overlap the computation) and
+// stored into the slot plane z - 1 frees; each thread's staging coordinates
+// are computed once.
 constexpr int SW = TXA + 2, SH = TYA + 2, SPLANE = SW * SH;
 
 __global__ void __launch_bounds__(NTA) adjoint_stencil_kernel(Box b, const float4 *__restrict__ lsrc,
@@ -504,27 +507,48 @@ __global__ void __launch_bounds__(NTA) adjoint_stencil_kernel(Box b, const float
     const int x0 = blockIdx.x * TXA, y0 = blockIdx.y * TYA;
     const int z_begin = blockIdx.z * kPlanes, z_end = min(b.nz, z_begin + kPlanes);
     const unsigned nx = (unsigned)b.nx;
-    auto load = [&](int z, int slot) {
+    // the (up to two) ring-tile nodes this thread stages, as in-plane offsets
+    // (periodic in x and y), fixed for the block
+    auto xy_of = [&](int e) {
+        const int r = e / SW, c = e - r * SW;
+        int gx = x0 - 1 + c, gy = y0 - 1 + r;
+        gx = gx < 0 ? gx + b.nx : (gx >= b.nx ? gx - b.nx : gx);
+        gy = gy < 0 ? gy + b.ny : (gy >= b.ny ? gy - b.ny : gy);
+        return (unsigned)gy * nx + (unsigned)gx;
+    };
+    const int e0 = tid, e1 = tid + NTA;
+    const bool two = e1 < SPLANE;
+    const unsigned xy0 = xy_of(e0), xy1 = two ? xy_of(e1) : 0u;
+    float4 v0, v1;
+    auto fetch = [&](int z) {   // plane z into registers (its loads stay in flight)
         const int zw = z < 0 ? z + b.nz : (z >= b.nz ? z - b.nz : z);
         const unsigned zo = (unsigned)zw * (unsigned)b.nxy;
-        for (int e = tid; e < SPLANE; e += NTA) {
-            const int r = e / SW, c = e - r * SW;
-            int gx = x0 - 1 + c, gy = y0 - 1 + r;
-            gx = gx < 0 ? gx + b.nx : (gx >= b.nx ? gx - b.nx : gx);
-            gy = gy < 0 ? gy + b.ny : (gy >= b.ny ? gy - b.ny : gy);
-            const float4 v = __ldg(lsrc + zo + (unsigned)gy * nx + (unsigned)gx);
-            sm[slot][0][e] = v.x;
-            sm[slot][1][e] = v.y;
-            sm[slot][2][e] = v.z;
-            sm[slot][3][e] = v.w;
+        v0 = __ldg(lsrc + zo + xy0);
+        if (two) v1 = __ldg(lsrc + zo + xy1);
+    };
+    auto put = [&](int z) {     // ... and into its ring slot, components apart
+        const int slot = (z + 3) % 3;
+        sm[slot][0][e0] = v0.x;
+        sm[slot][1][e0] = v0.y;
+        sm[slot][2][e0] = v0.z;
+        sm[slot][3][e0] = v0.w;
+        if (two) {
+            sm[slot][0][e1] = v1.x;
+            sm[slot][1][e1] = v1.y;
+            sm[slot][2][e1] = v1.z;
+            sm[slot][3][e1] = v1.w;
         }
     };
-    load(z_begin - 1, (z_begin + 2) % 3);
-    load(z_begin, z_begin % 3);
+    for (int z = z_begin - 1; z <= min(z_begin + 1, z_end); z++) {
+        fetch(z);
+        put(z);
+    }
+    __syncthreads();
     const int cell = (ty + 1) * SW + tx + 1;
     for (int z = z_begin; z < z_end; z++) {
-        load(z + 1, (z + 1) % 3);
-        __syncthreads();
+        // plane z + 2 is read from memory while plane z is computed
+        const bool next = z + 2 <= z_end;
+        if (next) fetch(z + 2);
         float lface = 0.f, ledge = 0.f, dface = 0.f, dedge = 0.f;
 #pragma unroll
         for (int i = 1; i < kQg; i++) {
@@ -547,6 +571,8 @@ __global__ void __launch_bounds__(NTA) adjoint_stencil_kernel(Box b, const float
         const float L = (ledge + 2.f * (lface - 12.f * c0)) * kInv6;
         const float D = (2.f * dface + dedge) * kInv12;
         lst[(unsigned)z * (unsigned)b.nxy + (unsigned)(y0 + ty) * nx + (unsigned)(x0 + tx)] = L - D;
+        __syncthreads();          // plane z - 1's slot is free (z + 2 takes it)
+        if (next) put(z + 2);
         __syncthreads();
     }
 }
