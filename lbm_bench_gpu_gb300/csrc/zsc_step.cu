@@ -53,6 +53,7 @@
 #include <cstdint>
 #include <cstring>
 #include <type_traits>
+#include <utility>
 
 #include "lattice.cuh"
 
@@ -217,6 +218,28 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned phase, unsigne
     for (unsigned it = 0; it < limit; ++it)
         if (mbar_try_wait(bar, phase)) return true;
     return false;
+}
+
+// Programmatic dependent launch: a step grid lets the next step's grid be
+// scheduled as soon as all its own blocks have started (so the next grid's
+// blocks take the SMs this grid's tail frees), and a block waits for the
+// previous grid's completion and memory before it first touches the state.
+// Measured (MLUPS, without -> with): 256^3 FP32 27 197 -> 27 433, FP16
+// 41 935 -> 42 287; 128^3 FP32 24 476 -> 24 852, FP16 33 558 -> 35 194.
+#ifndef ZSC_PDL
+#define ZSC_PDL 1
+#endif
+__device__ __forceinline__ void pdl_launch_dependents()
+{
+#if ZSC_PDL
+    asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
+#endif
+}
+__device__ __forceinline__ void pdl_wait()
+{
+#if ZSC_PDL
+    asm volatile("griddepcontrol.wait;\n" ::: "memory");
+#endif
 }
 
 // One warp waits, bounded, on a fresh mbarrier that nothing arrives at (no
@@ -569,6 +592,9 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
     const int o_yp = (y == b.ny - 1) ? -(b.ny - 1) * b.nx : b.nx;
 
     float fcur[XPT][kQf], fnext[XPT][kQf];
+
+    pdl_launch_dependents();
+    pdl_wait();   // the previous step's writes are complete and visible
 
     // prologue: P_f planes z0-2 .. z0+1, g of plane z0; phi of z0-1 and z0
     issue_f(z0 - 2);
@@ -1112,6 +1138,25 @@ int choose_tz(const Box &b)
     return best;
 }
 
+// A step launch with programmatic stream serialization (the kernel orders
+// itself after the previous grid with griddepcontrol.wait).
+template <typename... KArgs, typename... Args>
+cudaError_t launch_step_kernel(void (*kernel)(KArgs...), unsigned nblocks, dim3 block, int smem, cudaStream_t s,
+                               Args &&...args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(nblocks, 1, 1);
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = (size_t)smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = ZSC_PDL ? 1 : 0;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
+
 template <typename ST>
 cudaError_t launch_typed(const Box &b, const StepConst &c, const Quant &q, const StepView &v, bool f_streamed,
                          bool odd, bool write_moments, cudaStream_t s)
@@ -1157,23 +1202,13 @@ cudaError_t launch_typed(const Box &b, const StepConst &c, const Quant &q, const
     const dim3 block(TX / (use_pair<ST>() ? 2 : 1), TY, 1);
     const int wm = write_moments ? 1 : 0;
     constexpr int smem = Geo<ST>::SMEM;
+    auto go = [&](auto kernel) { return launch_step_kernel(kernel, nblocks, block, smem, s, P, b, c, m, tz, wm, gmap, f0map, fqmap); };
     if (f_streamed) {
         if (odd) return cudaErrorInvalidValue;  // the streamed initial state is always read by an even step
-        if (tma)
-            zsc_step_kernel<ST, true, false, true><<<nblocks, block, smem, s>>>(P, b, c, m, tz, wm, gmap, f0map, fqmap);
-        else
-            zsc_step_kernel<ST, true, false, false><<<nblocks, block, smem, s>>>(P, b, c, m, tz, wm, gmap, f0map, fqmap);
-    } else if (odd) {
-        if (tma)
-            zsc_step_kernel<ST, false, true, true><<<nblocks, block, smem, s>>>(P, b, c, m, tz, wm, gmap, f0map, fqmap);
-        else
-            zsc_step_kernel<ST, false, true, false><<<nblocks, block, smem, s>>>(P, b, c, m, tz, wm, gmap, f0map, fqmap);
-    } else if (tma) {
-        zsc_step_kernel<ST, false, false, true><<<nblocks, block, smem, s>>>(P, b, c, m, tz, wm, gmap, f0map, fqmap);
-    } else {
-        zsc_step_kernel<ST, false, false, false><<<nblocks, block, smem, s>>>(P, b, c, m, tz, wm, gmap, f0map, fqmap);
+        return tma ? go(zsc_step_kernel<ST, true, false, true>) : go(zsc_step_kernel<ST, true, false, false>);
     }
-    return cudaGetLastError();
+    if (odd) return tma ? go(zsc_step_kernel<ST, false, true, true>) : go(zsc_step_kernel<ST, false, true, false>);
+    return tma ? go(zsc_step_kernel<ST, false, false, true>) : go(zsc_step_kernel<ST, false, false, false>);
 }
 
 }  // namespace
