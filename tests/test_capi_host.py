@@ -145,3 +145,36 @@ def test_bubble_placement_rules():
     m = r + 4.0 + 1.0
     assert np.all(c[:, 0] >= m) and np.all(c[:, 0] <= 255 - m)
     assert np.all(c[:, 2] >= 1 + m) and np.all(c[:, 2] <= 256 - m)
+
+
+def test_integration_examples_compile_and_link(lib, tmp_path):
+    """The C examples of INTEGRATION.md (the reference's main loop on the C-ABI,
+    and the adjoint calls) compile with -Wall -Werror against the header and
+    link against the library: what a maintainer of the reference would build."""
+    import re
+    import shutil
+    import subprocess
+    from pathlib import Path
+    root = Path(__file__).resolve().parents[1]
+    blocks = re.findall(r"```c\n(.*?)```", (root / "INTEGRATION.md").read_text(), re.S)
+    assert len(blocks) >= 2
+    cc = shutil.which("cc") or shutil.which("gcc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    main_c = tmp_path / "main_loop.c"
+    main_c.write_text(blocks[0])
+    adjoint_c = tmp_path / "adjoint.c"
+    adjoint_c.write_text(
+        "#include <stdio.h>\n#include \"lbm_gb300.h\"\n"
+        "#define CHECK(x) do { int rc_ = (x); if (rc_) { fprintf(stderr, \"%s\\n\", lbm_strerror(rc_)); "
+        "return 1; } } while (0)\n"
+        "int adjoint_example(lbm_ctx *c, lbm_derived d, float *grad)\n{\n" + blocks[1] + "    return 0;\n}\n")
+    pkg = root / "lbm_bench_gpu_gb300"
+    for src in (main_c, adjoint_c):
+        args = [cc, "-std=c99", "-Wall", "-Werror", str(src), "-I", str(root / "include")]
+        if src is main_c:
+            args += ["-L", str(pkg), "-llbm_gb300", "-o", str(tmp_path / "main_loop")]
+        else:
+            args += ["-c", "-o", str(tmp_path / "adjoint.o")]
+        r = subprocess.run(args, capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
