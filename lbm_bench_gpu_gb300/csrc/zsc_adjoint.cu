@@ -295,6 +295,11 @@ __global__ void __launch_bounds__(NTA) source_init_kernel(Box b, int objective, 
 }
 
 struct AdjIn {
+    // per-field base pointers (kernel parameters: a field's address is one
+    // multiply-add on the node index, with no i * n on the load's path)
+    const void *g_f[kQg];                  // the state's g fields
+    const float *lf_f[kQf], *lg_f[kQg];    // lambda^{n+1}
+    float *lf_o[kQf], *lg_o[kQg];          // lambda^n
     const void *g;                         // native g of s^n
     const float *phi;                      // phi of s^n
     const float *lf, *lg, *lst;            // lambda^{n+1} (lf without its stencil part lst)
@@ -357,8 +362,18 @@ __global__ void __launch_bounds__(NTA, ZSC_ADJ_MIN_BLOCKS) adjoint_local_kernel(
         float lap, gr[3];
         stencil19(a.phi, p, lap, gr[0], gr[1], gr[2]);
         const float ph = __ldg(a.phi + t);
-        float rh, m[3];
-        g_moments<ST, ODD>(g, n, q, p, rh, m);
+        float rh = 0.f, m[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+        for (int i = 0; i < kQg; i++) {
+            const ST v = ODD ? static_cast<const ST *>(a.g_f[kOpp(i)])[dir_at(p, i, -1)]
+                             : static_cast<const ST *>(a.g_f[i])[t];
+            float gi = Fmt<ST>::load(v);
+            if constexpr (Fmt<ST>::kMapped) gi = gi * q.g_inv + q.g_shift[i];
+            rh += gi;
+            if (kCx(i)) m[0] += kCx(i) * gi;
+            if (kCy(i)) m[1] += kCy(i) * gi;
+            if (kCz(i)) m[2] += kCz(i) * gi;
+        }
         const float inv = 1.0f / rh;
         const float u[3] = {m[0] * inv, m[1] * inv, m[2] * inv};
         const float mu = c.alpha4 * ph * (ph * ph - c.phiStarSq) - c.kappa * lap;
@@ -373,15 +388,14 @@ __global__ void __launch_bounds__(NTA, ZSC_ADJ_MIN_BLOCKS) adjoint_local_kernel(
         // stream adjoint
         float lP[kQf], lQ[kQg];
         const float lst_here = __ldg(a.lst + t);
-        lP[0] = __ldg(a.lf + t) + lst_here;
+        lP[0] = __ldg(a.lf_f[0] + t) + lst_here;
 #pragma unroll
         for (int i = 1; i < kQf; i++) {
             const unsigned dn = dir_at(p, i, 1);
-            lP[i] = c.eta * (__ldg(a.lf + i * n + dn) + __ldg(a.lst + dn))
-                    + c.eta2 * (__ldg(a.lf + i * n + t) + lst_here);
+            lP[i] = c.eta * (__ldg(a.lf_f[i] + dn) + __ldg(a.lst + dn)) + c.eta2 * (__ldg(a.lf_f[i] + t) + lst_here);
         }
 #pragma unroll
-        for (int i = 0; i < kQg; i++) lQ[i] = __ldg(a.lg + i * n + dir_at(p, i, 1));
+        for (int i = 0; i < kQg; i++) lQ[i] = __ldg(a.lg_f[i] + dir_at(p, i, 1));
 
         // D3Q7 collision
         float lphi = 0.f, lmu = 0.f, lus[3] = {0.f, 0.f, 0.f}, lF[3] = {0.f, 0.f, 0.f}, lrho = 0.f;
@@ -471,14 +485,14 @@ __global__ void __launch_bounds__(NTA, ZSC_ADJ_MIN_BLOCKS) adjoint_local_kernel(
             lm[2] += dmz;
         }
 #pragma unroll
-        for (int i = 0; i < kQf; i++) a.lf_out[i * n + t] = c.invTauPhiOne * lP[i] + lphi;
+        for (int i = 0; i < kQf; i++) a.lf_o[i][t] = c.invTauPhiOne * lP[i] + lphi;
 #pragma unroll
         for (int i = 0; i < kQg; i++) {
             float o = c.invTauRhoOne * lQ[i] + lrho;
             if (kCx(i)) o += kCx(i) * lm[0];
             if (kCy(i)) o += kCy(i) * lm[1];
             if (kCz(i)) o += kCz(i) * lm[2];
-            a.lg_out[i * n + t] = o;
+            a.lg_o[i][t] = o;
         }
     }
     dg = block_sum(dg, red);
@@ -721,6 +735,16 @@ cudaError_t launch_adjoint_step(const Box &b, const StepConst &c, float phiStar,
     in.lst = a.lst_in;
     in.lf_out = a.lf_out;
     in.lg_out = a.lg_out;
+    const size_t n = (size_t)b.n, esz = storage_bytes(st.storage);
+    for (int i = 0; i < kQg; i++) {
+        in.g_f[i] = static_cast<const unsigned char *>(st.g) + (size_t)i * n * esz;
+        in.lg_f[i] = a.lg_in + (size_t)i * n;
+        in.lg_o[i] = a.lg_out + (size_t)i * n;
+    }
+    for (int i = 0; i < kQf; i++) {
+        in.lf_f[i] = a.lf_in + (size_t)i * n;
+        in.lf_o[i] = a.lf_out + (size_t)i * n;
+    }
     in.lsrc = a.lsrc;
     in.dgrav = a.dgrav;
     in.ab = a.ab;
