@@ -104,11 +104,21 @@ __device__ __forceinline__ void stencil19(const float *__restrict__ v, const Nb 
     gz = (2.f * (s[5] - s[6]) + s[11] - s[12] + s[14] - s[13] + s[15] - s[16] + s[18] - s[17]) * kInv12;
 }
 
+// Per-field base pointers of a state (kernel parameters: a field's address is
+// one multiply-add on the node index).
+struct GFields {
+    const void *f[kQg];       // g, AA layout
+};
+struct FQFields {
+    const void *f[kQf - 1];   // f_1 .. f_6
+};
+
 // Streamed g_i at the centre of p, FP32.
 template <typename ST, bool ODD>
-__device__ __forceinline__ float g_streamed(const ST *__restrict__ g, unsigned n, const Quant &q, const Nb &p, int i)
+__device__ __forceinline__ float g_streamed(const GFields &g, const Quant &q, const Nb &p, int i)
 {
-    const ST v = ODD ? g[kOpp(i) * n + dir_at(p, i, -1)] : g[i * n + p.at(0, 0, 0)];
+    const ST v = ODD ? static_cast<const ST *>(g.f[kOpp(i)])[dir_at(p, i, -1)]
+                     : static_cast<const ST *>(g.f[i])[p.at(0, 0, 0)];
     if constexpr (Fmt<ST>::kMapped)
         return Fmt<ST>::load(v) * q.g_inv + q.g_shift[i];
     else
@@ -117,14 +127,13 @@ __device__ __forceinline__ float g_streamed(const ST *__restrict__ g, unsigned n
 
 // rho and momentum of the streamed g at the centre of p.
 template <typename ST, bool ODD>
-__device__ __forceinline__ void g_moments(const ST *__restrict__ g, unsigned n, const Quant &q, const Nb &p,
-                                          float &rho, float m[3])
+__device__ __forceinline__ void g_moments(const GFields &g, const Quant &q, const Nb &p, float &rho, float m[3])
 {
     rho = 0.f;
     m[0] = m[1] = m[2] = 0.f;
 #pragma unroll
     for (int i = 0; i < kQg; i++) {
-        const float gi = g_streamed<ST, ODD>(g, n, q, p, i);
+        const float gi = g_streamed<ST, ODD>(g, q, p, i);
         rho += gi;
         if (kCx(i)) m[0] += kCx(i) * gi;
         if (kCy(i)) m[1] += kCy(i) * gi;
@@ -151,10 +160,9 @@ __device__ __forceinline__ unsigned block_id() { return blockIdx.x + gridDim.x *
 // phi = sum of the streamed f of a native state.
 template <typename ST>
 __global__ void __launch_bounds__(NTA) adjoint_phi_kernel(Box b, float eta, Quant q, const float *__restrict__ f0,
-                                                          const ST *__restrict__ fq, int f_streamed,
+                                                          const FQFields fq, int f_streamed,
                                                           float *__restrict__ phi)
 {
-    const unsigned n = (unsigned)b.n;
     const float eta2 = 1.f - eta;
     const int x = blockIdx.x * TXA + threadIdx.x, y = blockIdx.y * TYA + threadIdx.y;
     for (int z = blockIdx.z * kPlanes, z_end = min(b.nz, z + kPlanes); z < z_end; z++) {
@@ -163,7 +171,7 @@ __global__ void __launch_bounds__(NTA) adjoint_phi_kernel(Box b, float eta, Quan
         float s = f0[t];
 #pragma unroll
         for (int i = 1; i < kQf; i++) {
-            const ST *a = fq + (i - 1) * n;
+            const ST *a = static_cast<const ST *>(fq.f[i - 1]);
             const float inv = Fmt<ST>::kMapped ? q.f_inv : 1.f;
             const float here = Fmt<ST>::load(a[t]) * inv;
             s += f_streamed ? here : eta * (Fmt<ST>::load(a[dir_at(p, i, -1)]) * inv) + eta2 * here;
@@ -177,11 +185,10 @@ __global__ void __launch_bounds__(NTA) adjoint_phi_kernel(Box b, float eta, Quan
 // plane index z + 1 (objective 1); per-block partials.
 template <typename ST, bool ODD>
 __global__ void __launch_bounds__(NTA) objective_kernel(Box b, int objective, float phiStar, Quant q,
-                                                        const ST *__restrict__ g, const float *__restrict__ phi,
+                                                        const GFields g, const float *__restrict__ phi,
                                                         double *__restrict__ partials)
 {
     __shared__ double red[NTA / 32];
-    const unsigned n = (unsigned)b.n;
     const float half_inv = 0.5f / phiStar;
     double A = 0.0, B = 0.0;
     const int x = blockIdx.x * TXA + threadIdx.x, y = blockIdx.y * TYA + threadIdx.y;
@@ -192,7 +199,7 @@ __global__ void __launch_bounds__(NTA) objective_kernel(Box b, int objective, fl
         float qv;
         if (objective == 0) {
             float rho, m[3];
-            g_moments<ST, ODD>(g, n, q, p, rho, m);
+            g_moments<ST, ODD>(g, q, p, rho, m);
             qv = m[2] / rho;
         } else {
             qv = (float)(z + 1);
@@ -272,7 +279,7 @@ __device__ __forceinline__ void objective_source(int z, int objective, const Sou
 template <typename ST, bool ODD>
 __global__ void __launch_bounds__(NTA) source_init_kernel(Box b, int objective, double scale,
                                                           const double *__restrict__ ab, float phiStar, Quant q,
-                                                          const ST *__restrict__ g, const float *__restrict__ phi,
+                                                          const GFields g, const float *__restrict__ phi,
                                                           float *__restrict__ lf, float *__restrict__ lg,
                                                           float *__restrict__ lst)
 {
@@ -283,7 +290,7 @@ __global__ void __launch_bounds__(NTA) source_init_kernel(Box b, int objective, 
         const Nb p = neighbourhood(b, x, y, z);
         const unsigned t = p.at(0, 0, 0);
         float rho, m[3];
-        g_moments<ST, ODD>(g, n, q, p, rho, m);
+        g_moments<ST, ODD>(g, q, p, rho, m);
         float dphi, drho, dmz;
         objective_source(z, objective, k, phiStar, phi[t], rho, m[2], dphi, drho, dmz);
 #pragma unroll
@@ -678,6 +685,22 @@ cudaError_t dispatch(const NativeState &st, Fn &&fn)
 
 }  // namespace
 
+// per-field pointers of a native state
+GFields g_fields(const Box &b, const NativeState &st)
+{
+    GFields r;
+    const size_t stride = (size_t)b.n * storage_bytes(st.storage);
+    for (int i = 0; i < kQg; i++) r.f[i] = static_cast<const unsigned char *>(st.g) + (size_t)i * stride;
+    return r;
+}
+FQFields fq_fields(const Box &b, const NativeState &st)
+{
+    FQFields r;
+    const size_t stride = (size_t)b.n * storage_bytes(st.storage);
+    for (int i = 0; i < kQf - 1; i++) r.f[i] = static_cast<const unsigned char *>(st.fq) + (size_t)i * stride;
+    return r;
+}
+
 size_t adjoint_blocks(const Box &b)
 {
     return std::max(blocks_of(adjoint_grid(b)), blocks_of(local_grid(b)));
@@ -690,7 +713,7 @@ cudaError_t launch_adjoint_phi(const Box &b, float eta, const Quant &q, const Na
     even.g_odd = false;   // phi does not read g
     return dispatch(even, [&](auto tag, auto) {
         using ST = decltype(tag);
-        adjoint_phi_kernel<ST><<<adjoint_grid(b), kBlock, 0, s>>>(b, eta, q, st.f0, static_cast<const ST *>(st.fq),
+        adjoint_phi_kernel<ST><<<adjoint_grid(b), kBlock, 0, s>>>(b, eta, q, st.f0, fq_fields(b, st),
                                                                  st.f_streamed ? 1 : 0, phi);
         return cudaGetLastError();
     });
@@ -703,7 +726,7 @@ cudaError_t launch_objective(const Box &b, int objective, float phiStar, double 
     cudaError_t e = dispatch(st, [&](auto tag, auto odd) {
         using ST = decltype(tag);
         objective_kernel<ST, decltype(odd)::value><<<adjoint_grid(b), kBlock, 0, s>>>(
-            b, objective, phiStar, q, static_cast<const ST *>(st.g), phi, partials);
+            b, objective, phiStar, q, g_fields(b, st), phi, partials);
         return cudaGetLastError();
     });
     if (e != cudaSuccess) return e;
@@ -718,7 +741,7 @@ cudaError_t launch_source_init(const Box &b, int objective, double scale, const 
     return dispatch(st, [&](auto tag, auto odd) {
         using ST = decltype(tag);
         source_init_kernel<ST, decltype(odd)::value><<<adjoint_grid(b), kBlock, 0, s>>>(
-            b, objective, scale, ab, phiStar, q, static_cast<const ST *>(st.g), phi, lf, lg, lst);
+            b, objective, scale, ab, phiStar, q, g_fields(b, st), phi, lf, lg, lst);
         return cudaGetLastError();
     });
 }
