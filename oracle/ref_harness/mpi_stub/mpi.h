@@ -2,7 +2,7 @@
  * mpi.h -- single-rank MPI stub for building the reference's own CUDA program
  * (src/main.cu) on one GPU.
  *
- * TEST / BASELINE INFRASTRUCTURE ONLY: used by oracle/build.py to build
+ * TEST AND BENCHMARK INFRASTRUCTURE ONLY: used by oracle/build.py to build
  * oracle/_ref/lbm_ref_cuda, the reference's unmodified step timed beside the
  * product.  Never linked into the product.
  *
