@@ -264,15 +264,19 @@ def test_storage_roundtrip_error_bound(lib, storage):
 
 @pytest.mark.parametrize("storage", ["fp16", "bf16"])
 @pytest.mark.parametrize("steps", [1, 2, 10])
-@pytest.mark.parametrize("shape", [(64, 32, 48), (32, 8, 12)])
+@pytest.mark.parametrize("shape", [(64, 32, 48), (32, 8, 12), (128, 32, 16)])
 def test_storage_steps_match_oracle(lib, storage, steps, shape):
     """16-bit storage (two nodes per thread in the step kernel) against the
     FP64 oracle; the 32 x 8 x 12 box is one tile in x and y, so every +-x and
-    +-y neighbour of an odd step wraps inside the block's own tile."""
+    +-y neighbour of an odd step wraps inside the block's own tile; the
+    128 x 32 x 16 box has interior tiles, whose P_f planes come by TMA (the
+    tiles at the periodic seam stage them with cp.async)."""
     from lbm_bench_gpu_gb300 import capi
     nx, ny, nz = shape
     if shape == (64, 32, 48):
         b = np.array([[nx / 2 - 0.3, ny / 2 + 0.2, nz / 2 + 0.4, 10.0], [16, 8, 13, 6.0]], np.float32)
+    elif shape == (128, 32, 16):
+        b = np.array([[50.3, 15.8, 8.4, 6.0], [97.1, 9.2, 7.7, 4.5]], np.float32)
     else:
         b = np.array([[nx / 2 - 0.3, ny / 2 + 0.2, nz / 2 + 0.4, 3.0], [7.5, 2.2, 3.1, 2.0]], np.float32)
     p = make(nx, ny, nz, tauRho=0.8, tauPhi=0.9, storage=storage)
