@@ -6,11 +6,18 @@
 // Schedule.  The forward trajectory s^0 .. s^T is not kept: native state
 // snapshots (the step's own buffers, 26 distributions) go into a pool of slots
 // sized from the memory budget, and missing states are recomputed from the
-// nearest snapshot.  With c free slots and r sweeps at most
-// beta(c, r) = C(c + r, r) steps can be reversed; a segment [s, e) with its
-// start stored is split at m = e - min(beta(c - 1, r), e - s - 1) with r the
-// smallest sweep count that covers it: m is stored, [m, e) is reversed with
-// c - 1 free slots, then [s, m) with c (Griewank's binomial checkpointing).
+// nearest snapshot (Griewank's binomial checkpointing).  A segment [s, e) of
+// length l with its start stored and c free slots has n = c + 1 snapshots;
+// with r sweeps at most beta(n, r) = C(n + r, r) steps can be reversed, and
+// the minimum of forward steps, r l - beta(n + 1, r - 1) for the smallest r
+// with beta(n, r) >= l, is reached when the first checkpoint m lies in
+//   [max(beta(n, r - 2), l - beta(n - 1, r)), min(beta(n, r - 1), l - beta(n - 1, r - 1))]
+// steps from s (found by dynamic programming over the recursion below, and
+// checked against the formula): m is stored, [m, e) is reversed with c - 1
+// free slots, then [s, m) with c.  The lower end of the range is taken.
+// Measured on the recursion: 20 000 steps with 44 slots take 62 709 forward
+// steps (the minimum is 62 705), against 76 692 when m is placed so that the
+// right part is as long as c - 1 slots allow.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -333,10 +340,11 @@ struct Adjoint {
             }
             return LBM_OK;
         }
+        const int n = cfree + 1;
         int r = 1;
-        while (beta(cfree, r) < (double)len) r++;
-        const long long right = std::min<long long>((long long)beta(cfree - 1, r), len - 1);
-        const long long m = e - right;
+        while (beta(n, r) < (double)len) r++;
+        const double lo = std::max(r >= 2 ? beta(n, r - 2) : 1.0, (double)len - beta(n - 1, r));
+        const long long m = s + std::max<long long>(1, std::min<long long>((long long)lo, len - 1));
         const int sj = take_slot();
         if (sj < 0) return fail(LBM_ESTATE, "adjoint: checkpoint pool exhausted");
         if ((rc = advance_to_slot(si, s, m, sj))) return rc;
