@@ -220,6 +220,14 @@ int lbm_objective(lbm_ctx *c, const lbm_adjoint_opts *o, double *J);
  * Synchronises the context's stream. */
 int lbm_adjoint_release(lbm_ctx *c);
 
+/* Forward steps lbm_step_adjoint runs for nsteps steps with `slots` checkpoint
+ * slots (the initial state included; a budget of B bytes gives
+ * floor(B / snapshot bytes) slots, a snapshot being the state's 26
+ * distributions in its storage format), recomputation and the terminal state
+ * included: the same schedule, not run.  For planning a budget; no counterpart
+ * in the reference.  -1 if nsteps or slots is below 1. */
+long long lbm_adjoint_forward_steps(long long nsteps, int slots);
+
 /* Largest box lbm_stats_noalloc accepts: 512^3 nodes. */
 #define LBM_NOALLOC_MAX_NODES 134217728LL
 /* Number of doubles lbm_stats_noalloc writes. */

@@ -24,7 +24,7 @@ EXPORTS = [
     "lbm_get_dist", "lbm_set_dist", "lbm_steps_done", "lbm_stream", "lbm_sync", "lbm_destroy",
     "lbm_strerror", "lbm_last_error", "lbm_stats_noalloc", "lbm_step_adjoint",
     "lbm_objective", "lbm_stats_fields", "lbm_pressure", "lbm_device_name", "lbm_adjoint_release",
-    "lbm_wait_selftest",
+    "lbm_wait_selftest", "lbm_adjoint_forward_steps",
 ]
 OBJECTIVES = {"light_uz_mean": 0, "light_z_centroid": 1}
 
@@ -112,6 +112,8 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.lbm_objective.argtypes = [C.c_void_p, C.POINTER(AdjointOpts), C.POINTER(C.c_double)]
     lib.lbm_adjoint_release.argtypes = [C.c_void_p]
     lib.lbm_wait_selftest.argtypes = [C.c_void_p]
+    lib.lbm_adjoint_forward_steps.argtypes = [C.c_longlong, C.c_int]
+    lib.lbm_adjoint_forward_steps.restype = C.c_longlong
     lib.lbm_stats_fields.argtypes = [C.c_void_p, C.POINTER(StatsOut), _F, _F, _F, _F, _F]
     lib.lbm_pressure.argtypes = [C.c_void_p, _F]
     lib.lbm_device_name.argtypes = [C.c_int, C.c_char_p, C.c_int, C.POINTER(C.c_double)]
@@ -156,6 +158,11 @@ def make_params(nx: int, ny: int, nz: int, *, rhoL: float, rhoH: float, tauRho: 
     p.width, p.sigma, p.Gamma, p.Eo, p.rc0 = width, sigma, Gamma, Eo, rc0
     p.storage, p.device, p.compat = STORAGE[storage], device, int(compat)
     return p
+
+
+def adjoint_forward_steps(nsteps: int, slots: int) -> int:
+    """lbm_adjoint_forward_steps: forward steps of the checkpointing schedule (not run)."""
+    return int(load().lbm_adjoint_forward_steps(int(nsteps), int(slots)))
 
 
 def read_inputs(directory: str | os.PathLike, max_bubbles: int = 4096):

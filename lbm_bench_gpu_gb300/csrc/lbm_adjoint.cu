@@ -58,6 +58,49 @@ struct Carver {
     }
 };
 
+// First checkpoint of a segment of len >= 2 steps with its start stored and
+// cfree >= 1 free slots: the lower end of Griewank's optimal interval (see the
+// file comment).
+long long split_point(long long len, int cfree)
+{
+    const int n = cfree + 1;
+    int r = 1;
+    while (beta(n, r) < (double)len) r++;
+    const double lo = std::max(r >= 2 ? beta(n, r - 2) : 1.0, (double)len - beta(n - 1, r));
+    return std::max<long long>(1, std::min<long long>((long long)lo, len - 1));
+}
+
+// Forward steps of revolve(s, s + len, cfree) below, without running them
+// (the same recursion; `terminal` is whether lambda^T is still to be built).
+long long schedule_steps(long long T, long long s, long long e, int cfree, bool &terminal)
+{
+    const long long len = e - s;
+    if (len <= 0) return 0;
+    if (len == 1) {
+        if (terminal) {
+            terminal = false;
+            return 1;
+        }
+        return 0;
+    }
+    if (cfree == 0) {
+        long long steps = 0;
+        for (long long j = e - 1; j >= s; j--) {
+            if (terminal) {
+                terminal = false;
+                steps += T - s;
+            }
+            if (j != s) steps += j - s;
+        }
+        return steps;
+    }
+    const long long m = s + split_point(len, cfree);
+    long long steps = m - s;
+    steps += schedule_steps(T, m, e, cfree - 1, terminal);
+    steps += schedule_steps(T, s, m, cfree, terminal);
+    return steps;
+}
+
 struct Snapshot {
     long long step = -1;
     bool f_streamed = false, g_odd_next = false;
@@ -340,11 +383,7 @@ struct Adjoint {
             }
             return LBM_OK;
         }
-        const int n = cfree + 1;
-        int r = 1;
-        while (beta(n, r) < (double)len) r++;
-        const double lo = std::max(r >= 2 ? beta(n, r - 2) : 1.0, (double)len - beta(n - 1, r));
-        const long long m = s + std::max<long long>(1, std::min<long long>((long long)lo, len - 1));
+        const long long m = s + split_point(len, cfree);
         const int sj = take_slot();
         if (sj < 0) return fail(LBM_ESTATE, "adjoint: checkpoint pool exhausted");
         if ((rc = advance_to_slot(si, s, m, sj))) return rc;
@@ -578,4 +617,12 @@ extern "C" int lbm_adjoint_release(lbm_ctx *c)
     c->adj_work = c->adj_slots = nullptr;
     c->adj_work_bytes = c->adj_slot_bytes = 0;
     return LBM_OK;
+}
+
+extern "C" long long lbm_adjoint_forward_steps(long long nsteps, int slots)
+{
+    if (nsteps < 1 || slots < 1) return -1;
+    const long long nslots = std::min<long long>(slots, nsteps + 1);
+    bool terminal = true;
+    return schedule_steps(nsteps, 0, nsteps, (int)(nslots - 1), terminal);
 }

@@ -54,6 +54,9 @@ def test_checkpoint_budget_does_not_change_the_gradient(lib):
         tight = lat.adjoint(20, -3e-5, "light_uz_mean", 6, checkpoint_bytes=3.5 * snap)
     assert full["slots"] == 21 and tight["slots"] == 3
     assert full["forward_steps"] == 20 and tight["forward_steps"] > 20
+    # the planner runs the same schedule without stepping
+    assert tight["forward_steps"] == capi.adjoint_forward_steps(20, 3)
+    assert full["forward_steps"] == capi.adjoint_forward_steps(20, 21)
     assert tight["J"] == full["J"] and tight["dJ_dgrav"] == full["dJ_dgrav"]
     assert np.array_equal(tight["dJ_dphi0"], full["dJ_dphi0"])
 
