@@ -491,6 +491,7 @@ void setup(Adjoint &A, lbm_ctx *c, const lbm_adjoint_opts *o)
 
 extern "C" int lbm_objective(lbm_ctx *c, const lbm_adjoint_opts *o, double *J)
 {
+    const lbm::Range nvtx_range("lbm_objective");
     int rc = check_opts(c, o, J, "lbm_objective");
     if (rc) return rc;
     Adjoint A;
@@ -534,6 +535,7 @@ extern "C" int lbm_objective(lbm_ctx *c, const lbm_adjoint_opts *o, double *J)
 
 extern "C" int lbm_step_adjoint(lbm_ctx *c, const lbm_adjoint_opts *o, lbm_adjoint_out *out)
 {
+    const lbm::Range nvtx_range("lbm_step_adjoint");
     int rc0 = check_opts(c, o, out, "lbm_step_adjoint");
     if (rc0) return rc0;
     const auto t0 = std::chrono::steady_clock::now();

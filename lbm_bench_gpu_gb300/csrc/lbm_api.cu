@@ -225,6 +225,7 @@ int cuda_fail(cudaError_t e, const char *what)
 extern "C" int lbm_init(lbm_ctx **out, const lbm_params *p, const float *phi0, const float *rho0, const float *ux0,
                         const float *uy0, const float *uz0, const float *phi_ghost)
 {
+    const lbm::Range nvtx_range("lbm_init");
     if (!phi0 || !rho0) return fail(LBM_EINVAL, "phi0 and rho0 are required");
     lbm_ctx *c = nullptr;
     int rc = create(&c, p);
@@ -262,6 +263,7 @@ extern "C" int lbm_init(lbm_ctx **out, const lbm_params *p, const float *phi0, c
 
 extern "C" int lbm_init_bubbles(lbm_ctx **out, const lbm_params *p, const float *bubbles, int nbubbles)
 {
+    const lbm::Range nvtx_range("lbm_init_bubbles");
     if (nbubbles < 0 || (nbubbles > 0 && !bubbles)) return fail(LBM_EINVAL, "bad bubble list");
     lbm_ctx *c = nullptr;
     int rc = create(&c, p);
@@ -293,6 +295,7 @@ extern "C" int lbm_init_bubbles(lbm_ctx **out, const lbm_params *p, const float 
 
 extern "C" int lbm_step(lbm_ctx *c, int nsteps, float grav)
 {
+    const lbm::Range nvtx_range("lbm_step");
     if (!c) return fail(LBM_EINVAL, "context is NULL");
     if (nsteps < 0) return fail(LBM_EINVAL, "nsteps < 0");
     if (!std::isfinite(grav)) return fail(LBM_EINVAL, "grav is not finite");
@@ -312,6 +315,7 @@ extern "C" int lbm_step(lbm_ctx *c, int nsteps, float grav)
 
 extern "C" int lbm_stats(lbm_ctx *c, lbm_stats_out *s, float *phi, float *rho, float *ux, float *uy, float *uz)
 {
+    const lbm::Range nvtx_range("lbm_stats");
     if (!c) return fail(LBM_EINVAL, "context is NULL");
     const size_t n = (size_t)c->box.n, bytes = sizeof(float) * n;
     if (s) {
@@ -414,6 +418,7 @@ int fill_stats(const lbm_ctx *c, const double *r, lbm_stats_out *s)
 
 extern "C" int lbm_get_dist(lbm_ctx *c, float *f, float *g)
 {
+    const lbm::Range nvtx_range("lbm_get_dist");
     if (!c) return fail(LBM_EINVAL, "context is NULL");
     if (!f && !g) return LBM_OK;
     const size_t n = (size_t)c->box.n;
@@ -436,6 +441,7 @@ extern "C" int lbm_get_dist(lbm_ctx *c, float *f, float *g)
 
 extern "C" int lbm_set_dist(lbm_ctx *c, const float *f, const float *g)
 {
+    const lbm::Range nvtx_range("lbm_set_dist");
     if (!c || !f || !g) return fail(LBM_EINVAL, "NULL argument");
     const size_t n = (size_t)c->box.n;
     LBM_CUDA(cudaStreamSynchronize(c->stream), "lbm_set_dist");

@@ -7,6 +7,7 @@
 #include <string>
 
 #include "lbm_gb300.h"
+#include <nvtx3/nvToolsExt.h>   // header-only; no-ops unless a profiler is attached
 
 namespace lbm {
 
@@ -205,4 +206,13 @@ inline StepView state_view(lbm_ctx *c, int in)
 }
 int fail(int code, const std::string &msg);
 int cuda_fail(cudaError_t e, const char *what);
+
+// NVTX range over a C-ABI call (host side: the calls queue work on the
+// context's stream), for timelines of the library's work.
+struct Range {
+    explicit Range(const char *name) { nvtxRangePushA(name); }
+    ~Range() { nvtxRangePop(); }
+    Range(const Range &) = delete;
+    Range &operator=(const Range &) = delete;
+};
 }  // namespace lbm

@@ -357,8 +357,6 @@ template <typename ST, bool ODD>
 __global__ void __launch_bounds__(NTA, ZSC_ADJ_MIN_BLOCKS) adjoint_local_kernel(Box b, StepConst c, float phiStar, Quant q, AdjIn a)
 {
     __shared__ double red[NTA / 32];
-    const unsigned n = (unsigned)b.n;
-    const ST *__restrict__ g = static_cast<const ST *>(a.g);
     double dg = 0.0;
     const int x = blockIdx.x * TXA + threadIdx.x, y = blockIdx.y * TYA + threadIdx.y;
     if (blockIdx.z < (unsigned)b.nz) prefetch_plane<ST>(b, a, blockIdx.z);
