@@ -263,6 +263,19 @@ long long lbm_adjoint_forward_steps(long long nsteps, int slots);
 int lbm_stats_noalloc(const lbm_params *p, const float *phi, const float *rho, const float *ux,
                       const float *uy, const float *uz, double *raw_out, void *stream);
 
+/* Checkpoint / resume (no counterpart in the reference, whose VTK files are
+ * output only): a snapshot of the context's state in its native form (the
+ * current f_0 and f_1..f_6, g in its AA layout, the five moment fields, the
+ * 16-bit storage map, the step count), into caller-owned host memory of
+ * lbm_state_bytes bytes.  lbm_load_state restores it into a context of the
+ * same box and storage format (created with the same parameters); stepping on
+ * from there gives bit for bit what the saved context would have given.
+ * LBM_EINVAL for a buffer that is not a snapshot or another box or format.
+ * Both synchronise. */
+long long lbm_state_bytes(const lbm_ctx *c);
+int lbm_save_state(lbm_ctx *c, void *buf);
+int lbm_load_state(lbm_ctx *c, const void *buf);
+
 /* Steps taken since lbm_init. */
 long long lbm_steps_done(const lbm_ctx *c);
 

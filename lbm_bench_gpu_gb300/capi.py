@@ -24,7 +24,7 @@ EXPORTS = [
     "lbm_get_dist", "lbm_set_dist", "lbm_steps_done", "lbm_stream", "lbm_sync", "lbm_destroy",
     "lbm_strerror", "lbm_last_error", "lbm_stats_noalloc", "lbm_step_adjoint",
     "lbm_objective", "lbm_stats_fields", "lbm_pressure", "lbm_device_name", "lbm_adjoint_release",
-    "lbm_wait_selftest", "lbm_adjoint_forward_steps",
+    "lbm_wait_selftest", "lbm_adjoint_forward_steps", "lbm_state_bytes", "lbm_save_state", "lbm_load_state",
 ]
 OBJECTIVES = {"light_uz_mean": 0, "light_z_centroid": 1}
 
@@ -114,6 +114,10 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.lbm_wait_selftest.argtypes = [C.c_void_p]
     lib.lbm_adjoint_forward_steps.argtypes = [C.c_longlong, C.c_int]
     lib.lbm_adjoint_forward_steps.restype = C.c_longlong
+    lib.lbm_state_bytes.argtypes = [C.c_void_p]
+    lib.lbm_state_bytes.restype = C.c_longlong
+    lib.lbm_save_state.argtypes = [C.c_void_p, C.c_void_p]
+    lib.lbm_load_state.argtypes = [C.c_void_p, C.c_void_p]
     lib.lbm_stats_fields.argtypes = [C.c_void_p, C.POINTER(StatsOut), _F, _F, _F, _F, _F]
     lib.lbm_pressure.argtypes = [C.c_void_p, _F]
     lib.lbm_device_name.argtypes = [C.c_int, C.c_char_p, C.c_int, C.POINTER(C.c_double)]
@@ -274,6 +278,17 @@ class Lattice:
         J = C.c_double()
         check(load().lbm_objective(self._h, C.byref(o), C.byref(J)), "lbm_objective")
         return float(J.value)
+
+    def save_state(self) -> np.ndarray:
+        """lbm_save_state: the context's native state as a byte array (checkpoint)."""
+        buf = np.empty(int(load().lbm_state_bytes(self._h)), np.uint8)
+        check(load().lbm_save_state(self._h, buf.ctypes.data_as(C.c_void_p)), "lbm_save_state")
+        return buf
+
+    def load_state(self, buf: np.ndarray) -> None:
+        """lbm_load_state: restore a snapshot from save_state (resume)."""
+        buf = np.ascontiguousarray(buf, dtype=np.uint8)
+        check(load().lbm_load_state(self._h, buf.ctypes.data_as(C.c_void_p)), "lbm_load_state")
 
     def wait_selftest(self) -> int:
         """lbm_wait_selftest: the status code a timed-out bounded wait reports (LBM_ETIMEOUT)."""

@@ -457,6 +457,93 @@ extern "C" int lbm_set_dist(lbm_ctx *c, const float *f, const float *g)
     return rc;
 }
 
+// ---- state snapshots (checkpoint / resume) ----
+// Layout of a snapshot (host memory, this machine's byte order): the header,
+// then f_0 (n floats) and f_1..f_6 (6 n storage elements) of the current half,
+// g (19 n, AA layout as stored), the five moment fields (5 n floats).
+namespace {
+struct SnapshotHeader {
+    char magic[8];            // "LBMSTATE"
+    int version;              // 1
+    int nx, ny, nz, storage;
+    int f_streamed, g_odd_next;
+    long long steps;
+    lbm::Quant q;             // the 16-bit storage map
+};
+constexpr char kSnapMagic[8] = {'L', 'B', 'M', 'S', 'T', 'A', 'T', 'E'};
+
+size_t snapshot_payload(const lbm_ctx *c)
+{
+    const size_t n = (size_t)c->box.n;
+    return sizeof(float) * n + c->esz * (lbm::kQf - 1 + lbm::kQg) * n + sizeof(float) * 5 * n;
+}
+}  // namespace
+
+extern "C" long long lbm_state_bytes(const lbm_ctx *c)
+{
+    return c ? (long long)(sizeof(SnapshotHeader) + snapshot_payload(c)) : -1;
+}
+
+extern "C" int lbm_save_state(lbm_ctx *c, void *buf)
+{
+    const lbm::Range nvtx_range("lbm_save_state");
+    if (!c || !buf) return fail(LBM_EINVAL, "lbm_save_state: NULL argument");
+    SnapshotHeader h;
+    std::memset(&h, 0, sizeof(h));
+    std::memcpy(h.magic, kSnapMagic, sizeof(h.magic));
+    h.version = 1;
+    h.nx = c->box.nx;
+    h.ny = c->box.ny;
+    h.nz = c->box.nz;
+    h.storage = c->p.storage;
+    h.f_streamed = c->st.f_streamed ? 1 : 0;
+    h.g_odd_next = c->st.g_odd_next ? 1 : 0;
+    h.steps = c->st.steps;
+    h.q = c->q;
+    unsigned char *d = static_cast<unsigned char *>(buf);
+    std::memcpy(d, &h, sizeof(h));
+    d += sizeof(h);
+    const size_t n = (size_t)c->box.n, b0 = sizeof(float) * n, bq = c->esz * (lbm::kQf - 1) * n,
+                 bg = c->esz * lbm::kQg * n, bm = sizeof(float) * 5 * n;
+    const lbm::StepView v = view(c, c->st.f_cur);
+    LBM_CUDA(cudaMemcpyAsync(d, v.f0_in, b0, cudaMemcpyDeviceToHost, c->stream), "lbm_save_state");
+    LBM_CUDA(cudaMemcpyAsync(d + b0, v.fq_in, bq, cudaMemcpyDeviceToHost, c->stream), "lbm_save_state");
+    LBM_CUDA(cudaMemcpyAsync(d + b0 + bq, c->st.g, bg, cudaMemcpyDeviceToHost, c->stream), "lbm_save_state");
+    LBM_CUDA(cudaMemcpyAsync(d + b0 + bq + bg, c->st.mom, bm, cudaMemcpyDeviceToHost, c->stream), "lbm_save_state");
+    LBM_CUDA(cudaStreamSynchronize(c->stream), "lbm_save_state");
+    return device_error(c);
+}
+
+extern "C" int lbm_load_state(lbm_ctx *c, const void *buf)
+{
+    const lbm::Range nvtx_range("lbm_load_state");
+    if (!c || !buf) return fail(LBM_EINVAL, "lbm_load_state: NULL argument");
+    SnapshotHeader h;
+    std::memcpy(&h, buf, sizeof(h));
+    if (std::memcmp(h.magic, kSnapMagic, sizeof(h.magic)) != 0 || h.version != 1)
+        return fail(LBM_EINVAL, "lbm_load_state: not a state snapshot of this format");
+    if (h.nx != c->box.nx || h.ny != c->box.ny || h.nz != c->box.nz || h.storage != c->p.storage)
+        return fail(LBM_EINVAL, "lbm_load_state: the snapshot's box or storage format differs from the context's");
+    if (h.steps < 0) return fail(LBM_EINVAL, "lbm_load_state: bad step count");
+    const unsigned char *d = static_cast<const unsigned char *>(buf) + sizeof(h);
+    const size_t n = (size_t)c->box.n, b0 = sizeof(float) * n, bq = c->esz * (lbm::kQf - 1) * n,
+                 bg = c->esz * lbm::kQg * n, bm = sizeof(float) * 5 * n;
+    if (int rc = lbm_sync(c)) return rc;
+    const lbm::StepView v = view(c, 0);
+    LBM_CUDA(cudaMemcpyAsync(c->st.f0, d, b0, cudaMemcpyHostToDevice, c->stream), "lbm_load_state");
+    LBM_CUDA(cudaMemcpyAsync(const_cast<void *>(v.fq_in), d + b0, bq, cudaMemcpyHostToDevice, c->stream),
+             "lbm_load_state");
+    LBM_CUDA(cudaMemcpyAsync(c->st.g, d + b0 + bq, bg, cudaMemcpyHostToDevice, c->stream), "lbm_load_state");
+    LBM_CUDA(cudaMemcpyAsync(c->st.mom, d + b0 + bq + bg, bm, cudaMemcpyHostToDevice, c->stream), "lbm_load_state");
+    LBM_CUDA(cudaStreamSynchronize(c->stream), "lbm_load_state");
+    c->st.f_cur = 0;
+    c->st.f_streamed = h.f_streamed != 0;
+    c->st.g_odd_next = h.g_odd_next != 0;
+    c->st.steps = h.steps;
+    c->q = h.q;
+    return LBM_OK;
+}
+
 extern "C" long long lbm_steps_done(const lbm_ctx *c) { return c ? c->st.steps : -1; }
 
 extern "C" void *lbm_stream(const lbm_ctx *c) { return c ? (void *)c->stream : nullptr; }
