@@ -91,6 +91,38 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     return LIB
 
 
+CHECKED_BUILD = PKG / "_build_checked"
+CHECKED_LIB = PKG / "liblbm_gb300_checked.so"
+
+
+def build_checked(force: bool = False) -> Path:
+    """The library with ZSC_CHECKED=1 (every global store and cp.async source of
+    the step kernel checked against its field; an index outside it sets an error
+    bit and the access is skipped), for tests; returns its path."""
+    CHECKED_BUILD.mkdir(exist_ok=True)
+    srcs = _sources()
+
+    def one(src: Path) -> Path:
+        obj = CHECKED_BUILD / (src.name + ".o")
+        if not force and not _stale(obj, [src, *_headers()]):
+            return obj
+        if src.suffix == ".cu":
+            cmd = [nvcc(), *NVCC_FLAGS, "-DZSC_CHECKED=1", "-c", str(src), "-o", str(obj)]
+        else:
+            cmd = ["g++", *CXX_FLAGS, "-I", cuda_include(), "-c", str(src), "-o", str(obj)]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"compile failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+        return obj
+
+    with ThreadPoolExecutor(max_workers=max(2, min(8, os.cpu_count() or 2))) as ex:
+        objs = list(ex.map(one, srcs))
+    if force or _stale(CHECKED_LIB, objs):
+        subprocess.run([nvcc(), *ARCH, "-shared", "-cudart", "static", "-o", str(CHECKED_LIB), *map(str, objs)],
+                       check=True)
+    return CHECKED_LIB
+
+
 if __name__ == "__main__":
     build(force="--force" in sys.argv, verbose=True)
     print(LIB)

@@ -94,7 +94,8 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
     global _lib
     if _lib is not None and path is None:
         return _lib
-    p = Path(path) if path else LIB_PATH
+    # LBM_GB300_LIB selects another build of the library (the tests' checked build)
+    p = Path(path) if path else Path(os.environ.get("LBM_GB300_LIB", LIB_PATH))
     if not p.exists():
         raise OSError(f"{p} not found: build it with `python -m lbm_bench_gpu_gb300.build`")
     lib = C.CDLL(str(p))

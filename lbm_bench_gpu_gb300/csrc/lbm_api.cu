@@ -193,11 +193,15 @@ int init_from_mom(lbm_ctx *c, const float *ghost_lo, const float *ghost_hi)
     return rc;
 }
 
-// LBM_ETIMEOUT when a step kernel gave up a bounded wait (the flag stays set).
+// The step kernel's error flag (it stays set): bit 1 a bounded wait gave up
+// (LBM_ETIMEOUT), bit 2 a shared-memory stage was misaligned, bit 4 a checked
+// build found a global index outside its field (LBM_ECUDA).
 int device_error(lbm_ctx *c)
 {
     int flag = 0;
     LBM_CUDA(cudaMemcpy(&flag, c->err, sizeof(int), cudaMemcpyDeviceToHost), "error flag");
+    if (flag & 4) return fail(LBM_ECUDA, "a checked build found a global index outside its field");
+    if (flag & 2) return fail(LBM_ECUDA, "a step kernel's shared-memory stage was misaligned for TMA");
     if (flag) return fail(LBM_ETIMEOUT, "a step kernel timed out waiting for its staged data");
     return LBM_OK;
 }

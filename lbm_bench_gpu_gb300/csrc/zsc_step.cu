@@ -181,6 +181,24 @@ __device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+
+// Checked builds (ZSC_CHECKED=1, a separate library for testing): every global
+// store and cp.async source is checked against its field's extent first; an
+// index out of range sets bit 4 of the context's error flag and the access is
+// skipped, in place of the memory checker.  Other builds compile the checks away.
+#ifndef ZSC_CHECKED
+#define ZSC_CHECKED 0
+#endif
+__device__ __forceinline__ bool in_field(long long idx, int count, long long n, int *err)
+{
+#if ZSC_CHECKED
+    if (idx < 0 || idx + count > n) {
+        atomicOr(err, 4);
+        return false;
+    }
+#endif
+    return true;
+}
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
 // ---- mbarrier + TMA (bulk tensor copy) ----
@@ -457,12 +475,14 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
         }
         const unsigned zb = (unsigned)wrap(p, b.nz) * (unsigned)b.nxy;
         unsigned char *st = fstage(p);
-        if (f0_issuer) cp_async16(f0part(st) + f0_dst, P.f0in + (zb + (unsigned)f0_xy));
+        if (f0_issuer && in_field((long long)zb + f0_xy, 4, b.n, P.err))
+            cp_async16(f0part(st) + f0_dst, P.f0in + (zb + (unsigned)f0_xy));
         if (fq_issuer) {
             ST *dst = fqpart(st) + fq_dst;
             const unsigned base = zb + (unsigned)fq_xy;
 #pragma unroll
-            for (int a = 0; a < kQf - 1; a++) cp_async16(dst + a * FR * W, P.fin[a] + base);
+            for (int a = 0; a < kQf - 1; a++)
+                if (in_field(base, E, b.n, P.err)) cp_async16(dst + a * FR * W, P.fin[a] + base);
         }
     };
 
@@ -517,7 +537,7 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
             const unsigned base = (unsigned)z * (unsigned)b.nxy + (unsigned)(g_row_0 + g_x_hi);
             for_my_dirs([&](auto d) {
                 constexpr int i = decltype(d)::value;
-                cp_async16(dst + i * TY * W + E + E * g_k, P.gin[i] + base);
+                if (in_field(base, E, b.n, P.err)) cp_async16(dst + i * TY * W + E + E * g_k, P.gin[i] + base);
             });
         } else {
             const unsigned zb0 = (unsigned)z * (unsigned)b.nxy;
@@ -530,12 +550,15 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
                 const int row = cy > 0 ? g_row_p : (cy < 0 ? g_row_m : g_row_0);
                 const ST *src = P.gin[kOpp(i)] + (zb + (unsigned)row);
                 ST *d_row = dst + i * TY * W;
+                const long long r0 = (long long)zb + row;   // row start in the field
                 if (cx > 0) {
-                    cp_async16(d_row + E * g_k, src + g_x_lo);
-                    if (g_k == 0) cp_async16(d_row + TX, src + (x0 + TX - E));
+                    if (in_field(r0 + g_x_lo, E, b.n, P.err)) cp_async16(d_row + E * g_k, src + g_x_lo);
+                    if (g_k == 0 && in_field(r0 + x0 + TX - E, E, b.n, P.err))
+                        cp_async16(d_row + TX, src + (x0 + TX - E));
                 } else {
-                    cp_async16(d_row + E + E * g_k, src + g_x_hi);
-                    if (cx < 0 && g_k == 0) cp_async16(d_row + TX + E, src + g_x_wrap);
+                    if (in_field(r0 + g_x_hi, E, b.n, P.err)) cp_async16(d_row + E + E * g_k, src + g_x_hi);
+                    if (cx < 0 && g_k == 0 && in_field(r0 + g_x_wrap, E, b.n, P.err))
+                        cp_async16(d_row + TX + E, src + g_x_wrap);
                 }
             });
         }
@@ -702,7 +725,7 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
         const float uy = ((g[3] - g[4]) + d7 - d9 + d15 + d17) * invRhoG;
         const float uz = ((g[5] - g[6]) + d11 - d13 + d15 - d17) * invRhoG;
         const unsigned id = node_index(b, x, y, z);
-        if (write_moments) {
+        if (write_moments && in_field(id, 1, b.n, P.err)) {
             P.mom[0][id] = pc;
             P.mom[1][id] = rho;
             P.mom[2][id] = ux;
@@ -719,11 +742,13 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
         {
             const float Af = 0.5f * c.Gamma * c.invTauPhi * mu;
             const float a = c.invTauPhiOne;
-            P.f0out[id] = a * fcur[0][0] - 6.0f * Af + c.invTauPhi * pc;
+            if (in_field(id, 1, b.n, P.err)) P.f0out[id] = a * fcur[0][0] - 6.0f * Af + c.invTauPhi * pc;
             // f_1..f_6 in stored units: terms scaled by f_scale
             const float Afk = Fm::kMapped ? m.Af * mu : Af;
             const float Cf = (Fm::kMapped ? m.Cf : c.invTauPhi * c.invEta2) * pc;
-            auto put = [&](int k, float v) { P.fout[k][id] = Fm::store(v); };
+            auto put = [&](int k, float v) {
+                if (in_field(id, 1, b.n, P.err)) P.fout[k][id] = Fm::store(v);
+            };
             put(0, a * fcur[0][1] + Afk + Cf * usx);
             put(1, a * fcur[0][2] + Afk - Cf * usx);
             put(2, a * fcur[0][3] + Afk + Cf * usy);
@@ -833,7 +858,8 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
             if (!ODD) {
                 // even: own node, reversed slots
 #pragma unroll
-                for (int i = 0; i < kQg; i++) P.g[kOpp(i)][id] = enc(i, qv[i]);
+                for (int i = 0; i < kQg; i++)
+                    if (in_field(id, 1, b.n, P.err)) P.g[kOpp(i)][id] = enc(i, qv[i]);
             } else {
                 // odd: downstream neighbour x + c_i, natural slot i
                 const int o_zm = (z == 0) ? (b.nz - 1) * (int)b.nxy : -(int)b.nxy;
@@ -843,7 +869,8 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
                            + (kCz(i) > 0 ? o_zp : kCz(i) < 0 ? o_zm : 0);
                 };
 #pragma unroll
-                for (int i = 0; i < kQg; i++) P.g[i][id + off(i)] = enc(i, qv[i]);
+                for (int i = 0; i < kQg; i++)
+                    if (in_field((long long)id + off(i), 1, b.n, P.err)) P.g[i][id + off(i)] = enc(i, qv[i]);
             }
         }
 
@@ -917,7 +944,7 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
             const float2 uy = mul(add(add(sub(add(sub(g[3], g[4]), d7), d9), d15), d17), invRhoG);
             const float2 uz = mul(sub(add(sub(add(sub(g[5], g[6]), d11), d13), d15), d17), invRhoG);
             const unsigned id = node_index(b, x, y, z);   // node A (even: 8-byte aligned pairs)
-            if (write_moments) {
+            if (write_moments && in_field(id, 2, b.n, P.err)) {
                 *reinterpret_cast<float2 *>(P.mom[0] + id) = pc;
                 *reinterpret_cast<float2 *>(P.mom[1] + id) = rho;
                 *reinterpret_cast<float2 *>(P.mom[2] + id) = ux;
@@ -932,11 +959,14 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
                 const float2 a2 = splat(c.invTauPhiOne);
                 auto fc = [&](int k) { return make_float2(fcur[0][k], fcur[1][k]); };
                 const float2 Af = mul(splat(0.5f * c.Gamma * c.invTauPhi), mu);
-                *reinterpret_cast<float2 *>(P.f0out + id) =
-                    fma(a2, fc(0), fma(splat(-6.f), Af, mul(splat(c.invTauPhi), pc)));
+                if (in_field(id, 2, b.n, P.err))
+                    *reinterpret_cast<float2 *>(P.f0out + id) =
+                        fma(a2, fc(0), fma(splat(-6.f), Af, mul(splat(c.invTauPhi), pc)));
                 const float2 Afk = mul(splat(m.Af), mu), Cf = mul(splat(m.Cf), pc);
                 const float2 cux = mul(Cf, usx), cuy = mul(Cf, usy), cuz = mul(Cf, usz);
-                auto put2 = [&](int k, float2 v) { *reinterpret_cast<T2 *>(P.fout[k] + id) = Fm::store2(v); };
+                auto put2 = [&](int k, float2 v) {
+                    if (in_field(id, 2, b.n, P.err)) *reinterpret_cast<T2 *>(P.fout[k] + id) = Fm::store2(v);
+                };
                 put2(0, fma(a2, fc(1), add(Afk, cux)));
                 put2(1, fma(a2, fc(2), sub(Afk, cux)));
                 put2(2, fma(a2, fc(3), add(Afk, cuy)));
@@ -987,7 +1017,8 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
                 if (!ODD) {
                     // even: own nodes, reversed slots
 #pragma unroll
-                    for (int i = 0; i < kQg; i++) *reinterpret_cast<T2 *>(P.g[kOpp(i)] + id) = Fm::store2(qv[i]);
+                    for (int i = 0; i < kQg; i++)
+                        if (in_field(id, 2, b.n, P.err)) *reinterpret_cast<T2 *>(P.g[kOpp(i)] + id) = Fm::store2(qv[i]);
                 } else {
                     // odd: downstream neighbours x + c_i, natural slot i; a pair
                     // moved along x is not 32-bit aligned, so those directions
@@ -1003,10 +1034,13 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
                                         (kCz(i) > 0 ? o_zp : kCz(i) < 0 ? o_zm : 0);
                         const T2 h = Fm::store2(qv[i]);
                         if (kCx(i) == 0) {
-                            *reinterpret_cast<T2 *>(P.g[i] + id + oyz) = h;
+                            if (in_field((long long)id + oyz, 2, b.n, P.err))
+                                *reinterpret_cast<T2 *>(P.g[i] + id + oyz) = h;
                         } else {
-                            P.g[i][id + oyz + (kCx(i) > 0 ? 1 : oA_xm)] = h.x;
-                            P.g[i][id + 1 + oyz + (kCx(i) > 0 ? oB_xp : -1)] = h.y;
+                            const unsigned ia = id + oyz + (kCx(i) > 0 ? 1 : oA_xm);
+                            const unsigned ib = id + 1 + oyz + (kCx(i) > 0 ? oB_xp : -1);
+                            if (in_field(ia, 1, b.n, P.err)) P.g[i][ia] = h.x;
+                            if (in_field(ib, 1, b.n, P.err)) P.g[i][ib] = h.y;
                         }
                     }
                 }
