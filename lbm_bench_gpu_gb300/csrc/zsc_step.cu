@@ -104,7 +104,9 @@ constexpr int threads_of() { return use_pair<ST>() ? NT / 2 : NT; }
 #endif
 // odd steps by TMA too (19 per-direction copies per plane on interior tiles):
 // measured slower than cp.async (256^3: FP16 one node per thread 33.7k vs 36.2k,
-// two nodes per thread 39.5k vs 41.9k; FP32 26.7k vs 27.2k MLUPS), so off
+// two nodes per thread 39.5k vs 41.9k; FP32 26.7k vs 27.2k MLUPS), so off.
+// One 1-d bulk copy (cp.async.bulk) per shifted row instead, 152 per plane on
+// every tile, was slower still: FP16 36.8k vs 42.3k, FP32 26.5k vs 27.6k.
 #ifndef ZSC_TMA_ODD
 #define ZSC_TMA_ODD 0
 #endif
