@@ -115,6 +115,24 @@ def test_init_rejects_bad_params_without_touching_the_gpu(change, code):
     assert e.value.code == code
 
 
+@pytest.mark.parametrize("dims,change", [
+    ((1024, 1024, 256), {}),                 # 19 n >= 2^32: beyond 32-bit element indexing
+    ((32, 32, 32), dict(width=0.0)),
+    ((32, 32, 32), dict(tauPhi=-1.0)),
+    ((32, 32, 32), dict(Eo=1.0, rc0=0.0)),   # gravity from Eo needs a positive Rc0
+])
+def test_init_bubbles_rejects_bad_params_without_touching_the_gpu(dims, change):
+    from lbm_bench_gpu_gb300 import capi
+    kw = dict(rhoL=0.1, rhoH=1.0, tauRho=0.7, tauPhi=1.0, width=4.0, sigma=1e-3, Gamma=1.0)
+    kw.update(change)
+    p = capi.make_params(*dims, **kw)
+    # validation comes before any CUDA call: here, without a GPU, anything
+    # that got past it would fail with a CUDA error code instead
+    with pytest.raises(capi.LbmError) as e:
+        capi.Lattice.from_bubbles(p, np.zeros((0, 4), np.float32))
+    assert e.value.code == capi.LBM_EINVAL
+
+
 def test_strerror_covers_codes(lib):
     from lbm_bench_gpu_gb300 import capi
     for code in range(8):
