@@ -11,7 +11,9 @@
   (``oracle/ref_harness/mpi_stub/mpi.h``) into ``oracle/_ref/lbm_ref_cuda``:
   the reference's GPU step, timed beside the product as a baseline.  CUDA 13
   no longer declares ``cudaThreadSynchronize``; it is mapped to
-  ``cudaDeviceSynchronize`` on the command line.
+  ``cudaDeviceSynchronize`` on the command line.  The same program is also
+  built without ``-use_fast_math`` (``oracle/_ref/lbm_ref_cuda_exact``), to
+  separate the fast-math share of its differences from this library.
 
 The reference sources are read from ``$LBM_REFERENCE_SRC`` (default: the
 reference checkout's ``src/`` directory at /root/reference/src).  Where that
@@ -51,7 +53,8 @@ REFERENCE_FILES = [
 ]
 # ... and what src/main.cu adds for the GPU program.
 REFERENCE_CUDA_FILES = ["main.cu", "vtksave.c"]
-REF_CUDA_BIN = REF_DIR / "lbm_ref_cuda"
+REF_CUDA_BIN = REF_DIR / "lbm_ref_cuda"               # src/Makefile's flags
+REF_CUDA_EXACT_BIN = REF_DIR / "lbm_ref_cuda_exact"   # the same without -use_fast_math
 
 # Deterministic IEEE float arithmetic on x86-64 and aarch64 alike: no
 # contraction into fused multiply-adds, no fast-math.
@@ -127,11 +130,16 @@ def build_reference_cuda(force: bool = False) -> Path | None:
     stub = HERE / "ref_harness" / "mpi_stub" / "mpi.h"
     deps = [stub] + [src_dir / f for f in REFERENCE_FILES + REFERENCE_CUDA_FILES]
     REF_DIR.mkdir(exist_ok=True)
-    if force or not _newer(REF_CUDA_BIN, deps):
-        cmd = [nvcc, "-O3", "-use_fast_math", "-gencode", "arch=compute_103a,code=sm_103a", "-w",
-               "-DcudaThreadSynchronize=cudaDeviceSynchronize", "-include", "stdlib.h",
-               "-I", str(stub.parent), "-I", str(src_dir), str(src_dir / "main.cu"), "-o", str(REF_CUDA_BIN)]
-        subprocess.run(cmd, check=True)
+    jobs = []
+    for out, flags in ((REF_CUDA_BIN, ["-O3", "-use_fast_math"]), (REF_CUDA_EXACT_BIN, ["-O3"])):
+        if force or not _newer(out, deps):
+            cmd = [nvcc, *flags, "-gencode", "arch=compute_103a,code=sm_103a", "-w",
+                   "-DcudaThreadSynchronize=cudaDeviceSynchronize", "-include", "stdlib.h",
+                   "-I", str(stub.parent), "-I", str(src_dir), str(src_dir / "main.cu"), "-o", str(out)]
+            jobs.append((cmd, subprocess.Popen(cmd)))
+    for cmd, job in jobs:
+        if job.wait() != 0:
+            raise subprocess.CalledProcessError(job.returncode, cmd)
     return REF_CUDA_BIN
 
 
