@@ -102,14 +102,11 @@ constexpr int threads_of() { return use_pair<ST>() ? NT / 2 : NT; }
 #ifndef ZSC_TMA_G
 #define ZSC_TMA_G 1
 #endif
-// odd steps by TMA too (19 per-direction copies per plane on interior tiles):
-// measured slower than cp.async (256^3: FP16 one node per thread 33.7k vs 36.2k,
-// two nodes per thread 39.5k vs 41.9k; FP32 26.7k vs 27.2k MLUPS), so off.
-// One 1-d bulk copy (cp.async.bulk) per shifted row instead, 152 per plane on
-// every tile, was slower still: FP16 36.8k vs 42.3k, FP32 26.5k vs 27.6k.
-#ifndef ZSC_TMA_ODD
-#define ZSC_TMA_ODD 0
-#endif
+// Odd steps stage their shifted g rows with cp.async: one TMA tensor copy per
+// direction (19 per plane, interior tiles) measured slower (256^3: FP16 one
+// node per thread 33.7k vs 36.2k, two nodes per thread 39.5k vs 41.9k; FP32
+// 26.7k vs 27.2k MLUPS), and one 1-d bulk copy (cp.async.bulk) per shifted row,
+// 152 per plane, slower still (FP16 36.8k vs 42.3k, FP32 26.5k vs 27.6k).
 // the P_f planes by TMA on interior tiles (f_0 box W0 x FR, f_1..f_6 box
 // W x FR x 6), for the 16-bit formats: measured at 256^3 (same GPU, 500
 // steps), FP16 36 250 -> 37 060 MLUPS, while FP32 drops 27 110 -> 26 560 with
@@ -119,7 +116,6 @@ constexpr int threads_of() { return use_pair<ST>() ? NT / 2 : NT; }
 #define ZSC_TMA_F 1
 #endif
 constexpr bool kUseTma = ZSC_TMA_G != 0;
-constexpr bool kUseTmaOdd = ZSC_TMA_ODD != 0;
 constexpr bool kUseTmaF = ZSC_TMA_F != 0;
 template <typename ST>
 constexpr bool use_tma_f() { return kUseTmaF && (sizeof(ST) == 2 || ZSC_TMA_F == 2); }
@@ -346,9 +342,9 @@ StepMap step_map(const StepConst &c, const Quant &q)
     return m;
 }
 
-// TMA: the g rows come by tensor copies (gmap): even steps one copy per plane
-// in the dense layout [field][TY][TX]; odd steps, on interior tiles, one copy
-// per direction into the [dir][TY][W] rows.  Without TMA gmap is unused.
+// TMA: on even steps the g tile comes by one tensor copy per plane (gmap) in
+// the dense layout [field][TY][TX]; odd steps stage their shifted rows with
+// cp.async into [dir][TY][W].  Without TMA gmap is unused.
 template <typename ST, bool STREAMED, bool ODD, bool TMA>
 __global__ void __launch_bounds__(threads_of<ST>(), Fmt<ST>::kMinBlocks)
 zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const StepMap m, const int tz,
@@ -380,10 +376,7 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
     const int x = x0 + XPT * tx, y = y0 + ty;   // (first) node of the thread
 
     uint64_t *const mbar = reinterpret_cast<uint64_t *>(smem + Gm::MBAR_OFF);
-    // odd step: the rows y0 - 1 .. y0 + TY and columns x0 - E .. x0 + TX + E - 1
-    // must lie inside the box for the shifted tensor copies (uniform per block)
-    const bool tile_tma =
-        TMA && (!ODD || (kUseTmaOdd && x0 - E >= 0 && x0 + TX + E <= b.nx && y0 - 1 >= 0 && y0 + TY + 1 <= b.ny));
+    constexpr bool g_tma = TMA && !ODD;   // the even step's g tile: one TMA copy per plane
     // P_f planes by TMA: the staged rows y0 - 2 .. y0 + TY + 1 and columns
     // x0 - 4 .. x0 + TX + 3 (f_0) / x0 - E .. x0 + TX + E - 1 (f_1..f_6) inside the box
     const bool tile_tma_f = TMA && use_tma_f<ST>() && x0 - 4 >= 0 && x0 - E >= 0 && x0 + TX + 4 <= b.nx &&
@@ -515,24 +508,6 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
             }
             return;
         }
-        if (tile_tma) {
-            // odd step, interior tile: lane i of warp 0 copies direction i, the
-            // reversed slot of the upstream rows x - c_i (columns from x0 - E)
-            if (tid < 32) {
-                if (tid == 0) {
-                    fence_proxy_async();
-                    mbar_expect_tx(&mbar[s], (unsigned)Gm::G_STAGE);
-                }
-                __syncwarp();
-                if (tid < kQg) {
-                    const int i = tid;
-                    const int zc = wrap(z - kCz(i), b.nz);
-                    fence_proxy_async();
-                    tma_load_4d(G + s * G_ELEMS + i * TY * W, &gmap, x0 - E, y0 - kCy(i), zc, kOpp(i), &mbar[s]);
-                }
-            }
-            return;
-        }
         if (!g_issuer) return;
         ST *dst = G + s * G_ELEMS + g_r * W;
         if (!ODD) {
@@ -659,11 +634,11 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
         if constexpr (TMA) {
             // g of plane z: stage j & 1, its (j >> 1)-th use (cp.async tiles
             // were complete at the barrier above)
-            if (tile_tma) late |= !mbar_wait(&mbar[j & 1], (unsigned)(j >> 1) & 1u);
+            if (g_tma) late |= !mbar_wait(&mbar[j & 1], (unsigned)(j >> 1) & 1u);
             if (__syncthreads_or(late)) {
                 if (tid == 0) atomicOr(P.err, 1);
                 // copies still in flight: wait for them (bounded) before leaving
-                if (tile_tma && j + 1 < nzc) mbar_wait(&mbar[(j + 1) & 1], (unsigned)((j + 1) >> 1) & 1u);
+                if (g_tma && j + 1 < nzc) mbar_wait(&mbar[(j + 1) & 1], (unsigned)((j + 1) >> 1) & 1u);
                 if (tile_tma_f && j + 1 < nzc) mbar_wait(fbar(z + 3), fphase(z + 3));
                 return;
             }
@@ -1094,20 +1069,19 @@ constexpr CUtensorMapDataType tensor_type()
 }
 
 // The 19 g arrays at g (n elements each) as one 4-d tensor (x, y, z, field),
-// read in boxes of one plane's tile in all fields (even steps: 32 x 8 x 1 x 19)
-// or of one field's W-wide rows (odd steps: W x 8 x 1 x 1).  Strides are
-// multiples of 16 bytes (nx is a multiple of 32); the base must be 16-byte
-// aligned (a cudaMalloc pointer, or a checkpoint slot offset by whole fields).
+// read in boxes of one plane's tile in all fields (32 x 8 x 1 x 19, the even
+// step).  Strides are multiples of 16 bytes (nx is a multiple of 32); the base
+// must be 16-byte aligned (a cudaMalloc pointer, or a checkpoint slot offset by
+// whole fields).
 template <typename ST>
-bool encode_g_map(const Box &b, const ST *g, bool odd, CUtensorMap *map)
+bool encode_g_map(const Box &b, const ST *g, CUtensorMap *map)
 {
     const EncodeTiled encode = tensor_map_encoder();
     if (!encode) return false;
     const cuuint64_t es = sizeof(ST);
     const cuuint64_t dims[4] = {(cuuint64_t)b.nx, (cuuint64_t)b.ny, (cuuint64_t)b.nz, (cuuint64_t)kQg};
     const cuuint64_t strides[3] = {(cuuint64_t)b.nx * es, (cuuint64_t)b.nxy * es, (cuuint64_t)b.n * es};
-    const cuuint32_t box[4] = {odd ? (cuuint32_t)Geo<ST>::W : (cuuint32_t)TX, (cuuint32_t)TY, 1u,
-                               odd ? 1u : (cuuint32_t)kQg};
+    const cuuint32_t box[4] = {(cuuint32_t)TX, (cuuint32_t)TY, 1u, (cuuint32_t)kQg};
     const cuuint32_t elem[4] = {1u, 1u, 1u, 1u};
     if ((reinterpret_cast<uintptr_t>(g) & 15u) != 0) return false;
     return encode(map, tensor_type<ST>(), 4, const_cast<ST *>(g), dims, strides, box, elem,
@@ -1223,14 +1197,14 @@ cudaError_t launch_typed(const Box &b, const StepConst &c, const Quant &q, const
     if (e == cudaSuccess) e = configure<ST, false, true, true>();
     if (e != cudaSuccess) return e;
     // staging by TMA when the driver encodes every map the step needs: the g
-    // rows (even steps, and odd ones if enabled) and the P_f planes (if enabled)
+    // tile (even steps) and the P_f planes (if enabled)
     CUtensorMap gmap, f0map, fqmap;
     std::memset(&gmap, 0, sizeof(gmap));
     std::memset(&f0map, 0, sizeof(f0map));
     std::memset(&fqmap, 0, sizeof(fqmap));
-    const bool need_g = !odd || kUseTmaOdd;
+    const bool need_g = !odd;
     bool tma = kUseTma && (need_g || use_tma_f<ST>());
-    if (tma && need_g) tma = encode_g_map<ST>(b, gin, odd, &gmap);
+    if (tma && need_g) tma = encode_g_map<ST>(b, gin, &gmap);
     if (tma && use_tma_f<ST>()) tma = encode_f_maps<ST>(b, P.f0in, fin, &f0map, &fqmap);
     const int tz = choose_tz<ST>(b);
     const int nchunks = (b.nz + tz - 1) / tz;
