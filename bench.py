@@ -77,6 +77,16 @@ def workload(size: int, nbubbles: int):
     return inputs.bubbly(size, nbubbles, r_range=r_range, gravity=-1e-6)
 
 
+def workload_config(args, inp, world: int) -> dict:
+    """The `config` object of the JSON line, shared by both arms."""
+    r_range = list((6.0, 10.0) if args.size <= 256 else (6.0, 12.0))
+    return {"workload": f"bubbly_{args.size}: {args.size}^3 periodic, {args.bubbles} bubbles R~U{r_range}, gap>=3, "
+                        "rhoH=1 rhoL=0.1 sigma=1e-3 W=4 tau_rho=0.7 Gamma=1 tau_phi=1, gravity -1e-6 along z",
+            "nx": inp.nx, "ny": inp.ny, "nz": inp.nz, "bubbles": args.bubbles, "storage": args.storage,
+            "seed": 20261203, "parallelism": f"replicas x{world}",
+            "l2": "state >= 1.5 GB >> 129 MB L2: no flush needed"}
+
+
 def params_for(inp, storage="fp32", device=0):
     from lbm_bench_gpu_gb300 import capi
     return capi.make_params(inp.nx, inp.ny, inp.nz, rhoL=inp.rhoL, rhoH=inp.rhoH, tauRho=inp.tauRho,
@@ -308,13 +318,7 @@ def run_ours(args, rank, world, local):
         "metric": METRIC, "value": round(value, 1), "unit": "MLUPS", "n_gpus": world, "steps": K, "warmup": W,
         "ms_per_step": round(ms_step, 5), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32" if args.storage == "fp32" else f"f32 ({args.storage} storage)", "data": "synthetic",
-        "config": {"workload": f"bubbly_{args.size}: {args.size}^3 periodic, {args.bubbles} bubbles "
-                               f"R~U{list((6.0, 10.0) if args.size <= 256 else (6.0, 12.0))}, gap>=3, "
-                               "rhoH=1 rhoL=0.1 sigma=1e-3 W=4 tau_rho=0.7 Gamma=1 tau_phi=1, "
-                               "gravity -1e-6 along z",
-                   "nx": inp.nx, "ny": inp.ny, "nz": inp.nz, "bubbles": args.bubbles, "storage": args.storage,
-                   "seed": 20261203, "parallelism": f"replicas x{world}",
-                   "l2": "state >= 1.5 GB >> 129 MB L2: no flush needed"},
+        "config": workload_config(args, inp, world),
         "hbm_gbs": round(achieved, 1),
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic,
@@ -589,34 +593,52 @@ def run_e2e(args, inp, p, grav, local):
     for k in f0:
         host_in[k][...] = f0[k]
     torch.cuda.synchronize()
+    import ctypes as C
     n_stats = 0
+    t_steps = t_stats = 0.0
     t0 = time.perf_counter()
     lat = capi.Lattice.from_fields(p, host_in["phi"], host_in["rho"], host_in["ux"], host_in["uy"], host_in["uz"])
+    t_init = time.perf_counter() - t0
     done = 0
     while done < K:
         n = min(args.stat_every, K - done)
+        ta = time.perf_counter()
         lat.step(n, grav)
+        lat.sync()
+        tb = time.perf_counter()
         done += n
         lat.stats()
         n_stats += 1
+        t_steps += tb - ta
+        t_stats += time.perf_counter() - tb
+    ta = time.perf_counter()
     s = capi.StatsOut()
-    import ctypes as C
     capi.check(capi.load().lbm_stats(lat._h, C.byref(s), *[capi.fptr(host_out[k]) for k in
                                                              ("phi", "rho", "ux", "uy", "uz")]), "lbm_stats")
+    t_down = time.perf_counter() - ta
     dt = time.perf_counter() - t0
     lat.close()
     h2d = 5 * nodes * 4
     d2h = n_stats * 16 * 8 + 5 * nodes * 4 + 16 * 8
     return {"value": round(nodes * K / dt / 1e6, 1), "unit": "MLUPS",
             "h2d_bytes_per_step": round(h2d / K, 1), "d2h_bytes_per_step": round(d2h / K, 1),
-            "what": f"lbm_init from pinned host phi/rho/u, {K} x lbm_step with lbm_stats every "
-                    f"{args.stat_every} steps, final fields copied back; wall clock {dt:.3f} s"}
+            "breakdown_s": {"init_s": round(t_init, 5), "steps_s": round(t_steps, 5), "stats_s": round(t_stats, 5),
+                            "download_s": round(t_down, 5), "total_s": round(dt, 5)},
+            "steps_only_mlups": round(nodes * K / t_steps / 1e6, 1) if t_steps > 0 else None,
+            "what": f"lbm_init from pinned host phi/rho/u (context allocation, upload, initial equilibrium: "
+                    f"init_s), {K} x lbm_step (steps_s) with lbm_stats every {args.stat_every} steps (stats_s), "
+                    f"final fields copied back (download_s); wall clock {dt:.3f} s"}
 
 
 def run_reference(args, rank, world):
-    """The reference's own kernels on the host CPU (all threads), on a
-    256 x 256 x nz_s slab of the workload so that W + K steps fit in ~2 min."""
-    from lbm_bench_gpu_gb300 import capi, inputs
+    """The reference's own kernels on the host CPU (all threads), on the
+    workload's box, or on a slab of it when W + K steps of the full box would
+    not fit in about a minute.  Nothing of this library is loaded: the
+    reference reads the same properties.in / discrete.in and derives its own
+    constants (its paramRead, src/paramread.c:141-170); its phi comes from the
+    oracle's restatement of its bubble initialisation (src/init.c:39-59),
+    because the workload has more bubbles than its MAX_BUBBLES."""
+    from lbm_bench_gpu_gb300 import inputs
     from oracle.oracle import Oracle, RefCPU, ref_lib
     if rank != 0:
         return None
@@ -624,9 +646,8 @@ def run_reference(args, rank, world):
         return {"impl": "reference", "unavailable": "reference sources not staged (oracle/_ref/src missing)"}
     inp = workload(args.size, args.bubbles)
     K, W = args.steps, args.warmup
-    p = params_for(inp)
-    grav = float(capi.derive(p).grav)
-    o = Oracle.from_params(p)
+    o = Oracle(inp.nx, inp.ny, inp.nz, rhoL=inp.rhoL, rhoH=inp.rhoH, tauRho=inp.tauRho, tauPhi=inp.tauPhi,
+               width=inp.width, sigma=inp.sigma, Gamma=inp.Gamma, Eo=inp.Eo, rc0=inp.rc0)
     phi_full = o.bubble_phi(inp.bubbles).astype(np.float32)   # (nz+2, ny, nx), reference planes
     o.close()
 
@@ -642,6 +663,7 @@ def run_reference(args, rank, world):
 
     # calibrate: seconds per node-step on a 16-plane slab of the full x-y plane
     ref = make_ref(inp.nx, inp.ny, 16)
+    grav = float(ref.constants()["grav"])   # the reference's own derivation from the written inputs
     ref.step(1, grav)
     t0 = time.perf_counter()
     ref.step(2, grav)
@@ -664,13 +686,18 @@ def run_reference(args, rank, world):
     dt = time.perf_counter() - t0
     nodes = nxs * nys * nzs
     value = nodes * K / dt / 1e6
-    sample = (f"reference kernels (src/*.cu compiled for the host CPU), {nxs}x{nys}x{nzs} slab of the "
-              f"{inp.nx}^3 workload, {K} steps after {W} warm-up, {dt:.1f} s")
+    full = (nxs, nys, nzs) == (inp.nx, inp.ny, inp.nz)
+    sample = (f"reference kernels (src/*.cu compiled for the host CPU), "
+              + (f"the full {inp.nx}^3 box" if full else f"{nxs}x{nys}x{nzs} slab of the {inp.nx}^3 workload")
+              + f", {K} steps after {W} warm-up, {dt:.1f} s")
+    config = workload_config(args, inp, world)
+    if not full:
+        config.update({"workload": config["workload"] + f" (slab {nxs}x{nys}x{nzs})", "nx": nxs, "ny": nys,
+                       "nz": nzs})
     return {"metric": METRIC, "value": round(value, 2), "unit": "MLUPS", "n_gpus": world, "steps": K,
             "warmup": W, "ms_per_step": round(dt / K * 1e3, 3), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
-            "config": {"workload": f"bubbly_{args.size} (slab {nxs}x{nys}x{nzs})", "nx": nxs, "ny": nys,
-                       "nz": nzs, "storage": "fp32"},
+            "config": config,
             "cpu_baseline": {"value": round(value, 2), "unit": "MLUPS", "cores": RefCPU.threads(),
                              "kind": "reference", "sample": sample},
             "e2e": {"value": round(value, 2), "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}

@@ -255,11 +255,18 @@ long long lbm_adjoint_forward_steps(long long nsteps, int slots);
  * The per-block partial sums use a 1 MiB array in the library's static device
  * memory, which every GPU that loads the library keeps until the process
  * exits.  That array bounds the box: more than LBM_NOALLOC_MAX_NODES nodes is
- * rejected with LBM_EINVAL.  The first call on a device looks up the array's
- * device address (cudaGetSymbolAddress); make that first call before any
- * stream capture.  All calls share the array: calls whose kernels can overlap
- * on the GPU (other streams, other host threads) race and must be ordered by
- * the caller.  Nothing in the array needs clearing between calls. */
+ * rejected with LBM_EINVAL, and so are parameters whose constants cannot be
+ * derived (tauRho, tauPhi or width not positive, rhoH == rhoL).  The first
+ * call on a device looks up the array's device address
+ * (cudaGetSymbolAddress); under CUDA's lazy module loading (the default) that
+ * first call is also when the driver loads the library's kernels and
+ * reserves the array on that device, which is an allocation by the driver.
+ * Make that first call during set-up, outside the time loop and before any
+ * stream capture; later calls allocate nothing.  A cudaDeviceReset of the
+ * device discards the array: do not call this entry point on that device
+ * again.  All calls share the array: calls whose kernels can overlap on the
+ * GPU (other streams, other host threads) race and must be ordered by the
+ * caller.  Nothing in the array needs clearing between calls. */
 int lbm_stats_noalloc(const lbm_params *p, const float *phi, const float *rho, const float *ux,
                       const float *uy, const float *uz, double *raw_out, void *stream);
 

@@ -471,8 +471,6 @@ int check_opts(lbm_ctx *c, const lbm_adjoint_opts *o, const void *out, const cha
     if (!std::isfinite(o->grav)) return fail(LBM_EINVAL, f + ": grav is not finite");
     if (c->st.steps != 0)
         return fail(LBM_ESTATE, f + ": the context must hold its initial state (no step taken)");
-    cudaError_t e = cudaSetDevice(c->p.device);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
     return LBM_OK;
 }
 
@@ -494,6 +492,7 @@ extern "C" int lbm_objective(lbm_ctx *c, const lbm_adjoint_opts *o, double *J)
     const lbm::Range nvtx_range("lbm_objective");
     int rc = check_opts(c, o, J, "lbm_objective");
     if (rc) return rc;
+    LBM_ON_DEVICE(c->p.device);
     Adjoint A;
     setup(A, c, o);
     const size_t n = A.n;
@@ -538,6 +537,7 @@ extern "C" int lbm_step_adjoint(lbm_ctx *c, const lbm_adjoint_opts *o, lbm_adjoi
     const lbm::Range nvtx_range("lbm_step_adjoint");
     int rc0 = check_opts(c, o, out, "lbm_step_adjoint");
     if (rc0) return rc0;
+    LBM_ON_DEVICE(c->p.device);
     const auto t0 = std::chrono::steady_clock::now();
     cudaError_t e = cudaSuccess;
     Adjoint A;
@@ -611,8 +611,8 @@ extern "C" int lbm_step_adjoint(lbm_ctx *c, const lbm_adjoint_opts *o, lbm_adjoi
 extern "C" int lbm_adjoint_release(lbm_ctx *c)
 {
     if (!c) return fail(LBM_EINVAL, "lbm_adjoint_release: NULL context");
-    cudaError_t e = cudaSetDevice(c->p.device);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    LBM_ON_DEVICE(c->p.device);
+    const cudaError_t e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return cuda_fail(e, "lbm_adjoint_release");
     cudaFree(c->adj_work);
     cudaFree(c->adj_slots);

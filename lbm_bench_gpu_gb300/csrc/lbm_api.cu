@@ -37,10 +37,7 @@ int validate(const lbm_params *p)
     }
     const double n = (double)p->nx * p->ny * p->nz;
     if (n * lbm::kQg >= 4294967296.0) return fail(LBM_EINVAL, "box too large for 32-bit element indexing");
-    if (!(p->tauRho > 0.f) || !(p->tauPhi > 0.f) || !(p->width > 0.f))
-        return fail(LBM_EINVAL, "tauRho, tauPhi and width must be positive");
-    if (!(p->rhoH != p->rhoL)) return fail(LBM_EINVAL, "rhoH must differ from rhoL");
-    if (p->Eo != 0.f && !(p->rc0 > 0.f)) return fail(LBM_EINVAL, "rc0 must be positive when Eo is not zero");
+    if (const char *why = lbm::physics_error(*p)) return fail(LBM_EINVAL, why);
     if (p->storage != LBM_STORAGE_FP32 && p->storage != LBM_STORAGE_FP16 && p->storage != LBM_STORAGE_BF16)
         return fail(LBM_EINVAL, "unknown storage format");
     return LBM_OK;
@@ -59,7 +56,6 @@ int create(lbm_ctx **out, const lbm_params *p)
     *out = nullptr;
     int rc = validate(p);
     if (rc) return rc;
-    LBM_CUDA(cudaSetDevice(p->device), "cudaSetDevice");
     lbm_ctx *c = new (std::nothrow) lbm_ctx();
     if (!c) return fail(LBM_ENOMEM, "host allocation");
     c->p = *p;
@@ -231,6 +227,9 @@ extern "C" int lbm_init(lbm_ctx **out, const lbm_params *p, const float *phi0, c
 {
     const lbm::Range nvtx_range("lbm_init");
     if (!phi0 || !rho0) return fail(LBM_EINVAL, "phi0 and rho0 are required");
+    if (!out) return fail(LBM_EINVAL, "out is NULL");
+    if (int rc0 = validate(p)) return rc0;   // before any CUDA call
+    LBM_ON_DEVICE(p->device);
     lbm_ctx *c = nullptr;
     int rc = create(&c, p);
     if (rc) return rc;
@@ -269,6 +268,9 @@ extern "C" int lbm_init_bubbles(lbm_ctx **out, const lbm_params *p, const float 
 {
     const lbm::Range nvtx_range("lbm_init_bubbles");
     if (nbubbles < 0 || (nbubbles > 0 && !bubbles)) return fail(LBM_EINVAL, "bad bubble list");
+    if (!out) return fail(LBM_EINVAL, "out is NULL");
+    if (int rc0 = validate(p)) return rc0;   // before any CUDA call
+    LBM_ON_DEVICE(p->device);
     lbm_ctx *c = nullptr;
     int rc = create(&c, p);
     if (rc) return rc;
@@ -303,6 +305,7 @@ extern "C" int lbm_step(lbm_ctx *c, int nsteps, float grav)
     if (!c) return fail(LBM_EINVAL, "context is NULL");
     if (nsteps < 0) return fail(LBM_EINVAL, "nsteps < 0");
     if (!std::isfinite(grav)) return fail(LBM_EINVAL, "grav is not finite");
+    LBM_ON_DEVICE(c->p.device);
     const lbm::StepConst k = lbm::step_const(c->d, c->p, grav);
     for (int s = 0; s < nsteps; s++) {
         const int in = c->st.f_cur;
@@ -321,6 +324,7 @@ extern "C" int lbm_stats(lbm_ctx *c, lbm_stats_out *s, float *phi, float *rho, f
 {
     const lbm::Range nvtx_range("lbm_stats");
     if (!c) return fail(LBM_EINVAL, "context is NULL");
+    LBM_ON_DEVICE(c->p.device);
     const size_t n = (size_t)c->box.n, bytes = sizeof(float) * n;
     if (s) {
         cudaError_t e = lbm::launch_stats(c->box, c->d, c->st.mom, c->partials, c->partial_count, c->result,
@@ -346,7 +350,7 @@ extern "C" int lbm_stats_fields(lbm_ctx *c, lbm_stats_out *s, const float *phi, 
 {
     if (!c || !s) return fail(LBM_EINVAL, "lbm_stats_fields: NULL context or output");
     if (!phi || !rho || !ux || !uy || !uz) return fail(LBM_EINVAL, "lbm_stats_fields: every field is required");
-    LBM_CUDA(cudaSetDevice(c->p.device), "cudaSetDevice");
+    LBM_ON_DEVICE(c->p.device);
     const size_t n = (size_t)c->box.n, bytes = sizeof(float) * n;
     float *tmp = nullptr;
     LBM_CUDA(cudaMalloc(&tmp, 5 * bytes), "lbm_stats_fields scratch");
@@ -368,7 +372,7 @@ extern "C" int lbm_stats_fields(lbm_ctx *c, lbm_stats_out *s, const float *phi, 
 extern "C" int lbm_pressure(lbm_ctx *c, float *p)
 {
     if (!c || !p) return fail(LBM_EINVAL, "lbm_pressure: NULL argument");
-    LBM_CUDA(cudaSetDevice(c->p.device), "cudaSetDevice");
+    LBM_ON_DEVICE(c->p.device);
     const size_t n = (size_t)c->box.n;
     float *tmp = nullptr;
     LBM_CUDA(cudaMalloc(&tmp, sizeof(float) * n), "lbm_pressure scratch");
@@ -425,6 +429,7 @@ extern "C" int lbm_get_dist(lbm_ctx *c, float *f, float *g)
     const lbm::Range nvtx_range("lbm_get_dist");
     if (!c) return fail(LBM_EINVAL, "context is NULL");
     if (!f && !g) return LBM_OK;
+    LBM_ON_DEVICE(c->p.device);
     const size_t n = (size_t)c->box.n;
     float *tmp = nullptr;
     const size_t count = (f ? lbm::kQf : 0) + (g ? lbm::kQg : 0);
@@ -447,6 +452,7 @@ extern "C" int lbm_set_dist(lbm_ctx *c, const float *f, const float *g)
 {
     const lbm::Range nvtx_range("lbm_set_dist");
     if (!c || !f || !g) return fail(LBM_EINVAL, "NULL argument");
+    LBM_ON_DEVICE(c->p.device);
     const size_t n = (size_t)c->box.n;
     LBM_CUDA(cudaStreamSynchronize(c->stream), "lbm_set_dist");
     float *tmp = nullptr;
@@ -492,6 +498,7 @@ extern "C" int lbm_save_state(lbm_ctx *c, void *buf)
 {
     const lbm::Range nvtx_range("lbm_save_state");
     if (!c || !buf) return fail(LBM_EINVAL, "lbm_save_state: NULL argument");
+    LBM_ON_DEVICE(c->p.device);
     SnapshotHeader h;
     std::memset(&h, 0, sizeof(h));
     std::memcpy(h.magic, kSnapMagic, sizeof(h.magic));
@@ -529,6 +536,7 @@ extern "C" int lbm_load_state(lbm_ctx *c, const void *buf)
     if (h.nx != c->box.nx || h.ny != c->box.ny || h.nz != c->box.nz || h.storage != c->p.storage)
         return fail(LBM_EINVAL, "lbm_load_state: the snapshot's box or storage format differs from the context's");
     if (h.steps < 0) return fail(LBM_EINVAL, "lbm_load_state: bad step count");
+    LBM_ON_DEVICE(c->p.device);
     const unsigned char *d = static_cast<const unsigned char *>(buf) + sizeof(h);
     const size_t n = (size_t)c->box.n, b0 = sizeof(float) * n, bq = c->esz * (lbm::kQf - 1) * n,
                  bg = c->esz * lbm::kQg * n, bm = sizeof(float) * 5 * n;
@@ -555,6 +563,7 @@ extern "C" void *lbm_stream(const lbm_ctx *c) { return c ? (void *)c->stream : n
 extern "C" int lbm_sync(lbm_ctx *c)
 {
     if (!c) return fail(LBM_EINVAL, "context is NULL");
+    LBM_ON_DEVICE(c->p.device);
     LBM_CUDA(cudaStreamSynchronize(c->stream), "lbm_sync");
     return device_error(c);
 }
@@ -562,7 +571,7 @@ extern "C" int lbm_sync(lbm_ctx *c)
 extern "C" int lbm_wait_selftest(lbm_ctx *c)
 {
     if (!c) return fail(LBM_EINVAL, "context is NULL");
-    LBM_CUDA(cudaSetDevice(c->p.device), "cudaSetDevice");
+    LBM_ON_DEVICE(c->p.device);
     if (int rc = lbm_sync(c)) return rc;
     LBM_CUDA(lbm::launch_wait_selftest(c->err, c->stream), "wait self-test launch");
     LBM_CUDA(cudaStreamSynchronize(c->stream), "wait self-test");
@@ -576,7 +585,7 @@ extern "C" int lbm_wait_selftest(lbm_ctx *c)
 extern "C" void lbm_destroy(lbm_ctx *c)
 {
     if (!c) return;
-    cudaSetDevice(c->p.device);
+    const lbm::DeviceGuard device_guard(c->p.device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     cudaFree(c->st.f0);
     cudaFree(c->st.fq);

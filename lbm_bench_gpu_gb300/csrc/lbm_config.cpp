@@ -186,6 +186,20 @@ extern "C" int lbm_read_inputs(const char *dir, lbm_params *p, lbm_run *run, flo
     return LBM_OK;
 }
 
+namespace lbm {
+// The physical parameters every entry point needs before it derives the
+// constants (src/paramread.c:141-170 divides by tauRho, tauPhi, width and
+// rhoH - rhoL, and by rc0 when Eo is not zero); nullptr when they are usable.
+const char *physics_error(const lbm_params &p)
+{
+    if (!(p.tauRho > 0.f) || !(p.tauPhi > 0.f) || !(p.width > 0.f))
+        return "tauRho, tauPhi and width must be positive";
+    if (!(p.rhoH != p.rhoL)) return "rhoH must differ from rhoL";
+    if (p.Eo != 0.f && !(p.rc0 > 0.f)) return "rc0 must be positive when Eo is not zero";
+    return nullptr;
+}
+}  // namespace lbm
+
 extern "C" int lbm_derive(const lbm_params *p, lbm_derived *d)
 {
     if (!p || !d) {

@@ -107,6 +107,8 @@ const std::string &last_error();
 
 // Host-side derivation of the constants (src/paramread.c:141-170).
 void derive(const lbm_params &p, lbm_derived &d);
+// Why p's physical parameters cannot be derived from (nullptr: they can).
+const char *physics_error(const lbm_params &p);
 StepConst step_const(const lbm_derived &d, const lbm_params &p, float grav);
 
 // Kernel launchers (defined in the .cu files); all return the cudaError_t of the launch.
@@ -207,6 +209,36 @@ inline StepView state_view(lbm_ctx *c, int in)
 int fail(int code, const std::string &msg);
 int cuda_fail(cudaError_t e, const char *what);
 
+// Makes `device` current for the length of a C-ABI call and gives the caller
+// its own current device back afterwards.  Every entry point that queues or
+// waits for work of a context holds one, so a caller whose thread has another
+// GPU current (a second context, or torch's current device) still reaches the
+// context's stream and memory.  If the caller's device cannot be read (no
+// context on this thread yet), the context's device stays current.
+class DeviceGuard {
+public:
+    explicit DeviceGuard(int device)
+    {
+        have_prev_ = cudaGetDevice(&prev_) == cudaSuccess;
+        if (have_prev_ && prev_ == device) return;
+        err_ = cudaSetDevice(device);
+        changed_ = err_ == cudaSuccess && have_prev_;
+    }
+    ~DeviceGuard()
+    {
+        if (changed_) cudaSetDevice(prev_);
+    }
+    cudaError_t error() const { return err_; }
+    DeviceGuard(const DeviceGuard &) = delete;
+    DeviceGuard &operator=(const DeviceGuard &) = delete;
+
+private:
+    int prev_ = 0;
+    bool have_prev_ = false;
+    bool changed_ = false;
+    cudaError_t err_ = cudaSuccess;
+};
+
 // NVTX range over a C-ABI call (host side: the calls queue work on the
 // context's stream), for timelines of the library's work.
 struct Range {
@@ -216,3 +248,12 @@ struct Range {
     Range &operator=(const Range &) = delete;
 };
 }  // namespace lbm
+
+// Holds the context device for the rest of the enclosing C-ABI call; returns
+// the call's CUDA status if the device cannot be made current.
+#define LBM_ON_DEVICE(dev)                                                            \
+    const lbm::DeviceGuard lbm_device_guard_(dev);                                    \
+    do {                                                                              \
+        if (lbm_device_guard_.error() != cudaSuccess)                                 \
+            return lbm::cuda_fail(lbm_device_guard_.error(), "cudaSetDevice");       \
+    } while (0)

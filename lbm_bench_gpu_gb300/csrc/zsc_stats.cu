@@ -296,7 +296,9 @@ std::mutex g_noalloc_mutex;
 double *g_noalloc_ptr[kMaxDevices] = {};
 
 // Device address of the scratch array on `device` (which must be current).
-// Looked up on the first call per device; later calls reuse it.
+// Looked up on the first call per device; later calls reuse it.  A
+// cudaDeviceReset of that device ends the context that holds the array, so a
+// process that resets a device must not call lbm_stats_noalloc on it again.
 cudaError_t noalloc_scratch(int device, double **out)
 {
     std::lock_guard<std::mutex> lock(g_noalloc_mutex);
@@ -334,9 +336,15 @@ extern "C" int lbm_stats_noalloc(const lbm_params *p, const float *phi, const fl
         lbm::set_error("lbm_stats_noalloc: device ordinal out of range");
         return LBM_EINVAL;
     }
+    if (const char *why = lbm::physics_error(*p)) {
+        lbm::set_error(std::string("lbm_stats_noalloc: ") + why);
+        return LBM_EINVAL;
+    }
+    // the caller's current device is given back on return (when it can be read)
     int prev = 0;
-    cudaError_t e = cudaGetDevice(&prev);
-    if (e == cudaSuccess && prev != p->device) e = cudaSetDevice(p->device);
+    const bool have_prev = cudaGetDevice(&prev) == cudaSuccess;
+    const bool switch_device = !have_prev || prev != p->device;
+    cudaError_t e = switch_device ? cudaSetDevice(p->device) : cudaSuccess;
     double *scratch = nullptr;
     if (e == cudaSuccess) e = lbm::noalloc_scratch(p->device, &scratch);
     if (e == cudaSuccess) {
@@ -358,7 +366,7 @@ extern "C" int lbm_stats_noalloc(const lbm_params *p, const float *phi, const fl
             e = cudaGetLastError();
         }
     }
-    if (prev != p->device) cudaSetDevice(prev);
+    if (switch_device && have_prev) cudaSetDevice(prev);
     if (e != cudaSuccess) {
         lbm::set_error(std::string("lbm_stats_noalloc: ") + cudaGetErrorString(e));
         return LBM_ECUDA;

@@ -38,14 +38,12 @@
 // wrap) and the odd step's shifted g rows are cp.async 16-byte chunks: warps
 // 0-3 queue P_f, warps 4-7 queue g, each thread with chunk coordinates fixed
 // for the whole block; with nx a multiple of 32 no chunk straddles the seam.
-// The g rows go by TMA tensor copies (4-d tensor map x, y, z, field)
-// completing on an mbarrier: in the even step the tile itself in all 19
-// fields, one copy per plane (box 32 x 8 x 1 x 19); in the odd step, on tiles
-// whose shifted rows stay inside the box (no periodic wrap, which TMA's fill
-// cannot express), one copy per direction (box W x 8 x 1 x 1 at the shifted
-// origin, W = 32 + 2E as the cp.async rows); the other odd tiles keep
-// cp.async.  The mbarrier waits are bounded and report a timeout through an
-// error flag.
+// In the even step the g tile goes by one TMA tensor copy per plane (4-d
+// tensor map x, y, z, field; box 32 x 8 x 1 x 19) completing on an mbarrier;
+// the odd step stages its shifted g rows with cp.async only.  For 16-bit
+// storage the P_f planes of interior tiles also come by TMA (a 3-d f_0 box and
+// a 4-d f_1..f_6 box per plane).  The mbarrier waits are bounded and report a
+// timeout through an error flag.
 #include <cuda.h>   // CUtensorMap (the encoder is fetched from the driver at run time)
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>

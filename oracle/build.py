@@ -15,15 +15,23 @@
   built without ``-use_fast_math`` (``oracle/_ref/lbm_ref_cuda_exact``), to
   separate the fast-math share of its differences from this library.
 
-The reference sources are read from ``$LBM_REFERENCE_SRC`` (default: the
-reference checkout's ``src/`` directory at /root/reference/src).  Where that
-directory exists the recipe first stages an unmodified copy of the files it
-needs into ``oracle/_ref/src`` (ignored by git; a machine without the
-checkout, such as the GPU host, builds from that staged copy).  Nothing is
+The reference sources are read from ``$LBM_REFERENCE_SRC``, else from the
+checkout this recipe was written against (``CHECKOUT_SRC``; this file is the
+only one that names it).  Where that directory exists the recipe first stages
+an unmodified copy of the files it needs into ``oracle/_ref/src``, and the
+reference's sample ``Input/`` files into ``oracle/_ref/Input`` (ignored by git;
+a machine without the checkout, such as the GPU host, builds from the staged
+copy, and the tests read the staged copy only).  Nothing is
 patched: inputs with more bubbles than the reference's MAX_BUBBLES are fed in
 as a phi field instead (see ``zr_init``).
 
-Usage: ``python oracle/build.py [oracle|reference|reference_cuda|all]``.
+* ``build_reference_dump()`` builds the same program with
+  ``oracle/ref_harness/field_dump.c`` standing in for ``src/vtksave.c`` (same
+  signature; binary phi, rho, u at chosen steps) into
+  ``oracle/_ref/lbm_ref_cuda_dump`` and ``oracle/_ref/lbm_ref_cuda_exact_dump``,
+  for node-by-node parity with the reference's GPU fields.
+
+Usage: ``python oracle/build.py [oracle|reference|reference_cuda|reference_dump|all]``.
 """
 from __future__ import annotations
 
@@ -40,7 +48,8 @@ REF_STAGE = REF_DIR / "src"
 ORACLE_SO = BUILD_DIR / "libzsc_oracle.so"
 REF_SO = REF_DIR / "libzsc_ref.so"
 
-DEFAULT_REFERENCE_SRC = "/root/reference/src"
+CHECKOUT_SRC = "/root/reference/src"
+REF_INPUT_STAGE = REF_DIR / "Input"
 
 # Files of the reference that zsc_ref_cpu.cpp includes (src/main.cu:44-74 minus
 # the VTK writer).
@@ -55,6 +64,11 @@ REFERENCE_FILES = [
 REFERENCE_CUDA_FILES = ["main.cu", "vtksave.c"]
 REF_CUDA_BIN = REF_DIR / "lbm_ref_cuda"               # src/Makefile's flags
 REF_CUDA_EXACT_BIN = REF_DIR / "lbm_ref_cuda_exact"   # the same without -use_fast_math
+# The same program with ref_harness/field_dump.c in place of src/vtksave.c:
+# binary phi, rho, u at the steps LBM_DUMP_STEPS names, for per-node parity.
+REF_DUMP_STAGE = REF_DIR / "src_dump"
+REF_CUDA_DUMP_BIN = REF_DIR / "lbm_ref_cuda_dump"
+REF_CUDA_EXACT_DUMP_BIN = REF_DIR / "lbm_ref_cuda_exact_dump"
 
 # Deterministic IEEE float arithmetic on x86-64 and aarch64 alike: no
 # contraction into fused multiply-adds, no fast-math.
@@ -79,7 +93,7 @@ def build_oracle(force: bool = False) -> Path:
 
 def reference_src_dir() -> Path | None:
     """Directory holding the reference sources: the checkout, else the staged copy."""
-    env = os.environ.get("LBM_REFERENCE_SRC", DEFAULT_REFERENCE_SRC)
+    env = os.environ.get("LBM_REFERENCE_SRC", CHECKOUT_SRC)
     p = Path(env)
     if all((p / f).exists() for f in REFERENCE_FILES):
         return p
@@ -90,7 +104,7 @@ def reference_src_dir() -> Path | None:
 
 def stage_reference() -> Path | None:
     """Copy the needed reference files, unmodified, into oracle/_ref/src."""
-    p = Path(os.environ.get("LBM_REFERENCE_SRC", DEFAULT_REFERENCE_SRC))
+    p = Path(os.environ.get("LBM_REFERENCE_SRC", CHECKOUT_SRC))
     if not all((p / f).exists() for f in REFERENCE_FILES):
         return REF_STAGE if all((REF_STAGE / f).exists() for f in REFERENCE_FILES) else None
     REF_STAGE.mkdir(parents=True, exist_ok=True)
@@ -98,6 +112,12 @@ def stage_reference() -> Path | None:
         dst = REF_STAGE / f
         if not dst.exists() or dst.read_bytes() != (p / f).read_bytes():
             shutil.copyfile(p / f, dst)
+    sample = p.parent / "Input"
+    for f in ("properties.in", "discrete.in"):
+        if (sample / f).exists():
+            REF_INPUT_STAGE.mkdir(parents=True, exist_ok=True)
+            if not (REF_INPUT_STAGE / f).exists() or (REF_INPUT_STAGE / f).read_bytes() != (sample / f).read_bytes():
+                shutil.copyfile(sample / f, REF_INPUT_STAGE / f)
     return REF_STAGE
 
 
@@ -124,23 +144,60 @@ def build_reference_cuda(force: bool = False) -> Path | None:
     src_dir = reference_src_dir()
     if src_dir is None or not all((src_dir / f).exists() for f in REFERENCE_CUDA_FILES):
         return None
-    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
-    if not Path(nvcc).exists():
-        return None
-    stub = HERE / "ref_harness" / "mpi_stub" / "mpi.h"
-    deps = [stub] + [src_dir / f for f in REFERENCE_FILES + REFERENCE_CUDA_FILES]
+    deps = [src_dir / f for f in REFERENCE_FILES + REFERENCE_CUDA_FILES]
     REF_DIR.mkdir(exist_ok=True)
-    jobs = []
-    for out, flags in ((REF_CUDA_BIN, ["-O3", "-use_fast_math"]), (REF_CUDA_EXACT_BIN, ["-O3"])):
-        if force or not _newer(out, deps):
-            cmd = [nvcc, *flags, "-gencode", "arch=compute_103a,code=sm_103a", "-w",
-                   "-DcudaThreadSynchronize=cudaDeviceSynchronize", "-include", "stdlib.h",
-                   "-I", str(stub.parent), "-I", str(src_dir), str(src_dir / "main.cu"), "-o", str(out)]
-            jobs.append((cmd, subprocess.Popen(cmd)))
+    jobs = _nvcc_jobs(src_dir, ((REF_CUDA_BIN, ["-O3", "-use_fast_math"]), (REF_CUDA_EXACT_BIN, ["-O3"])), deps,
+                      force)
+    if jobs is None:
+        return None
     for cmd, job in jobs:
         if job.wait() != 0:
             raise subprocess.CalledProcessError(job.returncode, cmd)
     return REF_CUDA_BIN
+
+
+def _nvcc_jobs(src_dir: Path, outputs, deps, force: bool):
+    """Start one nvcc per (binary, flags) that is out of date; returns the jobs."""
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not Path(nvcc).exists():
+        return None
+    stub = HERE / "ref_harness" / "mpi_stub" / "mpi.h"
+    jobs = []
+    for out, flags in outputs:
+        if force or not _newer(out, deps + [stub]):
+            cmd = [nvcc, *flags, "-gencode", "arch=compute_103a,code=sm_103a", "-w",
+                   "-DcudaThreadSynchronize=cudaDeviceSynchronize", "-include", "stdlib.h",
+                   "-I", str(stub.parent), "-I", str(src_dir), str(src_dir / "main.cu"), "-o", str(out)]
+            jobs.append((cmd, subprocess.Popen(cmd)))
+    return jobs
+
+
+def build_reference_dump(force: bool = False) -> Path | None:
+    """The reference's CUDA program with ref_harness/field_dump.c as its VTK
+    writer: every other file is the reference's, unmodified, staged into
+    oracle/_ref/src_dump.  None if the sources or nvcc are absent."""
+    stage_reference()
+    src_dir = reference_src_dir()
+    if src_dir is None or not all((src_dir / f).exists() for f in REFERENCE_CUDA_FILES):
+        return None
+    writer = HERE / "ref_harness" / "field_dump.c"
+    REF_DUMP_STAGE.mkdir(parents=True, exist_ok=True)
+    for f in REFERENCE_FILES + ["main.cu"]:
+        dst = REF_DUMP_STAGE / f
+        if not dst.exists() or dst.read_bytes() != (src_dir / f).read_bytes():
+            shutil.copyfile(src_dir / f, dst)
+    dst = REF_DUMP_STAGE / "vtksave.c"
+    if not dst.exists() or dst.read_bytes() != writer.read_bytes():
+        shutil.copyfile(writer, dst)
+    deps = [REF_DUMP_STAGE / f for f in REFERENCE_FILES + REFERENCE_CUDA_FILES]
+    jobs = _nvcc_jobs(REF_DUMP_STAGE, ((REF_CUDA_DUMP_BIN, ["-O3", "-use_fast_math"]),
+                                       (REF_CUDA_EXACT_DUMP_BIN, ["-O3"])), deps, force)
+    if jobs is None:
+        return None
+    for cmd, job in jobs:
+        if job.wait() != 0:
+            raise subprocess.CalledProcessError(job.returncode, cmd)
+    return REF_CUDA_DUMP_BIN
 
 
 def main(argv: list[str]) -> int:
@@ -151,6 +208,8 @@ def main(argv: list[str]) -> int:
         print(build_reference(force=True) or "reference sources not found")
     if what in ("reference_cuda", "all"):
         print(build_reference_cuda(force=True) or "reference sources or nvcc not found")
+    if what in ("reference_dump", "all"):
+        print(build_reference_dump(force=True) or "reference sources or nvcc not found")
     return 0
 
 

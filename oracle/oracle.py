@@ -54,6 +54,7 @@ def oracle_lib() -> C.CDLL:
         lib.zo_moments.argtypes = [C.c_void_p, _D, _D, _D, _D, _D]
         lib.zo_dist.argtypes = [C.c_void_p, _D, _D]
         lib.zo_set_dist.argtypes = [C.c_void_p, _D, _D]
+        lib.zo_compare.argtypes = [C.c_void_p, _Fp, _Fp, _Fp, _D]
         lib.zo_stats.argtypes = [C.c_void_p, _D]
         lib.zo_steps.argtypes = [C.c_void_p]
         lib.zo_steps.restype = C.c_long
@@ -137,6 +138,23 @@ class Oracle:
         g = np.empty((19,) + self.shape, np.float64)
         self.lib.zo_dist(self.h, _dptr(f), _dptr(g))
         return f, g
+
+    FIELD_NAMES = ([f"f{i}" for i in range(7)] + [f"g{i}" for i in range(19)]
+                   + ["phi", "rho", "ux", "uy", "uz"])
+
+    def compare(self, f=None, g=None, mom=None) -> dict:
+        """Node-by-node comparison of float32 arrays with the oracle's state, in C
+        without copies: f (7, nz, ny, nx) and g (19, ...) streamed distributions,
+        mom (5, ...) phi, rho, ux, uy, uz.  Returns {field: (max |a - b|,
+        max |b|)} for the fields given."""
+        out = np.zeros(62, np.float64)
+        self.lib.zo_compare(self.h, _fptr(f), _fptr(g), _fptr(mom), _dptr(out))
+        res = {}
+        for q, name in enumerate(self.FIELD_NAMES):
+            given = (f is not None) if q < 7 else (g is not None) if q < 26 else (mom is not None)
+            if given:
+                res[name] = (float(out[2 * q]), float(out[2 * q + 1]))
+        return res
 
     def set_dist(self, f, g) -> None:
         self.lib.zo_set_dist(self.h, _dptr(np.ascontiguousarray(f, np.float64)),

@@ -3,7 +3,7 @@
  *
  * TEST INFRASTRUCTURE ONLY (builds oracle/_ref, the reference's own step
  * kernels run on the CPU).  Force-included before the reference sources by
- * oracle/build_ref.py.
+ * oracle/build.py.
  *
  * - CUDA qualifiers become no-ops; blockIdx / threadIdx / blockDim become
  *   thread-local variables set by the launch emulation in zsc_ref_cpu.cpp.

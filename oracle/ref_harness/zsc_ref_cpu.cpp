@@ -1,7 +1,7 @@
 /*
  * zsc_ref_cpu.cpp -- runs the reference's own step kernels on the host CPU.
  *
- * TEST INFRASTRUCTURE ONLY.  oracle/build_ref.py compiles this file together
+ * TEST INFRASTRUCTURE ONLY.  oracle/build.py compiles this file together
  * with the unmodified reference sources (included below by name, found through
  * -I on the reference's src/ directory) into oracle/_ref/libzsc_ref.so.  It is
  * used to pin the FP64 oracle (golden vectors) and as the CPU arm of bench.py

@@ -176,16 +176,31 @@ long zo_steps(const zo_ctx *s) { return s->steps; }
 void zo_bubble_phi(const zo_ctx *s, const float *bubbles, int nb, double *phi_g)
 {
     const int nx = s->nx, ny = s->ny, nzg = s->nz + 2;
+    const long ng = (long)nx * ny * nzg;
     const double phiStar = s->c.phiStar, width = s->c.width;
     const float widthf = (float)width;
 #pragma omp parallel for schedule(static)
-    for (int kk = 0; kk < nzg; kk++) {
-        for (int j = 0; j < ny; j++) {
-            for (int i = 0; i < nx; i++) {
-                double v = -phiStar;
-                for (int m = 0; m < nb; m++) {
-                    const float xc = bubbles[4 * m + 0], yc = bubbles[4 * m + 1];
-                    const float zc = bubbles[4 * m + 2], rc = bubbles[4 * m + 3];
+    for (long q = 0; q < ng; q++) phi_g[q] = -phiStar;
+    /* Bubbles in file order over the nodes of their bounding boxes (two nodes
+     * of margin around Rc + width, far more than the float rounding of R), so
+     * a later bubble overwrites an earlier one exactly where the reference's
+     * loop over all bubbles per node would. */
+    for (int m = 0; m < nb; m++) {
+        const float xc = bubbles[4 * m + 0], yc = bubbles[4 * m + 1];
+        const float zc = bubbles[4 * m + 2], rc = bubbles[4 * m + 3];
+        const double reach = (double)rc + width + 2.0;
+        int lo[3], hi[3];
+        const float cc[3] = {xc, yc, zc};
+        const int ext[3] = {nx, ny, nzg};
+        for (int a = 0; a < 3; a++) {
+            double l = floor((double)cc[a] - reach), h = ceil((double)cc[a] + reach);
+            lo[a] = l < 0 ? 0 : (l > ext[a] ? ext[a] : (int)l);
+            hi[a] = h > ext[a] - 1 ? ext[a] - 1 : (h < -1 ? -1 : (int)h);
+        }
+#pragma omp parallel for schedule(static)
+        for (int kk = lo[2]; kk <= hi[2]; kk++) {
+            for (int j = lo[1]; j <= hi[1]; j++) {
+                for (int i = lo[0]; i <= hi[0]; i++) {
                     volatile float dxf = (float)i - xc;
                     volatile float dyf = (float)j - yc;
                     volatile float dzf = (float)kk - zc;
@@ -196,10 +211,10 @@ void zo_bubble_phi(const zo_ctx *s, const float *bubbles, int nb, double *phi_g)
                     if (Rf <= rc + widthf) {
                         const double dx = (double)i - xc, dy = (double)j - yc, dz = (double)kk - zc;
                         const double R = sqrt(dx * dx + dy * dy + dz * dz);
-                        v = phiStar * tanh(2.0 * ((double)rc - R) / width);
+                        phi_g[(long)i + (long)nx * ((long)j + (long)ny * kk)] =
+                            phiStar * tanh(2.0 * ((double)rc - R) / width);
                     }
                 }
-                phi_g[(long)i + (long)nx * ((long)j + (long)ny * kk)] = v;
             }
         }
     }
@@ -444,6 +459,41 @@ void zo_dist(const zo_ctx *s, double *f, double *g)
 {
     for (int i = 0; i < 7; i++) if (f) memcpy(f + (long)i * s->n, s->f[i], sizeof(double) * s->n);
     for (int i = 0; i < 19; i++) if (g) memcpy(g + (long)i * s->n, s->g[i], sizeof(double) * s->n);
+}
+
+/*
+ * Node-by-node comparison of a float32 state with the oracle's, without
+ * copies: f (7 n), g (19 n) streamed distributions and mom (5 n: phi, rho,
+ * ux, uy, uz), each NULL to skip.  out[2 q] = max |a - b| and out[2 q + 1] =
+ * max |b| over field q, q = 0..6 f_0..f_6, 7..25 g_0..g_18, 26..30 the moments.
+ * Non-finite differences count as infinite.
+ */
+void zo_compare(const zo_ctx *s, const float *f, const float *g, const float *mom, double *out)
+{
+    const long n = s->n;
+    const double *ref[31];
+    const float *got[31];
+    for (int i = 0; i < 7; i++) { ref[i] = s->f[i]; got[i] = f ? f + (long)i * n : NULL; }
+    for (int i = 0; i < 19; i++) { ref[7 + i] = s->g[i]; got[7 + i] = g ? g + (long)i * n : NULL; }
+    const double *m[5] = {s->phi, s->rho, s->ux, s->uy, s->uz};
+    for (int i = 0; i < 5; i++) { ref[26 + i] = m[i]; got[26 + i] = mom ? mom + (long)i * n : NULL; }
+    for (int q = 0; q < 31; q++) {
+        double dmax = 0.0, rmax = 0.0;
+        if (got[q]) {
+            const double *b = ref[q];
+            const float *a = got[q];
+#pragma omp parallel for reduction(max : dmax, rmax) schedule(static)
+            for (long k = 0; k < n; k++) {
+                double d = fabs((double)a[k] - b[k]);
+                if (!(d == d) || d > 1e300) d = INFINITY;
+                if (d > dmax) dmax = d;
+                const double r = fabs(b[k]);
+                if (r > rmax) rmax = r;
+            }
+        }
+        out[2 * q] = dmax;
+        out[2 * q + 1] = rmax;
+    }
 }
 
 /* Overwrite the streamed distributions (resume from a snapshot). */

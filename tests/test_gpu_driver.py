@@ -283,3 +283,53 @@ def test_driver_adjoint_mode(lib, tmp_path):
     raw = (tmp_path / "adjoint_dphi0.vtk").read_bytes()
     data = np.frombuffer(raw[raw.index(b"LOOKUP_TABLE default\n") + 21:][: 4 * inp.nx * inp.ny * inp.nz], ">f4")
     np.testing.assert_array_equal(data.reshape(want["dJ_dphi0"].shape), want["dJ_dphi0"])
+
+
+def read_vtk_binary(path):
+    """Legacy binary VTK of lbm_zsc --vtk binary: the header lines, then
+    big-endian float32 blocks after each LOOKUP_TABLE / VECTORS line."""
+    raw = path.read_bytes()
+    header, data, pos = [], {}, 0
+    npts = None
+
+    def line():
+        nonlocal pos
+        end = raw.index(b"\n", pos)
+        s = raw[pos:end].decode()
+        pos = end + 1
+        return s
+
+    while pos < len(raw):
+        l = line()
+        header.append(l)
+        if l.startswith("POINT_DATA"):
+            npts = int(l.split()[1])
+        elif l.startswith("SCALARS") or l.startswith("VECTORS"):
+            name = l.split()[1]
+            count = npts
+            if l.startswith("SCALARS"):
+                line()   # LOOKUP_TABLE default (read_vtk does not keep it either)
+            else:
+                count = 3 * npts
+            data[name] = np.frombuffer(raw, ">f4", count, pos).astype(np.float64)
+            pos += 4 * count
+    return header, data
+
+
+def test_binary_vtk_matches_ascii(lib, tmp_path):
+    """--vtk binary writes the same snapshots as the ASCII files (the
+    reference's format): same names and header lines apart from the encoding
+    line, Phi, Pressure and Velocity (x, y, z interleaved per node) equal to
+    the ASCII values within their "%f" rounding (5e-7)."""
+    out = run_programs(tmp_path, ascii=[str(DRIVER), "."], binary=[str(DRIVER), ".", "--vtk", "binary"])
+    names = sorted(p.name for p in out["ascii"].glob("*.vtk"))
+    assert names and names == sorted(p.name for p in out["binary"].glob("*.vtk"))
+    for name in names:
+        ha, da = read_vtk(out["ascii"] / name)
+        hb, db = read_vtk_binary(out["binary"] / name)
+        strip = lambda h: [l for l in h if l.strip() and l not in ("ASCII", "BINARY")]
+        assert [l.lower() for l in strip(ha)] == [l.lower() for l in strip(hb)], name
+        assert set(da) == set(db) == {"Phi", "Pressure", "Velocity"}, name
+        for k in da:
+            assert da[k].shape == db[k].shape, (name, k)
+            assert np.abs(da[k] - db[k]).max() <= 5.01e-7, (name, k)

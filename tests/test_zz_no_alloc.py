@@ -16,10 +16,11 @@ import pytest
 from conftest import REL_TOL, U_TOL
 
 
-def _params(n=64):
+def _params(nx=64, ny=64, nz=64, **kw):
     from lbm_bench_gpu_gb300 import capi
-    return capi.make_params(n, n, n, rhoL=0.1, rhoH=1.0, tauRho=0.7, tauPhi=1.0, width=4.0, sigma=1e-3,
-                            Gamma=1.0, Eo=-0.4, rc0=10.0)
+    args = dict(rhoL=0.1, rhoH=1.0, tauRho=0.7, tauPhi=1.0, width=4.0, sigma=1e-3, Gamma=1.0, Eo=-0.4, rc0=10.0)
+    args.update(kw)
+    return capi.make_params(nx, ny, nz, **args)
 
 
 def test_noalloc_rejects_boxes_beyond_its_scratch(lib):
@@ -34,13 +35,33 @@ def test_noalloc_rejects_boxes_beyond_its_scratch(lib):
     assert "LBM_NOALLOC_MAX_NODES" in lib.lbm_last_error().decode()
 
 
+def test_noalloc_rejects_underivable_physics(lib):
+    """Parameters the constants cannot be derived from (zero interface width)
+    are rejected with LBM_EINVAL before any device work (runs without a GPU)."""
+    from lbm_bench_gpu_gb300 import capi
+    p = _params(width=0.0)
+    fake = C.c_void_p(16)
+    rc = lib.lbm_stats_noalloc(C.byref(p), fake, fake, fake, fake, fake, fake, None)
+    assert rc == capi.LBM_EINVAL
+    assert "width" in lib.lbm_last_error().decode()
+
+
+# a cubic box (16 partial rows) and a non-cubic one with many rows (192)
+BOXES = {
+    "64^3": ((64, 64, 64), [[31.6, 30.2, 33.4, 10.0], [12.0, 50.0, 20.0, 5.0]]),
+    "256x128x96": ((256, 128, 96), [[131.6, 60.2, 43.4, 12.0], [40.0, 100.0, 70.0, 7.0], [200.5, 20.0, 15.0, 6.0]]),
+}
+
+
 @pytest.mark.gpu
-def test_noalloc_stats_match_lbm_stats(lib):
+@pytest.mark.parametrize("box", sorted(BOXES))
+def test_noalloc_stats_match_lbm_stats(lib, box):
     import torch
     from lbm_bench_gpu_gb300 import capi
 
-    p = _params()
-    bubbles = np.array([[31.6, 30.2, 33.4, 10.0], [12.0, 50.0, 20.0, 5.0]], np.float32)
+    shape, bub = BOXES[box]
+    p = _params(*shape)
+    bubbles = np.array(bub, np.float32)
     with capi.Lattice.from_bubbles(p, bubbles) as lat:
         lat.step(12, capi.derive(p).grav)
         want, fields = lat.stats(fields=True)
