@@ -1,12 +1,12 @@
 """GPU path (liblbm_gb300.so through its C-ABI) against the FP64 oracle and the
 reference's own outputs.  Tolerances: see conftest (1e-5 relative for phi,
-rho and the distributions; 1e-5 c_s absolute for u) at <= 100 steps."""
+rho and the distribution sets; 1e-6 absolute for u) at <= 100 steps."""
 from __future__ import annotations
 
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, REL_TOL, U_TOL, assert_fields_close, rel_err
+from conftest import GOLDEN, REL_TOL, STORAGE_TOL, U_TOL, U_TOL_STORAGE, assert_fields_close, rel_err
 
 pytestmark = pytest.mark.gpu
 
@@ -118,7 +118,7 @@ def test_gpu_matches_reference_golden(lib, name, golden_manifest, tmp_path):
         lat.step(case["steps"], case["grav"])
         got = lat.fields()
     want = {k: ref[k] for k in ("phi", "rho", "ux", "uy", "uz")}
-    assert_fields_close(got, want, rel=2 * REL_TOL, utol=2 * U_TOL, what=f"golden {name}")
+    assert_fields_close(got, want, rel=2 * REL_TOL, utol=U_TOL, what=f"golden {name}")
 
 
 def random_state(shape, seed, p):
@@ -181,7 +181,8 @@ def test_stats_match_oracle(lib):
     assert s["p_dif"] == pytest.approx(so["p_dif"], rel=1e-3)
     assert s["ref"] == pytest.approx(so["ref"], rel=1e-3)
     for k in ("mom_x", "mom_y", "mom_z"):
-        assert abs(s[k] - so[k]) <= 1e-6 * so["rho_sum"] * U_TOL / 1e-5
+        # a momentum sum over n nodes: 1% of U_TOL per node on average
+        assert abs(s[k] - so[k]) <= 1e-2 * U_TOL * so["rho_sum"]
     assert s["nonfinite"] == 0
 
 
@@ -235,9 +236,8 @@ def test_full_size_conservation(lib):
 
 # 16-bit storage (f_1..f_6 and g in FP16 / BF16 with a shifted, power-of-two
 # scaled map; f_0 and all arithmetic FP32).  Tolerances against the FP64
-# oracle at 10 steps: FP16 5e-5 relative (phi, rho, distributions) and
-# 5e-5 c_s on u; BF16 (8-bit mantissa) 5e-4 and 5e-4 c_s.
-STORAGE_TOL = {"fp16": 5e-5, "bf16": 5e-4}
+# oracle at 10 steps (conftest): FP16 5e-5 relative (phi, rho, distributions)
+# and 1e-5 absolute on u; BF16 (8-bit mantissa) 5e-4 and 5e-5.
 
 
 @pytest.mark.parametrize("storage", ["fp16", "bf16"])
@@ -285,7 +285,8 @@ def test_storage_steps_match_oracle(lib, storage, steps, shape):
         o = oracle_for(make(nx, ny, nz, tauRho=0.8, tauPhi=0.9), b)
         lat.step(steps, -2e-5)
         o.step(steps, -2e-5)
-        assert_fields_close(lat.fields(), o.moments(), rel=tol, utol=tol * U_TOL / 1e-5, what=f"{storage} {steps}")
+        assert_fields_close(lat.fields(), o.moments(), rel=tol, utol=U_TOL_STORAGE[storage],
+                            what=f"{storage} {steps}")
         f, g = lat.dist()
         fo, go = o.dist()
         assert rel_err(f, fo) <= tol and rel_err(g, go) <= tol

