@@ -38,8 +38,12 @@ template <>
 struct Fmt<float> {
     static constexpr int kMinBlocks = 2;
     static constexpr bool kMapped = false;
+    using T2 = float2;   // (unused: FP32 keeps one node per thread)
     __device__ static float load(float v) { return v; }
     __device__ static float store(float v) { return v; }
+    __device__ static float2 load2(float2 v) { return v; }
+    __device__ static float2 store2(float2 v) { return v; }
+    __device__ static float2 swap2(float2 v) { return make_float2(v.y, v.x); }
 };
 template <>
 struct Fmt<__half> {
@@ -50,6 +54,7 @@ struct Fmt<__half> {
     __device__ static __half store(float v) { return __float2half_rn(v); }
     __device__ static float2 load2(__half2 v) { return __half22float2(v); }
     __device__ static __half2 store2(float2 v) { return __float22half2_rn(v); }
+    __device__ static __half2 swap2(__half2 v) { return __lowhigh2highlow(v); }
 };
 template <>
 struct Fmt<__nv_bfloat16> {
@@ -60,7 +65,24 @@ struct Fmt<__nv_bfloat16> {
     __device__ static __nv_bfloat16 store(float v) { return __float2bfloat16_rn(v); }
     __device__ static float2 load2(__nv_bfloat162 v) { return __bfloat1622float2(v); }
     __device__ static __nv_bfloat162 store2(float2 v) { return __float22bfloat162_rn(v); }
+    __device__ static __nv_bfloat162 swap2(__nv_bfloat162 v) { return __lowhigh2highlow(v); }
 };
+
+// Element index of node (x, row start t - x) in a field of the state: FP32
+// storage keeps the natural layout; the 16-bit formats keep the pair layout,
+// in which 32-bit word w of a row holds nodes x = w and x = w + nx/2 (so that
+// a step moving both nodes of a word by one node in x moves a whole word).
+// f_0 of a 16-bit state is in the pair layout too (float2 words).
+template <typename ST>
+__device__ __forceinline__ unsigned storage_index(const Box &b, unsigned t, int x)
+{
+    if constexpr (sizeof(ST) == 2) {
+        const int h = b.nx >> 1;
+        return t - (unsigned)x + (x < h ? 2u * (unsigned)x : 2u * (unsigned)(x - h) + 1u);
+    } else {
+        return t;
+    }
+}
 
 // Packed FP32 (f32x2): two lanes per instruction, each rounded as FP32.
 namespace pk {

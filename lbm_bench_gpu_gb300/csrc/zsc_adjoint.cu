@@ -83,6 +83,25 @@ __device__ __forceinline__ Nb neighbourhood(const Box &b, int x, int y, int z)
     return r;
 }
 
+// The same neighbourhood as element indices of the state's fields (FP32:
+// the node indices; 16-bit storage: the pair layout, see storage_index).
+template <typename ST>
+__device__ __forceinline__ Nb state_neighbourhood(const Box &b, int x, int y, int z)
+{
+    Nb r = neighbourhood(b, x, y, z);
+    if constexpr (sizeof(ST) == 2) {
+        const unsigned h = (unsigned)b.nx >> 1;
+#pragma unroll
+        for (int k = 0; k < 3; k++) r.X[k] = r.X[k] < h ? 2u * r.X[k] : 2u * (r.X[k] - h) + 1u;
+    }
+    return r;
+}
+
+__device__ __forceinline__ unsigned node_index_of(const Box &b, int x, int y, int z)
+{
+    return (unsigned)x + (unsigned)b.nx * ((unsigned)y + (unsigned)b.ny * (unsigned)z);
+}
+
 // index of the node at sign * c_i from the centre of p
 __device__ __forceinline__ unsigned dir_at(const Nb &p, int i, int sign)
 {
@@ -166,17 +185,17 @@ __global__ void __launch_bounds__(NTA) adjoint_phi_kernel(Box b, float eta, Quan
     const float eta2 = 1.f - eta;
     const int x = blockIdx.x * TXA + threadIdx.x, y = blockIdx.y * TYA + threadIdx.y;
     for (int z = blockIdx.z * kPlanes, z_end = min(b.nz, z + kPlanes); z < z_end; z++) {
-        const Nb p = neighbourhood(b, x, y, z);
-        const unsigned t = p.at(0, 0, 0);
-        float s = f0[t];
+        const Nb p = state_neighbourhood<ST>(b, x, y, z);
+        const unsigned ts = p.at(0, 0, 0);
+        float s = f0[ts];
 #pragma unroll
         for (int i = 1; i < kQf; i++) {
             const ST *a = static_cast<const ST *>(fq.f[i - 1]);
             const float inv = Fmt<ST>::kMapped ? q.f_inv : 1.f;
-            const float here = Fmt<ST>::load(a[t]) * inv;
+            const float here = Fmt<ST>::load(a[ts]) * inv;
             s += f_streamed ? here : eta * (Fmt<ST>::load(a[dir_at(p, i, -1)]) * inv) + eta2 * here;
         }
-        phi[t] = s;
+        phi[node_index_of(b, x, y, z)] = s;
     }
 }
 
@@ -193,13 +212,11 @@ __global__ void __launch_bounds__(NTA) objective_kernel(Box b, int objective, fl
     double A = 0.0, B = 0.0;
     const int x = blockIdx.x * TXA + threadIdx.x, y = blockIdx.y * TYA + threadIdx.y;
     for (int z = blockIdx.z * kPlanes, z_end = min(b.nz, z + kPlanes); z < z_end; z++) {
-        const Nb p = neighbourhood(b, x, y, z);
-        const unsigned t = p.at(0, 0, 0);
-        const float w = (phiStar - phi[t]) * half_inv;
+        const float w = (phiStar - phi[node_index_of(b, x, y, z)]) * half_inv;
         float qv;
         if (objective == 0) {
             float rho, m[3];
-            g_moments<ST, ODD>(g, q, p, rho, m);
+            g_moments<ST, ODD>(g, q, state_neighbourhood<ST>(b, x, y, z), rho, m);
             qv = m[2] / rho;
         } else {
             qv = (float)(z + 1);
@@ -287,10 +304,9 @@ __global__ void __launch_bounds__(NTA) source_init_kernel(Box b, int objective, 
     const SourceCoef k = source_coef(ab, phiStar);
     const int x = blockIdx.x * TXA + threadIdx.x, y = blockIdx.y * TYA + threadIdx.y;
     for (int z = blockIdx.z * kPlanes, z_end = min(b.nz, z + kPlanes); z < z_end; z++) {
-        const Nb p = neighbourhood(b, x, y, z);
-        const unsigned t = p.at(0, 0, 0);
+        const unsigned t = node_index_of(b, x, y, z);
         float rho, m[3];
-        g_moments<ST, ODD>(g, q, p, rho, m);
+        g_moments<ST, ODD>(g, q, state_neighbourhood<ST>(b, x, y, z), rho, m);
         float dphi, drho, dmz;
         objective_source(z, objective, k, phiStar, phi[t], rho, m[2], dphi, drho, dmz);
 #pragma unroll
@@ -343,8 +359,16 @@ __device__ __forceinline__ void prefetch_plane(const Box &b, const AdjIn &a, int
         } else if (field == kQg + kQf) {
             src = a.lst + node;
         } else if (field < 2 * kQg + kQf + 1) {
-            src = static_cast<const ST *>(a.g) + (field - kQg - kQf - 1) * n + node;
-            bytes = TXA * sizeof(ST);
+            // the tile row's nodes in the state's layout: FP32 the node range;
+            // pair layout the 32 words holding them (and the other half's)
+            unsigned first = node, count = TXA;
+            if constexpr (sizeof(ST) == 2) {
+                const unsigned h = (unsigned)b.nx >> 1, x0 = blockIdx.x * TXA;
+                first = node - x0 + 2u * (x0 < h ? x0 : x0 - h);
+                count = 2 * TXA;
+            }
+            src = static_cast<const ST *>(a.g) + (field - kQg - kQf - 1) * n + first;
+            bytes = count * sizeof(ST);
         } else {
             src = a.phi + node;
         }
@@ -368,10 +392,11 @@ __global__ void __launch_bounds__(NTA, ZSC_ADJ_MIN_BLOCKS) adjoint_local_kernel(
         stencil19(a.phi, p, lap, gr[0], gr[1], gr[2]);
         const float ph = __ldg(a.phi + t);
         float rh = 0.f, m[3] = {0.f, 0.f, 0.f};
+        const Nb ps = state_neighbourhood<ST>(b, x, y, z);
 #pragma unroll
         for (int i = 0; i < kQg; i++) {
-            const ST v = ODD ? static_cast<const ST *>(a.g_f[kOpp(i)])[dir_at(p, i, -1)]
-                             : static_cast<const ST *>(a.g_f[i])[t];
+            const ST v = ODD ? static_cast<const ST *>(a.g_f[kOpp(i)])[dir_at(ps, i, -1)]
+                             : static_cast<const ST *>(a.g_f[i])[ps.at(0, 0, 0)];
             float gi = Fmt<ST>::load(v);
             if constexpr (Fmt<ST>::kMapped) gi = gi * q.g_inv + q.g_shift[i];
             rh += gi;

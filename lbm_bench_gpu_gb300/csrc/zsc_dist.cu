@@ -6,7 +6,7 @@
 //                     (src/stream_f.cu:52-59); g in the AA layout is read from
 //                     the reversed slot of the upstream node when the next step
 //                     is odd; 16-bit storage is mapped back to FP32.
-//  quantize_kernel  : streamed FP32 -> state (natural layout, storage map).
+//  quantize_kernel  : streamed FP32 -> state (its layout, storage map).
 //  maxabs_kernel    : per-field max |value - shift|, to choose the 16-bit scales.
 //  moments_kernel   : phi, rho, u from streamed f and g
 //                     (src/update_phi.cu:42-43, src/update_rho.cu:46-50,
@@ -14,7 +14,7 @@
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
-#include "lbm_internal.h"
+#include "lattice.cuh"
 
 namespace lbm {
 namespace {
@@ -24,7 +24,7 @@ __constant__ int kCg[kQg][3] = {{0, 0, 0},  {1, 0, 0},   {-1, 0, 0}, {0, 1, 0}, 
                                 {0, 0, 1},  {0, 0, -1},  {1, 1, 0},  {-1, -1, 0}, {1, -1, 0},
                                 {-1, 1, 0}, {1, 0, 1},   {-1, 0, -1}, {1, 0, -1}, {-1, 0, 1},
                                 {0, 1, 1},  {0, -1, -1}, {0, 1, -1}, {0, -1, 1}};
-__constant__ int kOpp[kQg] = {0, 2, 1, 4, 3, 6, 5, 8, 7, 10, 9, 12, 11, 14, 13, 16, 15, 18, 17};
+__constant__ int kOppTab[kQg] = {0, 2, 1, 4, 3, 6, 5, 8, 7, 10, 9, 12, 11, 14, 13, 16, 15, 18, 17};
 
 __device__ __forceinline__ float to_f(float v) { return v; }
 __device__ __forceinline__ float to_f(__half v) { return __half2float(v); }
@@ -38,7 +38,8 @@ __device__ __forceinline__ __half from_f<__half>(float v) { return __float2half_
 template <>
 __device__ __forceinline__ __nv_bfloat16 from_f<__nv_bfloat16>(float v) { return __float2bfloat16_rn(v); }
 
-__device__ __forceinline__ long long shifted(const Box &b, int x, int y, int z, int dx, int dy, int dz)
+// node index of (x + dx, y + dy, z + dz), periodic; its x in *xo
+__device__ __forceinline__ long long shifted(const Box &b, int x, int y, int z, int dx, int dy, int dz, int *xo)
 {
     x += dx;
     y += dy;
@@ -46,6 +47,7 @@ __device__ __forceinline__ long long shifted(const Box &b, int x, int y, int z, 
     x = x < 0 ? x + b.nx : (x >= b.nx ? x - b.nx : x);
     y = y < 0 ? y + b.ny : (y >= b.ny ? y - b.ny : y);
     z = z < 0 ? z + b.nz : (z >= b.nz ? z - b.nz : z);
+    *xo = x;
     return x + (long long)b.nx * (y + (long long)b.ny * z);
 }
 
@@ -60,16 +62,19 @@ __global__ void stream_out_kernel(Box b, float eta, Quant q, const float *__rest
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < b.n;
          t += (long long)gridDim.x * blockDim.x) {
         const int x = (int)(t % b.nx), y = (int)((t / b.nx) % b.ny), z = (int)(t / b.nxy);
+        const unsigned st = storage_index<ST>(b, (unsigned)t, x);   // this node in the state's layout
+        int ux = 0;
         if (fo) {
-            fo[t] = f0[t];
+            fo[t] = f0[st];
             for (int i = 1; i < kQf; i++) {
                 const float inv = q.f_inv;
                 const ST *a = fq + (i - 1) * b.n;
                 if (f_streamed) {
-                    fo[i * b.n + t] = to_f(a[t]) * inv;
+                    fo[i * b.n + t] = to_f(a[st]) * inv;
                 } else {
-                    const long long up = shifted(b, x, y, z, -kCf[i][0], -kCf[i][1], -kCf[i][2]);
-                    fo[i * b.n + t] = eta * (to_f(a[up]) * inv) + eta2 * (to_f(a[t]) * inv);
+                    const long long up = shifted(b, x, y, z, -kCf[i][0], -kCf[i][1], -kCf[i][2], &ux);
+                    fo[i * b.n + t] = eta * (to_f(a[storage_index<ST>(b, (unsigned)up, ux)]) * inv)
+                                      + eta2 * (to_f(a[st]) * inv);
                 }
             }
         }
@@ -77,10 +82,10 @@ __global__ void stream_out_kernel(Box b, float eta, Quant q, const float *__rest
             for (int i = 0; i < kQg; i++) {
                 float v;
                 if (!odd) {
-                    v = to_f(g[i * b.n + t]);
+                    v = to_f(g[i * b.n + st]);
                 } else {
-                    const long long up = shifted(b, x, y, z, -kCg[i][0], -kCg[i][1], -kCg[i][2]);
-                    v = to_f(g[kOpp[i] * b.n + up]);
+                    const long long up = shifted(b, x, y, z, -kCg[i][0], -kCg[i][1], -kCg[i][2], &ux);
+                    v = to_f(g[kOppTab[i] * b.n + storage_index<ST>(b, (unsigned)up, ux)]);
                 }
                 go[i * b.n + t] = v * q.g_inv + q.g_shift[i];
             }
@@ -94,9 +99,10 @@ __global__ void quantize_kernel(Box b, Quant q, const float *__restrict__ f, con
 {
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < b.n;
          t += (long long)gridDim.x * blockDim.x) {
-        f0[t] = f[t];
-        for (int i = 1; i < kQf; i++) fq[(i - 1) * b.n + t] = from_f<ST>(f[i * b.n + t] * q.f_scale);
-        for (int i = 0; i < kQg; i++) gq[i * b.n + t] = from_f<ST>((g[i * b.n + t] - q.g_shift[i]) * q.g_scale);
+        const unsigned st = storage_index<ST>(b, (unsigned)t, (int)(t % b.nx));
+        f0[st] = f[t];
+        for (int i = 1; i < kQf; i++) fq[(i - 1) * b.n + st] = from_f<ST>(f[i * b.n + t] * q.f_scale);
+        for (int i = 0; i < kQg; i++) gq[i * b.n + st] = from_f<ST>((g[i * b.n + t] - q.g_shift[i]) * q.g_scale);
     }
 }
 

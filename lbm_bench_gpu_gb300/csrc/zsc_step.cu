@@ -69,6 +69,12 @@ constexpr int W0 = TX + 8;          // staged f_0 row (floats): x in [x0 - 4, x0
 constexpr int RW = TX + 2;          // phi ring width (tile + one-node ring)
 constexpr int RH = TY + 2;
 constexpr int RING = 2 * RW + 2 * TY;
+// 16-bit storage keeps its fields in the pair layout: 32-bit word w of a row
+// holds nodes x = w and x = w + nx/2.  A tile is TXW words (32 nodes) wide and
+// its phi ring holds float2 words (node w in .x, node w + nx/2 in .y).
+constexpr int TXW = TX / 2;
+constexpr int RWP = TXW + 2;
+constexpr int RINGP = 2 * RWP + 2 * TY;
 constexpr int NG = 2;               // g stages
 constexpr int NF = 4;               // P_f stages
 constexpr int NPHI = 4;             // phi planes
@@ -77,15 +83,12 @@ static_assert(TX == 32 && TY == 8, "issuer roles assume a 32 x 8 tile");
 
 constexpr float kInv6 = 0.16666666666666666667f;
 
-// 16-bit storage: two adjacent x nodes per thread (128 threads per 32 x 8
-// tile), all FP32 arithmetic in packed f32x2 pairs (node A in .x, node B in .y),
-// both nodes' 16-bit values converted and stored as one 32-bit word.
-#ifndef ZSC_PAIR
-#define ZSC_PAIR 1
-#endif
-constexpr bool kUsePair = ZSC_PAIR != 0;
+// 16-bit storage: two nodes per thread (128 threads per 32-node x 8 tile), the
+// two nodes of one 32-bit word of the pair layout (A = x in .x, B = x + nx/2 in
+// .y of every packed f32x2 value), both nodes' 16-bit values converted and
+// stored as one 32-bit word.
 template <typename ST>
-constexpr bool use_pair() { return kUsePair && sizeof(ST) == 2; }
+constexpr bool use_pair() { return sizeof(ST) == 2; }
 template <typename ST>
 constexpr int threads_of() { return use_pair<ST>() ? NT / 2 : NT; }
 
@@ -134,7 +137,7 @@ struct Geo {
     static constexpr int G_STAGE = kQg * TY * W * (int)sizeof(ST);            // bytes
     static constexpr int F0_BYTES = FR * W0 * 4;
     static constexpr int F_STAGE = F0_BYTES + (kQf - 1) * FR * W * (int)sizeof(ST);
-    static constexpr int PHI_STAGE = RH * RW * 4;
+    static constexpr int PHI_STAGE = sizeof(ST) == 2 ? RH * RWP * 8 : RH * RW * 4;
     static constexpr int G_OFF = 0;
     static constexpr int F_OFF = NG * G_STAGE;
     static constexpr int PHI_OFF = F_OFF + NF * F_STAGE;
@@ -393,23 +396,29 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
         __syncthreads();
     }
 
-    // Halo ring node handled by this thread (if any): top row, bottom row,
-    // left column, right column of the (TX+2) x (TY+2) phi tile.
-    const bool has_ring = tid < RING;
+    // Halo ring node (16-bit: ring word) handled by this thread (if any): top
+    // row, bottom row, left column, right column of the (RWX) x (TY+2) phi tile.
+    constexpr int RWX = PAIR ? RWP : RW;
+    const bool has_ring = tid < (PAIR ? RINGP : RING);
     int rlx = 0, rly = 0;
-    if (tid < RW) {
+    if (tid < RWX) {
         rlx = tid;
         rly = 0;
-    } else if (tid < 2 * RW) {
-        rlx = tid - RW;
+    } else if (tid < 2 * RWX) {
+        rlx = tid - RWX;
         rly = TY + 1;
-    } else if (tid < 2 * RW + TY) {
+    } else if (tid < 2 * RWX + TY) {
         rlx = 0;
-        rly = tid - 2 * RW + 1;
+        rly = tid - 2 * RWX + 1;
     } else if (has_ring) {
-        rlx = TX + 1;
-        rly = tid - 2 * RW - TY + 1;
+        rlx = RWX - 1;
+        rly = tid - 2 * RWX - TY + 1;
     }
+    // Pair layout: staged words that came round the periodic x seam hold their
+    // two nodes swapped (word w - nx/2 of the row is word w's neighbour pair in
+    // the other order).  Tiles at the left seam (x0 = 0) see that in the staged
+    // columns left of the tile, tiles at the right seam right of it.
+    const bool seam_l = x0 == 0, seam_r = x0 + TX == b.nx;
 
     // P_f stage of plane p (p >= z0 - 2): f_0 part and f_1..f_6 part
     auto fstage = [&](int p) { return F + ((p - z0 + 4) & (NF - 1)) * Gm::F_STAGE; };
@@ -583,13 +592,59 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
         }
     };
 
+    // Pair layout (16-bit storage): the same for the two nodes of a word at
+    // once.  Ring word column lx (0 = row word x0/2 - 1) is staged f_0 word
+    // column lx + 1 (f_0 rows start at word x0/2 - 2) and f_1..f_6 word column
+    // lx + 3 (rows start at word x0/2 - 4); a word that came round the x seam
+    // is swapped back on read.
+    using T2 = typename Fm::T2;
+    auto fq_word = [&](unsigned char *S, int a, int rr, int cw) -> float2 {
+        T2 v = reinterpret_cast<const T2 *>(fqpart(S))[(a * FR + rr) * (W / 2) + cw];
+        if ((seam_l && cw < 4) || (seam_r && cw >= TXW + 4)) v = Fm::swap2(v);
+        return Fm::load2(v);
+    };
+    auto phi_pair = [&](int p, int lx, int ly, float2(&f)[kQf]) -> float2 {
+        using namespace pk;
+        const int row = ly + 1, c0 = lx + 1, cq = lx + 3;
+        unsigned char *S1 = fstage(p);
+        float2 v0 = reinterpret_cast<const float2 *>(f0part(S1))[row * (W0 / 2) + c0];
+        if ((seam_l && c0 < 2) || (seam_r && c0 >= TXW + 2)) v0 = make_float2(v0.y, v0.x);
+        f[0] = v0;
+        if (STREAMED) {
+#pragma unroll
+            for (int a = 0; a < kQf - 1; a++) f[a + 1] = fq_word(S1, a, row, cq);
+        } else {
+            unsigned char *S0 = fstage(p - 1), *S2 = fstage(p + 1);
+            // eta P(x - c) + (1 - eta) P(x), in stored units
+            auto blend = [&](unsigned char *Su, int a, int ru, int cu) {
+                return fma(splat(c.eta), fq_word(Su, a, ru, cu), mul(splat(c.eta2), fq_word(S1, a, row, cq)));
+            };
+            f[1] = blend(S1, 0, row, cq - 1);
+            f[2] = blend(S1, 1, row, cq + 1);
+            f[3] = blend(S1, 2, row - 1, cq);
+            f[4] = blend(S1, 3, row + 1, cq);
+            f[5] = blend(S0, 4, row, cq);
+            f[6] = blend(S2, 5, row, cq);
+        }
+        return fma(splat(m.f_inv), add(add(add(add(add(f[1], f[2]), f[3]), f[4]), f[5]), f[6]), f[0]);
+    };
+    auto build_pair = [&](int p, int s, float2(&fo)[kQf]) {
+        float2 *ph = reinterpret_cast<float2 *>(PHI) + s * (RH * RWP);
+        ph[(ty + 1) * RWP + tx + 1] = phi_pair(p, tx + 1, ty + 1, fo);
+        if (has_ring) {
+            float2 tmp[kQf];
+            ph[rly * RWP + rlx] = phi_pair(p, rlx, rly, tmp);
+        }
+    };
+
     // Neighbour offsets in x and y are fixed for the thread; z per plane.
     const int o_xm = (x == 0) ? b.nx - 1 : -1;
     const int o_xp = (x == b.nx - 1) ? -(b.nx - 1) : 1;
     const int o_ym = (y == 0) ? (b.ny - 1) * b.nx : -b.nx;
     const int o_yp = (y == b.ny - 1) ? -(b.ny - 1) * b.nx : b.nx;
 
-    float fcur[XPT][kQf], fnext[XPT][kQf];
+    float fcur[XPT][kQf], fnext[XPT][kQf];   // one node per thread (FP32)
+    float2 fcur2[kQf], fnext2[kQf];           // pair layout (16-bit storage)
 
     pdl_launch_dependents();
     pdl_wait();   // the previous step's writes are complete and visible
@@ -607,11 +662,15 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
         for (int p = z0 - 2; p <= z0 + 1; p++) late |= !mbar_wait(fbar(p), fphase(p));
     }
     __syncthreads();
-    {
+    if constexpr (PAIR) {
+        float2 tmp[kQf];
+        build_pair(z0 - 1, 0, tmp);
+        build_pair(z0, 1, fcur2);
+    } else {
         float tmp[XPT][kQf];
         build_plane(z0 - 1, 0, tmp);
+        build_plane(z0, 1, fcur);
     }
-    build_plane(z0, 1, fcur);
     __syncthreads();
     issue_f(z0 + 2);
     cp_async_commit();
@@ -628,7 +687,8 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
         // P_f plane z + 2 is first read here (a late copy only spoils values:
         // the uniform exit below comes before anything is stored)
         if (tile_tma_f) late |= !mbar_wait(fbar(z + 2), fphase(z + 2));
-        build_plane(z + 1, (j + 2) & 3, fnext);
+        if constexpr (PAIR) build_pair(z + 1, (j + 2) & 3, fnext2);
+        else build_plane(z + 1, (j + 2) & 3, fnext);
         if constexpr (TMA) {
             // g of plane z: stage j & 1, its (j >> 1)-th use (cp.async tiles
             // were complete at the barrier above)
@@ -850,31 +910,28 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
         }
 
         } else {
-            // Two nodes per thread: A = (x, y, z) in the .x lanes, B = (x + 1, y, z)
-            // in the .y lanes of packed FP32; 16-bit storage only, so g and f_1..f_6
-            // are in stored units (StepMap) and each store writes both nodes.
+            // Two nodes per thread, the two of one pair-layout word w = x0/2 + tx:
+            // A = (w, y, z) in the .x lanes, B = (w + nx/2, y, z) in the .y lanes of
+            // packed FP32; 16-bit storage only, so g and f_1..f_6 are in stored
+            // units (StepMap) and each store writes both nodes.  Their x
+            // neighbours are the neighbouring words' nodes, so every stencil point
+            // is one float2 of the phi ring.
             using namespace pk;
-            using T2 = typename Fm::T2;
-            const int lx = 2 * tx + 1, ly = ty + 1;   // ring-tile column of A
-            // phi at columns lx - 1 .. lx + 2 of row yy of a plane: two aligned float2
-            auto row4 = [&](const float *S, int yy, float2 &lo, float2 &hi) {
-                const float2 *r = reinterpret_cast<const float2 *>(S + yy * RW + lx - 1);
-                lo = r[0];
-                hi = r[1];
-            };
-            auto col = [&](const float *S, int yy) { return make_float2(S[yy * RW + lx], S[yy * RW + lx + 1]); };
-            float2 cl, ch, nl, nh, sl, sh, tl, th, bl, bh;
-            row4(S1, ly, cl, ch);
-            row4(S1, ly + 1, nl, nh);
-            row4(S1, ly - 1, sl, sh);
-            row4(S2, ly, tl, th);
-            row4(S0, ly, bl, bh);
-            // the same points as the one-node stencil (lo = x - 1, hi = x + 1)
-            const float2 pc = make_float2(cl.y, ch.x), pe = ch, pw = cl;
-            const float2 pn = make_float2(nl.y, nh.x), ps = make_float2(sl.y, sh.x);
-            const float2 pt = make_float2(tl.y, th.x), pb = make_float2(bl.y, bh.x);
-            const float2 pen = nh, pwn = nl, pes = sh, pws = sl, pet = th, pwt = tl, peb = bh, pwb = bl;
-            const float2 pnt = col(S2, ly + 1), psb = col(S0, ly - 1), pnb = col(S0, ly + 1), pst = col(S2, ly - 1);
+            const float2 *Q0 = reinterpret_cast<const float2 *>(PHI) + (j & 3) * (RH * RWP);        // plane z - 1
+            const float2 *Q1 = reinterpret_cast<const float2 *>(PHI) + ((j + 1) & 3) * (RH * RWP);  // plane z
+            const float2 *Q2 = reinterpret_cast<const float2 *>(PHI) + ((j + 2) & 3) * (RH * RWP);  // plane z + 1
+            const int lx = tx + 1, ly = ty + 1;
+            auto at = [&](const float2 *S, int yy, int xx) { return S[yy * RWP + xx]; };
+            const float2 pc = at(Q1, ly, lx);
+            const float2 pe = at(Q1, ly, lx + 1), pw = at(Q1, ly, lx - 1);
+            const float2 pn = at(Q1, ly + 1, lx), ps = at(Q1, ly - 1, lx);
+            const float2 pt = at(Q2, ly, lx), pb = at(Q0, ly, lx);
+            const float2 pen = at(Q1, ly + 1, lx + 1), pws = at(Q1, ly - 1, lx - 1);
+            const float2 pes = at(Q1, ly - 1, lx + 1), pwn = at(Q1, ly + 1, lx - 1);
+            const float2 pet = at(Q2, ly, lx + 1), pwb = at(Q0, ly, lx - 1);
+            const float2 peb = at(Q0, ly, lx + 1), pwt = at(Q2, ly, lx - 1);
+            const float2 pnt = at(Q2, ly + 1, lx), psb = at(Q0, ly - 1, lx);
+            const float2 pnb = at(Q0, ly + 1, lx), pst = at(Q2, ly - 1, lx);
 
             float2 se = add(add(add(pen, pws), add(pes, pwn)), add(add(pet, pwb), add(peb, pwt)));
             se = add(se, add(add(pnt, psb), add(pnb, pst)));
@@ -891,8 +948,12 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
             if (pc.x > 0.f) Fz.x += c.grav;
             if (pc.y > 0.f) Fz.y += c.grav;
 
-            // D3Q19 values of both nodes from the staged rows (AA pattern)
+            // D3Q19 values of both nodes from the staged rows (AA pattern); an
+            // odd step's x-shifted direction reads the neighbouring word, which
+            // came round the x seam (swapped) for the first / last word of a
+            // seam tile
             const ST *Gs = G + (j & 1) * G_ELEMS;
+            const bool wrap_l = seam_l && tx == 0, wrap_r = seam_r && tx == TXW - 1;
             float2 g[kQg];
 #pragma unroll
             for (int i = 0; i < kQg; i++) {
@@ -901,8 +962,9 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
                 } else if (!ODD || kCx(i) == 0) {
                     g[i] = Fm::load2(*reinterpret_cast<const T2 *>(Gs + (i * TY + ty) * W + E + 2 * tx));
                 } else {
-                    const ST *r = Gs + (i * TY + ty) * W + E + 2 * tx - kCx(i);
-                    g[i] = make_float2(Fm::load(r[0]), Fm::load(r[1]));
+                    T2 v = *reinterpret_cast<const T2 *>(Gs + (i * TY + ty) * W + E + 2 * tx - 2 * kCx(i));
+                    if (kCx(i) > 0 ? wrap_l : wrap_r) v = Fm::swap2(v);
+                    g[i] = Fm::load2(v);
                 }
             }
 
@@ -918,13 +980,18 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
             const float2 ux = mul(add(add(add(add(sub(g[1], g[2]), d7), d9), d11), d13), invRhoG);
             const float2 uy = mul(add(add(sub(add(sub(g[3], g[4]), d7), d9), d15), d17), invRhoG);
             const float2 uz = mul(sub(add(sub(add(sub(g[5], g[6]), d11), d13), d15), d17), invRhoG);
-            const unsigned id = node_index(b, x, y, z);   // node A (even: 8-byte aligned pairs)
-            if (write_moments && in_field(id, 2, b.n, P.err)) {
-                *reinterpret_cast<float2 *>(P.mom[0] + id) = pc;
-                *reinterpret_cast<float2 *>(P.mom[1] + id) = rho;
-                *reinterpret_cast<float2 *>(P.mom[2] + id) = ux;
-                *reinterpret_cast<float2 *>(P.mom[3] + id) = uy;
-                *reinterpret_cast<float2 *>(P.mom[4] + id) = uz;
+            // element index of the word (its A half) in every pair-layout field
+            const unsigned id = node_index(b, x, y, z);
+            const int half = b.nx / 2;
+            if (write_moments) {
+                // the moment fields are in the natural layout: A and B apart
+                const unsigned ia = node_index(b, x0 / 2 + tx, y, z), ib = ia + (unsigned)half;
+                const float2 mv[5] = {pc, rho, ux, uy, uz};
+#pragma unroll
+                for (int k = 0; k < 5; k++) {
+                    if (in_field(ia, 1, b.n, P.err)) P.mom[k][ia] = mv[k].x;
+                    if (in_field(ib, 1, b.n, P.err)) P.mom[k][ib] = mv[k].y;
+                }
             }
             const float2 hinv = mul(splat(0.5f), invRho);
             const float2 usx = fma(Fx, hinv, ux), usy = fma(Fy, hinv, uy), usz = fma(Fz, hinv, uz);
@@ -932,7 +999,7 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
             // D3Q7 collision (A/B store), f_1..f_6 in stored units
             {
                 const float2 a2 = splat(c.invTauPhiOne);
-                auto fc = [&](int k) { return make_float2(fcur[0][k], fcur[1][k]); };
+                auto fc = [&](int k) { return fcur2[k]; };
                 const float2 Af = mul(splat(0.5f * c.Gamma * c.invTauPhi), mu);
                 if (in_field(id, 2, b.n, P.err))
                     *reinterpret_cast<float2 *>(P.f0out + id) =
@@ -995,37 +1062,36 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
                     for (int i = 0; i < kQg; i++)
                         if (in_field(id, 2, b.n, P.err)) *reinterpret_cast<T2 *>(P.g[kOpp(i)] + id) = Fm::store2(qv[i]);
                 } else {
-                    // odd: downstream neighbours x + c_i, natural slot i; a pair
-                    // moved along x is not 32-bit aligned, so those directions
-                    // store the two 16-bit values apart (A = x is even: only its
-                    // -x neighbour wraps; only B's +x neighbour wraps)
+                    // odd: downstream neighbours x + c_i, natural slot i.  Both
+                    // nodes of the word move to the neighbouring word together;
+                    // past the x seam (word nx/2 - 1 -> 0 and back) the pair
+                    // lands swapped.
                     const int o_zm = (z == 0) ? (b.nz - 1) * (int)b.nxy : -(int)b.nxy;
                     const int o_zp = (z == b.nz - 1) ? -(b.nz - 1) * (int)b.nxy : (int)b.nxy;
-                    const int oA_xm = (x == 0) ? b.nx - 1 : -1;
-                    const int oB_xp = (x + 1 == b.nx - 1) ? -(b.nx - 1) : 1;
+                    const int o_wp = wrap_r ? -2 * (half - 1) : 2;   // element offset of word w + 1
+                    const int o_wm = wrap_l ? 2 * (half - 1) : -2;   // ... of word w - 1
 #pragma unroll
                     for (int i = 0; i < kQg; i++) {
-                        const int oyz = (kCy(i) > 0 ? o_yp : kCy(i) < 0 ? o_ym : 0) +
-                                        (kCz(i) > 0 ? o_zp : kCz(i) < 0 ? o_zm : 0);
-                        const T2 h = Fm::store2(qv[i]);
-                        if (kCx(i) == 0) {
-                            if (in_field((long long)id + oyz, 2, b.n, P.err))
-                                *reinterpret_cast<T2 *>(P.g[i] + id + oyz) = h;
-                        } else {
-                            const unsigned ia = id + oyz + (kCx(i) > 0 ? 1 : oA_xm);
-                            const unsigned ib = id + 1 + oyz + (kCx(i) > 0 ? oB_xp : -1);
-                            if (in_field(ia, 1, b.n, P.err)) P.g[i][ia] = h.x;
-                            if (in_field(ib, 1, b.n, P.err)) P.g[i][ib] = h.y;
-                        }
+                        const int o = (kCx(i) > 0 ? o_wp : kCx(i) < 0 ? o_wm : 0) +
+                                      (kCy(i) > 0 ? o_yp : kCy(i) < 0 ? o_ym : 0) +
+                                      (kCz(i) > 0 ? o_zp : kCz(i) < 0 ? o_zm : 0);
+                        T2 h = Fm::store2(qv[i]);
+                        if (kCx(i) != 0 && (kCx(i) > 0 ? wrap_r : wrap_l)) h = Fm::swap2(h);
+                        if (in_field((long long)id + o, 2, b.n, P.err)) *reinterpret_cast<T2 *>(P.g[i] + id + o) = h;
                     }
                 }
             }
         }
 
+        if constexpr (PAIR) {
 #pragma unroll
-        for (int k = 0; k < XPT; k++)
+            for (int i = 0; i < kQf; i++) fcur2[i] = fnext2[i];
+        } else {
 #pragma unroll
-            for (int i = 0; i < kQf; i++) fcur[k][i] = fnext[k][i];
+            for (int k = 0; k < XPT; k++)
+#pragma unroll
+                for (int i = 0; i < kQf; i++) fcur[k][i] = fnext[k][i];
+        }
     }
 }
 
