@@ -44,6 +44,7 @@ struct Fmt<float> {
     __device__ static float2 load2(float2 v) { return v; }
     __device__ static float2 store2(float2 v) { return v; }
     __device__ static float2 swap2(float2 v) { return make_float2(v.y, v.x); }
+    __device__ static float2 perm2(float2 v, unsigned) { return v; }
 };
 template <>
 struct Fmt<__half> {
@@ -55,6 +56,12 @@ struct Fmt<__half> {
     __device__ static float2 load2(__half2 v) { return __half22float2(v); }
     __device__ static __half2 store2(float2 v) { return __float22half2_rn(v); }
     __device__ static __half2 swap2(__half2 v) { return __lowhigh2highlow(v); }
+    // the word's two halves in the order selector sel gives (kKeep / kSwap)
+    __device__ static __half2 perm2(__half2 v, unsigned sel)
+    {
+        const unsigned w = __byte_perm(*reinterpret_cast<const unsigned *>(&v), 0u, sel);
+        return *reinterpret_cast<const __half2 *>(&w);
+    }
 };
 template <>
 struct Fmt<__nv_bfloat16> {
@@ -66,6 +73,11 @@ struct Fmt<__nv_bfloat16> {
     __device__ static float2 load2(__nv_bfloat162 v) { return __bfloat1622float2(v); }
     __device__ static __nv_bfloat162 store2(float2 v) { return __float22bfloat162_rn(v); }
     __device__ static __nv_bfloat162 swap2(__nv_bfloat162 v) { return __lowhigh2highlow(v); }
+    __device__ static __nv_bfloat162 perm2(__nv_bfloat162 v, unsigned sel)
+    {
+        const unsigned w = __byte_perm(*reinterpret_cast<const unsigned *>(&v), 0u, sel);
+        return *reinterpret_cast<const __nv_bfloat162 *>(&w);
+    }
 };
 
 // Element index of node (x, row start t - x) in a field of the state: FP32
@@ -83,6 +95,9 @@ __device__ __forceinline__ unsigned storage_index(const Box &b, unsigned t, int 
         return t;
     }
 }
+
+// __byte_perm selectors: a 32-bit word as it is, or with its 16-bit halves swapped.
+constexpr unsigned kKeep = 0x3210u, kSwap = 0x1032u;
 
 // Packed FP32 (f32x2): two lanes per instruction, each rounded as FP32.
 namespace pk {

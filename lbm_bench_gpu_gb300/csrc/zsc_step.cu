@@ -105,9 +105,10 @@ constexpr int threads_of() { return use_pair<ST>() ? NT / 2 : NT; }
 #endif
 // Odd steps stage their shifted g rows with cp.async: one TMA tensor copy per
 // direction (19 per plane, interior tiles) measured slower (256^3: FP16 one
-// node per thread 33.7k vs 36.2k, two nodes per thread 39.5k vs 41.9k; FP32
-// 26.7k vs 27.2k MLUPS), and one 1-d bulk copy (cp.async.bulk) per shifted row,
-// 152 per plane, slower still (FP16 36.8k vs 42.3k, FP32 26.5k vs 27.6k).
+// node per thread 33.7k vs 36.2k, two nodes per thread 39.5k vs 41.9k, pair
+// layout 41.9k vs 45.5k; FP32 26.7k vs 27.2k MLUPS), and one 1-d bulk copy
+// (cp.async.bulk) per shifted row, 152 per plane, slower still (FP16 36.8k vs
+// 42.3k, FP32 26.5k vs 27.6k).
 // the P_f planes by TMA on interior tiles (f_0 box W0 x FR, f_1..f_6 box
 // W x FR x 6), for the 16-bit formats: measured at 256^3 (same GPU, 500
 // steps), FP16 36 250 -> 37 060 MLUPS, while FP32 drops 27 110 -> 26 560 with
@@ -598,42 +599,59 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
     // lx + 3 (rows start at word x0/2 - 4); a word that came round the x seam
     // is swapped back on read.
     using T2 = typename Fm::T2;
-    auto fq_word = [&](unsigned char *S, int a, int rr, int cw) -> float2 {
-        T2 v = reinterpret_cast<const T2 *>(fqpart(S))[(a * FR + rr) * (W / 2) + cw];
-        if ((seam_l && cw < 4) || (seam_r && cw >= TXW + 4)) v = Fm::swap2(v);
-        return Fm::load2(v);
+    // byte_perm selectors of the staged columns a word position reads, fixed
+    // per thread: fq columns cq - 1, cq, cq + 1 and the f_0 column.  The own
+    // word (cq = tx + 4) only reads across the seam at the tile's edge words.
+    struct Sel {
+        unsigned m, c, p;
+        bool f0;
     };
-    auto phi_pair = [&](int p, int lx, int ly, float2(&f)[kQf]) -> float2 {
+    auto sel_of = [&](int lx) {
+        const int cq = lx + 3, c0 = lx + 1;
+        auto q = [&](int cw) { return (seam_l && cw < 4) || (seam_r && cw >= TXW + 4) ? kSwap : kKeep; };
+        Sel r;
+        r.m = q(cq - 1);
+        r.c = q(cq);
+        r.p = q(cq + 1);
+        r.f0 = (seam_l && c0 < 2) || (seam_r && c0 >= TXW + 2);
+        return r;
+    };
+    const Sel sel_own = {seam_l && tx == 0 ? kSwap : kKeep, kKeep, seam_r && tx == TXW - 1 ? kSwap : kKeep, false};
+    const Sel sel_ring = sel_of(rlx);
+    auto fq_word = [&](unsigned char *S, int a, int rr, int cw, unsigned sel) -> float2 {
+        const T2 v = reinterpret_cast<const T2 *>(fqpart(S))[(a * FR + rr) * (W / 2) + cw];
+        return Fm::load2(Fm::perm2(v, sel));
+    };
+    auto phi_pair = [&](int p, int lx, int ly, const Sel &sw, float2(&f)[kQf]) -> float2 {
         using namespace pk;
         const int row = ly + 1, c0 = lx + 1, cq = lx + 3;
         unsigned char *S1 = fstage(p);
-        float2 v0 = reinterpret_cast<const float2 *>(f0part(S1))[row * (W0 / 2) + c0];
-        if ((seam_l && c0 < 2) || (seam_r && c0 >= TXW + 2)) v0 = make_float2(v0.y, v0.x);
-        f[0] = v0;
+        const float2 v0 = reinterpret_cast<const float2 *>(f0part(S1))[row * (W0 / 2) + c0];
+        f[0] = sw.f0 ? make_float2(v0.y, v0.x) : v0;
         if (STREAMED) {
 #pragma unroll
-            for (int a = 0; a < kQf - 1; a++) f[a + 1] = fq_word(S1, a, row, cq);
+            for (int a = 0; a < kQf - 1; a++) f[a + 1] = fq_word(S1, a, row, cq, sw.c);
         } else {
             unsigned char *S0 = fstage(p - 1), *S2 = fstage(p + 1);
             // eta P(x - c) + (1 - eta) P(x), in stored units
-            auto blend = [&](unsigned char *Su, int a, int ru, int cu) {
-                return fma(splat(c.eta), fq_word(Su, a, ru, cu), mul(splat(c.eta2), fq_word(S1, a, row, cq)));
+            auto blend = [&](unsigned char *Su, int a, int ru, int cu, unsigned su) {
+                return fma(splat(c.eta), fq_word(Su, a, ru, cu, su), mul(splat(c.eta2), fq_word(S1, a, row, cq, sw.c)));
             };
-            f[1] = blend(S1, 0, row, cq - 1);
-            f[2] = blend(S1, 1, row, cq + 1);
-            f[3] = blend(S1, 2, row - 1, cq);
-            f[4] = blend(S1, 3, row + 1, cq);
-            f[5] = blend(S0, 4, row, cq);
-            f[6] = blend(S2, 5, row, cq);
+            f[1] = blend(S1, 0, row, cq - 1, sw.m);
+            f[2] = blend(S1, 1, row, cq + 1, sw.p);
+            f[3] = blend(S1, 2, row - 1, cq, sw.c);
+            f[4] = blend(S1, 3, row + 1, cq, sw.c);
+            f[5] = blend(S0, 4, row, cq, sw.c);
+            f[6] = blend(S2, 5, row, cq, sw.c);
         }
         return fma(splat(m.f_inv), add(add(add(add(add(f[1], f[2]), f[3]), f[4]), f[5]), f[6]), f[0]);
     };
     auto build_pair = [&](int p, int s, float2(&fo)[kQf]) {
         float2 *ph = reinterpret_cast<float2 *>(PHI) + s * (RH * RWP);
-        ph[(ty + 1) * RWP + tx + 1] = phi_pair(p, tx + 1, ty + 1, fo);
+        ph[(ty + 1) * RWP + tx + 1] = phi_pair(p, tx + 1, ty + 1, sel_own, fo);
         if (has_ring) {
             float2 tmp[kQf];
-            ph[rly * RWP + rlx] = phi_pair(p, rlx, rly, tmp);
+            ph[rly * RWP + rlx] = phi_pair(p, rlx, rly, sel_ring, tmp);
         }
     };
 
@@ -954,6 +972,7 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
             // seam tile
             const ST *Gs = G + (j & 1) * G_ELEMS;
             const bool wrap_l = seam_l && tx == 0, wrap_r = seam_r && tx == TXW - 1;
+            const unsigned sel_l = wrap_l ? kSwap : kKeep, sel_r = wrap_r ? kSwap : kKeep;
             float2 g[kQg];
 #pragma unroll
             for (int i = 0; i < kQg; i++) {
@@ -962,9 +981,8 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
                 } else if (!ODD || kCx(i) == 0) {
                     g[i] = Fm::load2(*reinterpret_cast<const T2 *>(Gs + (i * TY + ty) * W + E + 2 * tx));
                 } else {
-                    T2 v = *reinterpret_cast<const T2 *>(Gs + (i * TY + ty) * W + E + 2 * tx - 2 * kCx(i));
-                    if (kCx(i) > 0 ? wrap_l : wrap_r) v = Fm::swap2(v);
-                    g[i] = Fm::load2(v);
+                    const T2 v = *reinterpret_cast<const T2 *>(Gs + (i * TY + ty) * W + E + 2 * tx - 2 * kCx(i));
+                    g[i] = Fm::load2(Fm::perm2(v, kCx(i) > 0 ? sel_l : sel_r));
                 }
             }
 
@@ -1076,7 +1094,7 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
                                       (kCy(i) > 0 ? o_yp : kCy(i) < 0 ? o_ym : 0) +
                                       (kCz(i) > 0 ? o_zp : kCz(i) < 0 ? o_zm : 0);
                         T2 h = Fm::store2(qv[i]);
-                        if (kCx(i) != 0 && (kCx(i) > 0 ? wrap_r : wrap_l)) h = Fm::swap2(h);
+                        if (kCx(i) != 0) h = Fm::perm2(h, kCx(i) > 0 ? sel_r : sel_l);
                         if (in_field((long long)id + o, 2, b.n, P.err)) *reinterpret_cast<T2 *>(P.g[i] + id + o) = h;
                     }
                 }
