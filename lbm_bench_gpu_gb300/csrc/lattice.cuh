@@ -30,8 +30,9 @@ __host__ __device__ constexpr int kOpp(int i) { return i == 0 ? 0 : ((i & 1) ? i
 
 // Storage formats: element conversions, and the resident blocks per SM the
 // step kernel's launch bounds ask for.  FP32 stages 108 KB of shared memory
-// per block (2 blocks per SM); the 16-bit formats stage 70 KB, and 3 blocks per
-// SM fit when the kernel stays within 85 registers (it does, without spills).
+// per block (2 blocks of 256 threads per SM, 128 registers); the 16-bit
+// formats stage 54 KB per block of 128 threads, 4 blocks per SM (128
+// registers).
 template <typename ST>
 struct Fmt;
 template <>
@@ -48,7 +49,7 @@ struct Fmt<float> {
 };
 template <>
 struct Fmt<__half> {
-    static constexpr int kMinBlocks = 3;
+    static constexpr int kMinBlocks = 4;
     static constexpr bool kMapped = true;
     using T2 = __half2;   // two adjacent nodes, one 32-bit word
     __device__ static float load(__half v) { return __half2float(v); }
@@ -65,7 +66,7 @@ struct Fmt<__half> {
 };
 template <>
 struct Fmt<__nv_bfloat16> {
-    static constexpr int kMinBlocks = 3;
+    static constexpr int kMinBlocks = 4;
     static constexpr bool kMapped = true;
     using T2 = __nv_bfloat162;
     __device__ static float load(__nv_bfloat16 v) { return __bfloat162float(v); }

@@ -76,8 +76,6 @@ constexpr int TXW = TX / 2;
 constexpr int RWP = TXW + 2;
 constexpr int RINGP = 2 * RWP + 2 * TY;
 constexpr int NG = 2;               // g stages
-constexpr int NF = 4;               // P_f stages
-constexpr int NPHI = 4;             // phi planes
 static_assert(RING <= NT, "one ring node per thread at most");
 static_assert(TX == 32 && TY == 8, "issuer roles assume a 32 x 8 tile");
 
@@ -128,14 +126,22 @@ struct Dir {
     static constexpr int value = I;
 };
 
-// Staging geometry implied by the element size.
+// Staging geometry implied by the element size.  FP32 (two blocks per SM)
+// stages 4 P_f planes and 4 phi planes; the 16-bit formats fit four blocks per
+// SM into the shared memory with 3 + 3 and g rows one chunk narrower (the odd
+// step's shifted rows need one extra chunk on one side only).
 template <typename ST>
 struct Geo {
+    static constexpr bool kSmall = sizeof(ST) == 2;
     static constexpr int E = 16 / (int)sizeof(ST);   // elements per 16-byte chunk
-    static constexpr int W = TX + 2 * E;             // staged row: x in [x0 - E, x0 + TX + E)
+    static constexpr int W = TX + 2 * E;             // staged P_f row: x in [x0 - E, x0 + TX + E)
+    static constexpr int GW = kSmall ? TX + E : TX + 2 * E;   // staged g row
+    static constexpr int GX0 = kSmall ? 0 : E;       // g row column of x0 (even step: E)
+    static constexpr int NF = kSmall ? 3 : 4;        // P_f stages
+    static constexpr int NPHI = kSmall ? 3 : 4;      // phi planes
     static constexpr int CR = W / E;                 // chunks per staged row
     static constexpr int CM = TX / E;                // chunks covering [x0, x0 + TX)
-    static constexpr int G_STAGE = kQg * TY * W * (int)sizeof(ST);            // bytes
+    static constexpr int G_STAGE = kQg * TY * GW * (int)sizeof(ST);           // bytes
     static constexpr int F0_BYTES = FR * W0 * 4;
     static constexpr int F_STAGE = F0_BYTES + (kQf - 1) * FR * W * (int)sizeof(ST);
     static constexpr int PHI_STAGE = sizeof(ST) == 2 ? RH * RWP * 8 : RH * RW * 4;
@@ -149,6 +155,7 @@ struct Geo {
     static constexpr int D = (NT / 2) / TPD;         // directions per pass of the g issuers
     static_assert(G_STAGE % 16 == 0 && F_STAGE % 16 == 0 && F0_BYTES % 16 == 0, "16-byte aligned stages");
     static_assert(G_STAGE % 128 == 0 && G_TMA_BYTES <= G_STAGE, "TMA destinations: 128-byte aligned, inside a stage");
+    static_assert(E + TX <= GW, "even-step rows staged from column E fit a g row");
     static_assert(MBAR_OFF % 8 == 0, "8-byte aligned mbarriers");
     static_assert(F_OFF % 128 == 0 && F_STAGE % 128 == 0 && F0_BYTES % 128 == 0, "P_f TMA destinations 128-byte aligned");
     static_assert(FR * (W0 / 4) <= NT / 2 && FR * CR <= NT / 2, "P_f issuers fit in warps 0-3");
@@ -355,12 +362,13 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
 {
     using Gm = Geo<ST>;
     using Fm = Fmt<ST>;
-    constexpr int E = Gm::E, W = Gm::W, CR = Gm::CR, CM = Gm::CM;
+    constexpr int E = Gm::E, W = Gm::W, GW = Gm::GW, GX0 = Gm::GX0, CR = Gm::CR, CM = Gm::CM;
+    constexpr int NF = Gm::NF, NPHI = Gm::NPHI;
     extern __shared__ __align__(128) unsigned char smem[];
-    ST *const G = reinterpret_cast<ST *>(smem + Gm::G_OFF);            // [NG][19][TY][W]
+    ST *const G = reinterpret_cast<ST *>(smem + Gm::G_OFF);            // [NG][19][TY][GW]
     unsigned char *const F = smem + Gm::F_OFF;                          // [NF]{f0 [FR][W0]; fq [6][FR][W]}
-    float *const PHI = reinterpret_cast<float *>(smem + Gm::PHI_OFF);   // [NPHI][RH][RW]
-    constexpr int G_ELEMS = kQg * TY * W;                               // per stage
+    float *const PHI = reinterpret_cast<float *>(smem + Gm::PHI_OFF);   // [NPHI][RH][RW] (pairs: float2 [RWP])
+    constexpr int G_ELEMS = kQg * TY * GW;                              // per stage
 
     constexpr bool PAIR = use_pair<ST>();
     constexpr int XPT = PAIR ? 2 : 1;          // x nodes per thread (block TX / XPT x TY)
@@ -421,8 +429,10 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
     // columns left of the tile, tiles at the right seam right of it.
     const bool seam_l = x0 == 0, seam_r = x0 + TX == b.nx;
 
-    // P_f stage of plane p (p >= z0 - 2): f_0 part and f_1..f_6 part
-    auto fstage = [&](int p) { return F + ((p - z0 + 4) & (NF - 1)) * Gm::F_STAGE; };
+    // P_f stage of plane p (p >= z0 - 2): planes z0 - 2 + m go to stage m % NF
+    // for their (m / NF)-th use; f_0 part and f_1..f_6 part
+    auto fslot = [&](int p) { return (unsigned)(p - z0 + 2) % (unsigned)NF; };
+    auto fstage = [&](int p) { return F + fslot(p) * Gm::F_STAGE; };
     auto f0part = [&](unsigned char *st) { return reinterpret_cast<float *>(st); };
     auto fqpart = [&](unsigned char *st) { return reinterpret_cast<ST *>(st + Gm::F0_BYTES); };
 
@@ -458,10 +468,11 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
         g_x_wrap = wrap(x0 + TX, b.nx);                // c_x = -1 also needs x0 + TX
     }
 
-    // P_f stage p's mbarrier and the phase of plane p's use of it (planes
-    // z0 - 2 + m go to stage (m + 2) & 3 for their (m >> 2)-th use)
-    auto fbar = [&](int p) { return &mbar[NG + ((p - z0 + 4) & (NF - 1))]; };
-    auto fphase = [&](int p) { return (unsigned)((p - z0 + 2) >> 2) & 1u; };
+    // P_f stage p's mbarrier and the phase of plane p's use of it
+    auto fbar = [&](int p) { return &mbar[NG + fslot(p)]; };
+    auto fphase = [&](int p) { return ((unsigned)(p - z0 + 2) / (unsigned)NF) & 1u; };
+    // phi slot of plane p (planes z0 - 1 + m go to slot m % NPHI)
+    auto pslot = [&](int p) { return (int)((unsigned)(p - z0 + 1) % (unsigned)NPHI); };
 
     // Queue the 7 P_f planes of plane p (tile + halo) into its stage.
     auto issue_f = [&](int p) {
@@ -517,12 +528,12 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
             return;
         }
         if (!g_issuer) return;
-        ST *dst = G + s * G_ELEMS + g_r * W;
+        ST *dst = G + s * G_ELEMS + g_r * GW;
         if (!ODD) {
             const unsigned base = (unsigned)z * (unsigned)b.nxy + (unsigned)(g_row_0 + g_x_hi);
             for_my_dirs([&](auto d) {
                 constexpr int i = decltype(d)::value;
-                if (in_field(base, E, b.n, P.err)) cp_async16(dst + i * TY * W + E + E * g_k, P.gin[i] + base);
+                if (in_field(base, E, b.n, P.err)) cp_async16(dst + i * TY * GW + E + E * g_k, P.gin[i] + base);
             });
         } else {
             const unsigned zb0 = (unsigned)z * (unsigned)b.nxy;
@@ -534,16 +545,18 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
                 const unsigned zb = cz > 0 ? zbp : (cz < 0 ? zbm : zb0);
                 const int row = cy > 0 ? g_row_p : (cy < 0 ? g_row_m : g_row_0);
                 const ST *src = P.gin[kOpp(i)] + (zb + (unsigned)row);
-                ST *d_row = dst + i * TY * W;
+                ST *d_row = dst + i * TY * GW;
                 const long long r0 = (long long)zb + row;   // row start in the field
                 if (cx > 0) {
+                    // columns 0 .. TX + E - 1 hold x0 - E .. x0 + TX - 1
                     if (in_field(r0 + g_x_lo, E, b.n, P.err)) cp_async16(d_row + E * g_k, src + g_x_lo);
                     if (g_k == 0 && in_field(r0 + x0 + TX - E, E, b.n, P.err))
                         cp_async16(d_row + TX, src + (x0 + TX - E));
                 } else {
-                    if (in_field(r0 + g_x_hi, E, b.n, P.err)) cp_async16(d_row + E + E * g_k, src + g_x_hi);
+                    // columns GX0 .. hold x0 .. x0 + TX (+ E for cx < 0)
+                    if (in_field(r0 + g_x_hi, E, b.n, P.err)) cp_async16(d_row + GX0 + E * g_k, src + g_x_hi);
                     if (cx < 0 && g_k == 0 && in_field(r0 + g_x_wrap, E, b.n, P.err))
-                        cp_async16(d_row + TX + E, src + g_x_wrap);
+                        cp_async16(d_row + TX + GX0, src + g_x_wrap);
                 }
             });
         }
@@ -667,28 +680,39 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
     pdl_launch_dependents();
     pdl_wait();   // the previous step's writes are complete and visible
 
-    // prologue: P_f planes z0-2 .. z0+1, g of plane z0; phi of z0-1 and z0
+    // prologue: P_f planes z0-2 .. z0+1 (with 3 stages: z0+1 after the first
+    // build), g of plane z0; phi of z0-1 and z0
+    constexpr int kAhead = NF - 1;   // P_f planes past z0 - 2 staged before the first build
     issue_f(z0 - 2);
     issue_f(z0 - 1);
     issue_f(z0);
-    issue_f(z0 + 1);
+    if (kAhead >= 3) issue_f(z0 + 1);
     issue_g(z0, 0);
     cp_async_commit();
     cp_async_wait_all();
     bool late = false;
     if (tile_tma_f) {
-        for (int p = z0 - 2; p <= z0 + 1; p++) late |= !mbar_wait(fbar(p), fphase(p));
+        for (int p = z0 - 2; p <= z0 - 2 + kAhead; p++) late |= !mbar_wait(fbar(p), fphase(p));
     }
     __syncthreads();
     if constexpr (PAIR) {
         float2 tmp[kQf];
-        build_pair(z0 - 1, 0, tmp);
-        build_pair(z0, 1, fcur2);
+        build_pair(z0 - 1, pslot(z0 - 1), tmp);
     } else {
         float tmp[XPT][kQf];
-        build_plane(z0 - 1, 0, tmp);
-        build_plane(z0, 1, fcur);
+        build_plane(z0 - 1, pslot(z0 - 1), tmp);
     }
+    if (kAhead < 3) {
+        // the stage of plane z0 - 2 is free once every thread has built z0 - 1
+        __syncthreads();
+        issue_f(z0 + 1);
+        cp_async_commit();
+        cp_async_wait_all();
+        if (tile_tma_f) late |= !mbar_wait(fbar(z0 + 1), fphase(z0 + 1));
+        __syncthreads();
+    }
+    if constexpr (PAIR) build_pair(z0, pslot(z0), fcur2);
+    else build_plane(z0, pslot(z0), fcur);
     __syncthreads();
     issue_f(z0 + 2);
     cp_async_commit();
@@ -699,14 +723,14 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
         __syncthreads();
         if (j + 1 < nzc) {
             issue_g(z + 1, (j + 1) & 1);
-            issue_f(z + 3);
+            if (kAhead >= 3) issue_f(z + 3);
         }
         cp_async_commit();
         // P_f plane z + 2 is first read here (a late copy only spoils values:
         // the uniform exit below comes before anything is stored)
         if (tile_tma_f) late |= !mbar_wait(fbar(z + 2), fphase(z + 2));
-        if constexpr (PAIR) build_pair(z + 1, (j + 2) & 3, fnext2);
-        else build_plane(z + 1, (j + 2) & 3, fnext);
+        if constexpr (PAIR) build_pair(z + 1, pslot(z + 1), fnext2);
+        else build_plane(z + 1, pslot(z + 1), fnext);
         if constexpr (TMA) {
             // g of plane z: stage j & 1, its (j >> 1)-th use (cp.async tiles
             // were complete at the barrier above)
@@ -715,16 +739,22 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
                 if (tid == 0) atomicOr(P.err, 1);
                 // copies still in flight: wait for them (bounded) before leaving
                 if (g_tma && j + 1 < nzc) mbar_wait(&mbar[(j + 1) & 1], (unsigned)((j + 1) >> 1) & 1u);
-                if (tile_tma_f && j + 1 < nzc) mbar_wait(fbar(z + 3), fphase(z + 3));
+                if (kAhead >= 3 && tile_tma_f && j + 1 < nzc) mbar_wait(fbar(z + 3), fphase(z + 3));
                 return;
             }
         } else {
             __syncthreads();
         }
+        // with 3 P_f stages plane z + 3 goes into plane z's stage, free now
+        // that every thread has built phi of z + 1
+        if (kAhead < 3) {
+            if (j + 1 < nzc) issue_f(z + 3);
+            cp_async_commit();
+        }
 
-        const float *S0 = PHI + (j & 3) * (RH * RW);        // plane z - 1
-        const float *S1 = PHI + ((j + 1) & 3) * (RH * RW);  // plane z
-        const float *S2 = PHI + ((j + 2) & 3) * (RH * RW);  // plane z + 1
+        const float *S0 = PHI + pslot(z - 1) * (RH * RW);   // plane z - 1
+        const float *S1 = PHI + pslot(z) * (RH * RW);       // plane z
+        const float *S2 = PHI + pslot(z + 1) * (RH * RW);   // plane z + 1
         if constexpr (!PAIR) {
         const int lx = tx + 1, ly = ty + 1;
         auto at = [&](const float *S, int yy, int xx) { return S[yy * RW + xx]; };
@@ -761,7 +791,7 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
 #pragma unroll
         for (int i = 0; i < kQg; i++)
             g[i] = Fm::load((TMA && !ODD) ? Gs[(i * TY + ty) * TX + tx]
-                                          : Gs[(i * TY + ty) * W + E + tx - (ODD ? kCx(i) : 0)]);
+                            : Gs[(i * TY + ty) * GW + (!ODD || kCx(i) > 0 ? E : GX0) + tx - (ODD ? kCx(i) : 0)]);
 
         // moments: src/update_rho.cu:46-50, src/update_velocity.cu:47-59
         float rho = g[0];
@@ -935,9 +965,9 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
             // neighbours are the neighbouring words' nodes, so every stencil point
             // is one float2 of the phi ring.
             using namespace pk;
-            const float2 *Q0 = reinterpret_cast<const float2 *>(PHI) + (j & 3) * (RH * RWP);        // plane z - 1
-            const float2 *Q1 = reinterpret_cast<const float2 *>(PHI) + ((j + 1) & 3) * (RH * RWP);  // plane z
-            const float2 *Q2 = reinterpret_cast<const float2 *>(PHI) + ((j + 2) & 3) * (RH * RWP);  // plane z + 1
+            const float2 *Q0 = reinterpret_cast<const float2 *>(PHI) + pslot(z - 1) * (RH * RWP);   // plane z - 1
+            const float2 *Q1 = reinterpret_cast<const float2 *>(PHI) + pslot(z) * (RH * RWP);       // plane z
+            const float2 *Q2 = reinterpret_cast<const float2 *>(PHI) + pslot(z + 1) * (RH * RWP);   // plane z + 1
             const int lx = tx + 1, ly = ty + 1;
             auto at = [&](const float2 *S, int yy, int xx) { return S[yy * RWP + xx]; };
             const float2 pc = at(Q1, ly, lx);
@@ -978,10 +1008,13 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
             for (int i = 0; i < kQg; i++) {
                 if (TMA && !ODD) {
                     g[i] = Fm::load2(*reinterpret_cast<const T2 *>(Gs + (i * TY + ty) * TX + 2 * tx));
-                } else if (!ODD || kCx(i) == 0) {
-                    g[i] = Fm::load2(*reinterpret_cast<const T2 *>(Gs + (i * TY + ty) * W + E + 2 * tx));
+                } else if (!ODD) {
+                    g[i] = Fm::load2(*reinterpret_cast<const T2 *>(Gs + (i * TY + ty) * GW + E + 2 * tx));
+                } else if (kCx(i) == 0) {
+                    g[i] = Fm::load2(*reinterpret_cast<const T2 *>(Gs + (i * TY + ty) * GW + GX0 + 2 * tx));
                 } else {
-                    const T2 v = *reinterpret_cast<const T2 *>(Gs + (i * TY + ty) * W + E + 2 * tx - 2 * kCx(i));
+                    const T2 v = *reinterpret_cast<const T2 *>(Gs + (i * TY + ty) * GW + (kCx(i) > 0 ? E : GX0) + 2 * tx
+                                                               - 2 * kCx(i));
                     g[i] = Fm::load2(Fm::perm2(v, kCx(i) > 0 ? sel_l : sel_r));
                 }
             }
@@ -1118,8 +1151,13 @@ cudaError_t configure()
 {
     static bool done = false;   // per template instance, per process
     if (done) return cudaSuccess;
-    const cudaError_t e = cudaFuncSetAttribute(zsc_step_kernel<ST, S, O, T>,
-                                               cudaFuncAttributeMaxDynamicSharedMemorySize, Geo<ST>::SMEM);
+    cudaError_t e = cudaFuncSetAttribute(zsc_step_kernel<ST, S, O, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         Geo<ST>::SMEM);
+    // all of the unified L1 / shared storage as shared memory: the resident
+    // blocks per SM the launch bounds ask for need it
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(zsc_step_kernel<ST, S, O, T>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 (int)cudaSharedmemCarveoutMaxShared);
     if (e == cudaSuccess) done = true;
     return e;
 }
