@@ -174,14 +174,31 @@ int load_state(lbm_ctx *c, const float *tf, const float *tg)
     return LBM_OK;
 }
 
-// Equilibrium from the fields in c->st.mom into the state.
+// Equilibrium from the fields in c->st.mom into the state.  FP32 storage
+// holds the streamed FP32 distributions as they are, so the equilibrium is
+// written straight into half 0; the 16-bit formats go through FP32 scratch,
+// from which the storage map is chosen.
 int init_from_mom(lbm_ctx *c, const float *ghost_lo, const float *ghost_hi)
 {
     const size_t n = (size_t)c->box.n;
+    if (c->p.storage == LBM_STORAGE_FP32) {
+        identity_quant(c->q);
+        const lbm::StepView v = view(c, 0);
+        LBM_CUDA(lbm::launch_equilibrium(c->box, c->d, c->p.Gamma, c->st.mom, c->st.mom + n, ghost_lo, ghost_hi,
+                                         c->st.f0, static_cast<float *>(const_cast<void *>(v.fq_in)),
+                                         static_cast<float *>(c->st.g), c->stream),
+                 "equilibrium kernel");
+        LBM_CUDA(cudaStreamSynchronize(c->stream), "init");
+        c->st.f_cur = 0;
+        c->st.f_streamed = true;
+        c->st.g_odd_next = false;
+        c->st.steps = 0;
+        return LBM_OK;
+    }
     float *tmp = nullptr;
     LBM_CUDA(cudaMalloc(&tmp, sizeof(float) * (lbm::kQf + lbm::kQg) * n), "init scratch");
     cudaError_t e = lbm::launch_equilibrium(c->box, c->d, c->p.Gamma, c->st.mom, c->st.mom + n, ghost_lo, ghost_hi,
-                                            tmp, tmp + lbm::kQf * n, c->stream);
+                                            tmp, tmp + n, tmp + lbm::kQf * n, c->stream);
     int rc = e == cudaSuccess ? load_state(c, tmp, tmp + lbm::kQf * n) : cuda_fail(e, "equilibrium kernel");
     cudaStreamSynchronize(c->stream);
     cudaFree(tmp);

@@ -53,7 +53,9 @@ struct Quant {
 //  g      : 19 x n              D3Q19 in the in-place AA layout
 //  mom    : 5 x n floats        phi, rho, ux, uy, uz as the reference's arrays hold them
 // f holds post-collision values, except right after init / lbm_set_dist
-// (f_streamed), when it holds streamed values.
+// (f_streamed), when it holds streamed values.  FP32 storage keeps f0, fq and
+// g in the natural layout; the 16-bit formats keep them in the pair layout
+// (storage_index in lattice.cuh); mom is always natural.
 struct State {
     float *f0 = nullptr;
     void *fq = nullptr;
@@ -114,9 +116,11 @@ StepConst step_const(const lbm_derived &d, const lbm_params &p, float grav);
 // Kernel launchers (defined in the .cu files); all return the cudaError_t of the launch.
 cudaError_t launch_bubble_phi(const Box &b, const float *bubbles_dev, int nbubbles, float phiStar, float width,
                               float *phi_ghosted, cudaStream_t s);
-// At-rest equilibrium into FP32 arrays f (7 x n) and g (19 x n), streamed layout.
+// At-rest equilibrium into FP32 arrays f_0 (n), f_1..f_6 (6 x n) and g (19 x n),
+// streamed natural layout.
 cudaError_t launch_equilibrium(const Box &b, const lbm_derived &d, float Gamma, const float *phi, const float *rho,
-                               const float *ghost_lo, const float *ghost_hi, float *f, float *g, cudaStream_t s);
+                               const float *ghost_lo, const float *ghost_hi, float *f0, float *fq, float *g,
+                               cudaStream_t s);
 cudaError_t launch_fill(float *p, long long n, float v, cudaStream_t s);
 cudaError_t launch_step(const Box &b, const StepConst &c, const Quant &q, const StepView &v, bool f_streamed,
                         bool odd, bool write_moments, cudaStream_t s);
@@ -125,7 +129,7 @@ cudaError_t launch_wait_selftest(int *err, cudaStream_t s);
 // State (post-collision / AA layout, any storage) -> streamed FP32 f (7 x n) and g (19 x n).
 cudaError_t launch_stream_out(const Box &b, float eta, const Quant &q, const StepView &v, bool f_streamed, bool odd,
                               float *f_out, float *g_out, cudaStream_t s);
-// Streamed FP32 f, g -> state half 0 (natural layout), applying the storage map.
+// Streamed FP32 f, g -> state half 0 (natural g slots, the storage's layout), applying the storage map.
 cudaError_t launch_quantize(const Box &b, const Quant &q, int storage, const float *f, const float *g, float *f0,
                             void *fq, void *gq, cudaStream_t s);
 // Per-field max |x - shift| of the 7 f and 19 g FP32 arrays (26 floats at out, device).

@@ -47,7 +47,7 @@ __global__ void bubble_phi_kernel(Box b, const float *__restrict__ bubbles, int 
 __global__ void equilibrium_kernel(Box b, float alpha4, float kappa, float phiStarSq, float Gamma,
                                    const float *__restrict__ phi, const float *__restrict__ rho,
                                    const float *__restrict__ ghost_lo, const float *__restrict__ ghost_hi,
-                                   float *__restrict__ f, float *__restrict__ g)
+                                   float *__restrict__ f0, float *__restrict__ fq, float *__restrict__ g)
 {
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < b.n;
          t += (long long)gridDim.x * blockDim.x) {
@@ -69,8 +69,8 @@ __global__ void equilibrium_kernel(Box b, float alpha4, float kappa, float phiSt
                                     - 12.f * phin)) * kInv6;
         const float mu = alpha4 * phin * (phin * phin - phiStarSq) - kappa * lap;
         const float Af = 0.5f * Gamma * mu;
-        f[t] = phin - 3.f * Gamma * mu;
-        for (int q = 1; q < kQf; q++) f[q * b.n + t] = Af;
+        f0[t] = phin - 3.f * Gamma * mu;
+        for (int q = 1; q < kQf; q++) fq[(q - 1) * b.n + t] = Af;
         const float rhon = rho[t];
         const float Ag1 = kW1 * (3.f * phin * mu + rhon);
         const float Ag2 = kW2 * (3.f * phin * mu + rhon);
@@ -104,10 +104,11 @@ cudaError_t launch_bubble_phi(const Box &b, const float *bubbles_dev, int nbubbl
 }
 
 cudaError_t launch_equilibrium(const Box &b, const lbm_derived &d, float Gamma, const float *phi, const float *rho,
-                               const float *ghost_lo, const float *ghost_hi, float *f, float *g, cudaStream_t s)
+                               const float *ghost_lo, const float *ghost_hi, float *f0, float *fq, float *g,
+                               cudaStream_t s)
 {
     equilibrium_kernel<<<grid_for(b.n), 256, 0, s>>>(b, d.alpha4, d.kappa, d.phiStarSq, Gamma, phi, rho, ghost_lo,
-                                                      ghost_hi, f, g);
+                                                      ghost_hi, f0, fq, g);
     return cudaGetLastError();
 }
 
