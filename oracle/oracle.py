@@ -55,6 +55,13 @@ def oracle_lib() -> C.CDLL:
         lib.zo_dist.argtypes = [C.c_void_p, _D, _D]
         lib.zo_set_dist.argtypes = [C.c_void_p, _D, _D]
         lib.zo_compare.argtypes = [C.c_void_p, _Fp, _Fp, _Fp, _D]
+        lib.zo_slab_create.argtypes = [C.c_int, C.c_int, C.c_int, _D]
+        lib.zo_slab_create.restype = C.c_void_p
+        for name in ("zo_slab_moments", "zo_slab_stream"):
+            getattr(lib, name).argtypes = [C.c_void_p]
+        lib.zo_slab_collide.argtypes = [C.c_void_p, C.c_double]
+        for name in ("zo_slab_phi_plane", "zo_slab_set_phi_ghost", "zo_slab_post_plane", "zo_slab_set_post_ghost"):
+            getattr(lib, name).argtypes = [C.c_void_p, C.c_int, _D]
         lib.zo_stats.argtypes = [C.c_void_p, _D]
         lib.zo_steps.argtypes = [C.c_void_p]
         lib.zo_steps.restype = C.c_long
@@ -227,6 +234,58 @@ class Oracle:
             self.close()
         except Exception:
             pass
+
+
+class SlabOracle(Oracle):
+    """The FP64 step on planes [z0, z0 + nz) of a periodic box whose other
+    planes live elsewhere (another rank): the reference's domain split
+    (src/vgrid.c:38-52) with its three halo exchanges per step, as whole
+    planes (zsc_oracle.c, zo_slab_*).  One step is
+
+        moments(); exchange phi planes; collide(grav); exchange post planes; stream()
+
+    where an exchange sends plane(side 0) to the slab below and plane(side 1)
+    to the slab above, and sets the received planes as ghosts (side 0 below,
+    side 1 above)."""
+
+    def __init__(self, nx: int, ny: int, nz: int, **kw):
+        self.lib = oracle_lib()
+        prm = np.array([np.float32(kw[k]) for k in ("rhoL", "rhoH", "tauRho", "tauPhi", "width", "sigma", "Gamma")]
+                       + [np.float32(kw.get("Eo", 0.0)), np.float32(kw.get("rc0", 0.0))], np.float64)
+        self.h = self.lib.zo_slab_create(nx, ny, nz, _dptr(prm))
+        if not self.h:
+            raise MemoryError("zo_slab_create failed")
+        self.shape = (nz, ny, nx)
+        self.nx, self.ny, self.nz = nx, ny, nz
+        self.rhoL, self.rhoH = float(prm[0]), float(prm[1])
+
+    def moments_update(self) -> None:
+        self.lib.zo_slab_moments(self.h)
+
+    def phi_plane(self, side: int) -> np.ndarray:
+        out = np.empty((self.ny, self.nx), np.float64)
+        self.lib.zo_slab_phi_plane(self.h, side, _dptr(out))
+        return out
+
+    def set_phi_ghost(self, side: int, plane) -> None:
+        self.lib.zo_slab_set_phi_ghost(self.h, side, _dptr(np.ascontiguousarray(plane, np.float64)))
+
+    def collide(self, grav: float) -> None:
+        self.lib.zo_slab_collide(self.h, float(grav))
+
+    def post_plane(self, side: int) -> np.ndarray:
+        out = np.empty((26, self.ny, self.nx), np.float64)
+        self.lib.zo_slab_post_plane(self.h, side, _dptr(out))
+        return out
+
+    def set_post_ghost(self, side: int, planes) -> None:
+        self.lib.zo_slab_set_post_ghost(self.h, side, _dptr(np.ascontiguousarray(planes, np.float64)))
+
+    def stream(self) -> None:
+        self.lib.zo_slab_stream(self.h)
+
+    def step(self, n: int, grav: float = 0.0) -> None:
+        raise TypeError("a slab steps through moments_update / collide / stream with exchanges between them")
 
 
 def oracle_from_inputs(p, bubbles=None) -> Oracle:

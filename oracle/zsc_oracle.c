@@ -66,6 +66,12 @@ typedef struct zo_ctx {
     unsigned char *heavy_log;
     long heavy_cap, heavy_pos;
     int heavy_mode;               /* 0 phi > 0, 1 record, 2 replay */
+    /* z-slab of a larger periodic box (zo_slab_create): no z wrap; the planes
+     * just below and above the slab come from its neighbours, phi after the
+     * moments (2 planes) and the post-collision P, Q after the collision
+     * (2 x 26 planes: side, then f 0..6, g 0..18). */
+    int slab;
+    double *phi_ghost, *post_ghost;
 } zo_ctx;
 
 static inline long zo_idx(const zo_ctx *s, int x, int y, int z)
@@ -145,6 +151,8 @@ void zo_destroy(zo_ctx *s)
     for (int i = 0; i < 19; i++) { free(s->g[i]); free(s->gp[i]); }
     free(s->phi); free(s->rho); free(s->ux); free(s->uy); free(s->uz);
     free(s->heavy_log);
+    free(s->phi_ghost);
+    free(s->post_ghost);
     free(s);
 }
 
@@ -334,7 +342,7 @@ static void zo_collide(zo_ctx *s, double grav)
             for (int x = 0; x < s->nx; x++) {
                 const long id = zo_idx(s, x, y, z);
                 double lap, gx, gy, gz;
-                stencil(s, s->phi, NULL, x, y, z, &lap, &gx, &gy, &gz);
+                stencil(s, s->phi, s->phi_ghost, x, y, z, &lap, &gx, &gy, &gz);
                 const double ph = s->phi[id], rh = s->rho[id];
                 const double mu = c->alpha4 * ph * (ph * ph - c->phiStarSq) - c->kappa * lap;
                 const double Fx = mu * gx, Fy = mu * gy;
@@ -431,6 +439,106 @@ static void zo_stream(zo_ctx *s)
             }
         }
     }
+}
+
+/*
+ * z-slabs: the same step split over ranks that each hold planes [z0, z0 + nz)
+ * of a periodic box, as the reference splits it over MPI ranks
+ * (src/vgrid.c:38-52), with its three halo exchanges per step
+ * (src/main.cu:496-608): phi after update_phi (src/pack_mpi_phi.cu,
+ * src/mpiupdate_phi.c), then the post-collision f and g before streaming
+ * (src/pack_mpi_f.cu, src/pack_mpi.cu, src/mpiupdate*.c).  Here each exchange
+ * moves whole planes: a rank sends its first plane to the rank below and its
+ * last plane to the rank above, and receives the neighbours' planes as its
+ * ghosts (side 0 below, side 1 above).  One step of a slab:
+ *   zo_slab_moments; exchange phi (zo_slab_phi_plane -> zo_slab_set_phi_ghost);
+ *   zo_slab_collide; exchange P, Q (zo_slab_post_plane -> zo_slab_set_post_ghost);
+ *   zo_slab_stream.
+ * Streaming pulls, f_i(x) = eta P_i(x - c_i) + (1 - eta) P_i(x) and
+ * g_i(x) = Q_i(x - c_i) with the upstream values below / above the slab from
+ * the ghosts: the same arithmetic as zo_stream's push, node for node.
+ */
+zo_ctx *zo_slab_create(int nx, int ny, int nz, const double *prm)
+{
+    if (nz < 1) return NULL;
+    /* zo_create wants nz >= 3 for the periodic box; a slab may be thinner */
+    zo_ctx *s = zo_create(nx, ny, nz < 3 ? 3 : nz, prm);
+    if (!s) return NULL;
+    s->nz = nz;
+    s->n = (long)nx * ny * nz;
+    s->slab = 1;
+    const long nxy = (long)nx * ny;
+    s->phi_ghost = (double *)calloc((size_t)(2 * nxy), sizeof(double));
+    s->post_ghost = (double *)calloc((size_t)(2 * 26 * nxy), sizeof(double));
+    if (!s->phi_ghost || !s->post_ghost) {
+        zo_destroy(s);
+        return NULL;
+    }
+    return s;
+}
+
+void zo_slab_moments(zo_ctx *s) { zo_moments_update(s); }
+
+/* phi of the slab's first (side 0) or last (side 1) plane, nx*ny values */
+void zo_slab_phi_plane(const zo_ctx *s, int side, double *out)
+{
+    const long nxy = (long)s->nx * s->ny;
+    memcpy(out, s->phi + (side ? (long)(s->nz - 1) * nxy : 0), sizeof(double) * nxy);
+}
+
+/* the plane below (side 0) or above (side 1) the slab */
+void zo_slab_set_phi_ghost(zo_ctx *s, int side, const double *in)
+{
+    const long nxy = (long)s->nx * s->ny;
+    memcpy(s->phi_ghost + (side ? nxy : 0), in, sizeof(double) * nxy);
+}
+
+void zo_slab_collide(zo_ctx *s, double grav) { zo_collide(s, grav); }
+
+/* post-collision P_0..P_6, Q_0..Q_18 of the first (side 0) or last (side 1)
+ * plane: 26 x nx*ny values */
+void zo_slab_post_plane(const zo_ctx *s, int side, double *out)
+{
+    const long nxy = (long)s->nx * s->ny, off = side ? (long)(s->nz - 1) * nxy : 0;
+    for (int i = 0; i < 7; i++) memcpy(out + (long)i * nxy, s->fp[i] + off, sizeof(double) * nxy);
+    for (int i = 0; i < 19; i++) memcpy(out + (long)(7 + i) * nxy, s->gp[i] + off, sizeof(double) * nxy);
+}
+
+void zo_slab_set_post_ghost(zo_ctx *s, int side, const double *in)
+{
+    const long nxy = (long)s->nx * s->ny;
+    memcpy(s->post_ghost + (long)side * 26 * nxy, in, sizeof(double) * 26 * nxy);
+}
+
+/* post-collision field q (0..6 P, 7..25 Q) at (x, y, z) - c, z - c_z possibly
+ * outside the slab (then from the ghost of that side) */
+static inline double slab_upstream(const zo_ctx *s, int q, const double *arr, int x, int y, int z, const int *c)
+{
+    const long nxy = (long)s->nx * s->ny;
+    const int xs = wrap(x - c[0], s->nx), ys = wrap(y - c[1], s->ny), zs = z - c[2];
+    const long p = (long)xs + (long)s->nx * ys;
+    if (zs < 0) return s->post_ghost[(long)q * nxy + p];
+    if (zs >= s->nz) return s->post_ghost[(long)(26 + q) * nxy + p];
+    return arr[zo_idx(s, xs, ys, zs)];
+}
+
+void zo_slab_stream(zo_ctx *s)
+{
+    const double eta = s->c.eta, eta2 = s->c.eta2;
+#pragma omp parallel for schedule(static)
+    for (int z = 0; z < s->nz; z++) {
+        for (int y = 0; y < s->ny; y++) {
+            for (int x = 0; x < s->nx; x++) {
+                const long id = zo_idx(s, x, y, z);
+                s->f[0][id] = s->fp[0][id];
+                for (int i = 1; i < 7; i++)
+                    s->f[i][id] = eta * slab_upstream(s, i, s->fp[i], x, y, z, CF[i]) + eta2 * s->fp[i][id];
+                s->g[0][id] = s->gp[0][id];
+                for (int i = 1; i < 19; i++) s->g[i][id] = slab_upstream(s, 7 + i, s->gp[i], x, y, z, CG[i]);
+            }
+        }
+    }
+    s->steps++;
 }
 
 /* One or more steps in the order of src/main.cu:363-473 (relaxation loop) and
