@@ -270,6 +270,84 @@ long long lbm_adjoint_forward_steps(long long nsteps, int slots);
 int lbm_stats_noalloc(const lbm_params *p, const float *phi, const float *rho, const float *ux,
                       const float *uy, const float *uz, double *raw_out, void *stream);
 
+/* ---- z-slab decomposition: one box over several contexts (GPUs) ----
+ *
+ * The reference splits the box in z over MPI ranks (src/vgrid.c:38-52) and
+ * exchanges halo planes three times per step through host buffers
+ * (src/main.cu:496-608 with src/pack_mpi*.cu, src/unpack_mpi*.cu,
+ * src/mpiupdate*.c).  Here a z-slab context holds planes [z0, z0 + nz) of the
+ * box, on its own device, with ghost planes around its fields; the fused step
+ * needs two exchanges per step, both of whole planes:
+ *   before every step (LBM_HALO_PRE): the two boundary planes of the seven f
+ *     fields each way (the step's phi stencil reaches two planes out), and,
+ *     before an odd step of the in-place (AA) g update, one boundary plane of
+ *     the five g fields whose direction crosses the slab boundary;
+ *   after an odd step (LBM_HALO_POST): the g values the step wrote into the
+ *     ghost planes, back to the neighbour whose nodes they belong to.
+ * A slab sends its "lo" buffer to the slab below and its "hi" buffer to the
+ * slab above (periodic in z: the first slab's "below" is the last slab), and
+ * unpacks what it receives from below as "lo" and from above as "hi".
+ * LBM_HALO_PHI moves the boundary planes of the phi field for the statistics.
+ * Slab contexts do not step with lbm_step and have no lbm_get_dist /
+ * lbm_set_dist / snapshots / adjoint: they are made from and merged back into
+ * a whole-box context. */
+#define LBM_HALO_PRE 0
+#define LBM_HALO_POST 1
+#define LBM_HALO_PHI 2
+
+/* Split the state of a whole-box context into nslabs z-slab contexts of
+ * depths[k] >= 2 planes (summing to the box's nz; slab k starts at the sum of
+ * the depths before it), slab k on device devices[k] (NULL: the whole
+ * context's device), each with the whole context's parameters, storage map
+ * and step count.  No counterpart in the reference (its ranks each build their
+ * slab from the input files).  The whole context is left as it was. */
+int lbm_split_z(lbm_ctx *whole, int nslabs, const int *depths, const int *devices, lbm_ctx **slabs);
+
+/* Gather the states of the slabs (as lbm_split_z made them, in order) back
+ * into the whole-box context they came from (or one created with the same
+ * parameters).  LBM_ESTATE if a slab still owes its neighbours the
+ * LBM_HALO_POST exchange of an odd step.  Synchronises. */
+int lbm_merge_z(lbm_ctx *const *slabs, int nslabs, lbm_ctx *whole);
+
+/* nsteps steps of the whole box held by the slabs, with every exchange done
+ * by device-to-device copies between the slabs' buffers (peer copies across
+ * devices), ordered by events on the slabs' streams: the one-process driver
+ * of the protocol above.  The phi, rho, u fields are written on the last step.
+ * Asynchronous (lbm_sync each slab, or lbm_merge_z). */
+int lbm_slab_step(lbm_ctx *const *slabs, int nslabs, int nsteps, float grav);
+
+/* For one slab per process: the bytes of one side's buffer for a phase at the
+ * slab's current step (0 when the phase has nothing to move: LBM_HALO_POST
+ * after an even step), and the copies between the slab's planes and the
+ * caller's device buffers (send_lo / send_hi, recv_lo / recv_hi, that many
+ * bytes each), queued on the slab's stream.  A process moves the buffers to
+ * its neighbours (NCCL send / recv, MPI, ...) between pack and unpack. */
+long long lbm_halo_bytes(const lbm_ctx *slab, int phase);
+int lbm_halo_pack(lbm_ctx *slab, int phase, void *send_lo, void *send_hi);
+int lbm_halo_unpack(lbm_ctx *slab, int phase, const void *recv_lo, const void *recv_hi);
+
+/* One step of a slab whose LBM_HALO_PRE exchange the caller has done; after
+ * an odd step the LBM_HALO_POST exchange follows.  Writes the phi, rho, u
+ * fields.  Asynchronous. */
+int lbm_slab_step_local(lbm_ctx *slab, float grav);
+
+/* The 16 raw FP64 sums and maxima behind lbm_stats_out of a context's phi,
+ * rho, u fields (layout of lbm_stats_noalloc's raw_out), for combining over
+ * slabs: sums add and entries 0 and 13 (max |u|^2) take the maximum, the FP64
+ * counterpart of the reference's MPI_Reduce of its statistics
+ * (src/stats.c:57-58).  A slab's pressure sums need the phi planes around
+ * it: do the LBM_HALO_PHI exchange first.  Synchronises. */
+int lbm_stats_raw(lbm_ctx *c, double *raw);
+
+/* lbm_stats_out of a whole box (p: its parameters, steps: its step count)
+ * from raw statistics combined over its slabs (nraw sets of 16, combined
+ * here; or one set the caller already reduced across processes). */
+int lbm_stats_combine(const lbm_params *p, long long steps, const double *raw, int nraw, lbm_stats_out *s);
+
+/* Statistics of the whole box held by the slabs: the LBM_HALO_PHI exchange,
+ * lbm_stats_raw of each slab and lbm_stats_combine.  Synchronises. */
+int lbm_slab_stats(lbm_ctx *const *slabs, int nslabs, lbm_stats_out *s);
+
 /* Checkpoint / resume (no counterpart in the reference, whose VTK files are
  * output only): a snapshot of the context's state in its native form (the
  * current f_0 and f_1..f_6, g in its AA layout, the five moment fields, the

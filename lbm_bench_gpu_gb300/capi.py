@@ -25,6 +25,8 @@ EXPORTS = [
     "lbm_strerror", "lbm_last_error", "lbm_stats_noalloc", "lbm_step_adjoint",
     "lbm_objective", "lbm_stats_fields", "lbm_pressure", "lbm_device_name", "lbm_adjoint_release",
     "lbm_wait_selftest", "lbm_adjoint_forward_steps", "lbm_state_bytes", "lbm_save_state", "lbm_load_state",
+    "lbm_split_z", "lbm_merge_z", "lbm_slab_step", "lbm_halo_bytes", "lbm_halo_pack", "lbm_halo_unpack",
+    "lbm_slab_step_local", "lbm_stats_raw", "lbm_stats_combine", "lbm_slab_stats",
 ]
 OBJECTIVES = {"light_uz_mean": 0, "light_z_centroid": 1}
 
@@ -133,6 +135,18 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.lbm_strerror.restype = C.c_char_p
     lib.lbm_last_error.argtypes = []
     lib.lbm_last_error.restype = C.c_char_p
+    _V, _I, _D = C.POINTER(C.c_void_p), C.POINTER(C.c_int), C.POINTER(C.c_double)
+    lib.lbm_split_z.argtypes = [C.c_void_p, C.c_int, _I, _I, _V]
+    lib.lbm_merge_z.argtypes = [_V, C.c_int, C.c_void_p]
+    lib.lbm_slab_step.argtypes = [_V, C.c_int, C.c_int, C.c_float]
+    lib.lbm_halo_bytes.argtypes = [C.c_void_p, C.c_int]
+    lib.lbm_halo_bytes.restype = C.c_longlong
+    lib.lbm_halo_pack.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+    lib.lbm_halo_unpack.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+    lib.lbm_slab_step_local.argtypes = [C.c_void_p, C.c_float]
+    lib.lbm_stats_raw.argtypes = [C.c_void_p, _D]
+    lib.lbm_stats_combine.argtypes = [C.POINTER(Params), C.c_longlong, _D, C.c_int, C.POINTER(StatsOut)]
+    lib.lbm_slab_stats.argtypes = [_V, C.c_int, C.POINTER(StatsOut)]
     if path is None:
         _lib = lib
     return lib
@@ -189,6 +203,18 @@ def derive(p: Params) -> Derived:
     d = Derived()
     check(load().lbm_derive(C.byref(p), C.byref(d)), "lbm_derive")
     return d
+
+
+LBM_HALO_PRE, LBM_HALO_POST, LBM_HALO_PHI = 0, 1, 2
+
+
+def stats_combine(params: Params, steps: int, raw) -> dict:
+    """lbm_stats_combine: lbm_stats_out of a whole box from per-slab raw statistics."""
+    r = np.ascontiguousarray(raw, np.float64).reshape(-1, 16)
+    s = StatsOut()
+    check(load().lbm_stats_combine(C.byref(params), int(steps), r.ctypes.data_as(C.POINTER(C.c_double)), len(r),
+                                   C.byref(s)), "lbm_stats_combine")
+    return s.as_dict()
 
 
 class Lattice:
@@ -313,6 +339,61 @@ class Lattice:
     def close(self) -> None:
         if self._h:
             load().lbm_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Slabs:
+    """A whole box held by z-slab contexts (lbm_split_z): slab k holds
+    depths[k] consecutive planes, on devices[k] (default: the whole context's
+    device); lbm_slab_step steps them together with their halo exchanges."""
+
+    def __init__(self, whole: Lattice, depths, devices=None):
+        self.params = whole.params
+        self.n = len(depths)
+        d = (C.c_int * self.n)(*[int(v) for v in depths])
+        dev = (C.c_int * self.n)(*[int(v) for v in devices]) if devices is not None else None
+        self._h = (C.c_void_p * self.n)()
+        check(load().lbm_split_z(whole._h, self.n, d, dev, self._h), "lbm_split_z")
+        self.depths = list(depths)
+
+    def step(self, nsteps: int, grav: float = 0.0) -> None:
+        check(load().lbm_slab_step(self._h, self.n, int(nsteps), float(grav)), "lbm_slab_step")
+
+    def stats(self) -> dict:
+        s = StatsOut()
+        check(load().lbm_slab_stats(self._h, self.n, C.byref(s)), "lbm_slab_stats")
+        return s.as_dict()
+
+    def raw_stats(self) -> np.ndarray:
+        """lbm_stats_raw of every slab (after an LBM_HALO_PHI exchange by stats())."""
+        out = np.zeros((self.n, 16), np.float64)
+        for k in range(self.n):
+            check(load().lbm_stats_raw(self._h[k], out[k].ctypes.data_as(C.POINTER(C.c_double))), "lbm_stats_raw")
+        return out
+
+    def merge_into(self, whole: Lattice) -> None:
+        check(load().lbm_merge_z(self._h, self.n, whole._h), "lbm_merge_z")
+
+    def handle(self, k: int):
+        return self._h[k]
+
+    def close(self) -> None:
+        if self._h is not None:
+            for k in range(self.n):
+                if self._h[k]:
+                    load().lbm_destroy(self._h[k])
             self._h = None
 
     def __enter__(self):

@@ -469,6 +469,7 @@ int check_opts(lbm_ctx *c, const lbm_adjoint_opts *o, const void *out, const cha
     if (o->objective == LBM_OBJ_LIGHT_UZ_MEAN && (o->window < 1 || o->window > o->nsteps))
         return fail(LBM_EINVAL, f + ": window must be in [1, nsteps]");
     if (!std::isfinite(o->grav)) return fail(LBM_EINVAL, f + ": grav is not finite");
+    if (c->box.zghost) return fail(LBM_EINVAL, f + ": not available on a z-slab context");
     if (c->st.steps != 0)
         return fail(LBM_ESTATE, f + ": the context must hold its initial state (no step taken)");
     return LBM_OK;

@@ -50,12 +50,28 @@ void identity_quant(lbm::Quant &q)
 }
 
 // Allocate a context and its buffers; the state is left uninitialised.
-int create(lbm_ctx **out, const lbm_params *p)
+int create(lbm_ctx **out, const lbm_params *p) { return lbm::create_context(out, p, 0); }
+
+lbm::StepView view(lbm_ctx *c, int in) { return lbm::state_view(c, in); }
+
+}  // namespace
+
+namespace lbm {
+// Allocate a context and its buffers; the state is left uninitialised.  With
+// zghost the context is a z-slab: its f fields carry two ghost planes below
+// and above, its g fields one (p->nz >= 2 interior planes).
+int create_context(lbm_ctx **out, const lbm_params *p, int zghost)
 {
     if (!out) return fail(LBM_EINVAL, "out is NULL");
     *out = nullptr;
-    int rc = validate(p);
-    if (rc) return rc;
+    if (zghost) {
+        if (!p || p->nz < 2) return fail(LBM_EINVAL, "a z-slab needs at least 2 planes");
+        lbm_params q = *p;
+        q.nz = 3;   // the checks of a whole box, apart from its depth
+        if (int rc = validate(&q)) return rc;
+    } else if (int rc = validate(p)) {
+        return rc;
+    }
     lbm_ctx *c = new (std::nothrow) lbm_ctx();
     if (!c) return fail(LBM_ENOMEM, "host allocation");
     c->p = *p;
@@ -71,11 +87,14 @@ int create(lbm_ctx **out, const lbm_params *p)
     c->box.nz = p->nz;
     c->box.nxy = (long long)p->nx * p->ny;
     c->box.n = c->box.nxy * p->nz;
-    const size_t n = (size_t)c->box.n;
+    c->box.zghost = zghost ? 1 : 0;
+    c->box.nf = c->box.nxy * (p->nz + (zghost ? 4 : 0));
+    c->box.ng = c->box.nxy * (p->nz + (zghost ? 2 : 0));
+    const size_t n = (size_t)c->box.n, nf = (size_t)c->box.nf, ng = (size_t)c->box.ng;
     cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaMalloc(&c->st.f0, sizeof(float) * 2 * n);
-    if (e == cudaSuccess) e = cudaMalloc(&c->st.fq, c->esz * 2 * (lbm::kQf - 1) * n);
-    if (e == cudaSuccess) e = cudaMalloc(&c->st.g, c->esz * lbm::kQg * n);
+    if (e == cudaSuccess) e = cudaMalloc(&c->st.f0, sizeof(float) * 2 * nf);
+    if (e == cudaSuccess) e = cudaMalloc(&c->st.fq, c->esz * 2 * (lbm::kQf - 1) * nf);
+    if (e == cudaSuccess) e = cudaMalloc(&c->st.g, c->esz * lbm::kQg * ng);
     if (e == cudaSuccess) e = cudaMalloc(&c->st.mom, sizeof(float) * 5 * n);
     c->partial_count = lbm::stats_partial_count(c->box);
     if (e == cudaSuccess) e = cudaMalloc(&c->partials, sizeof(double) * lbm::kStatsValues * c->partial_count);
@@ -90,8 +109,9 @@ int create(lbm_ctx **out, const lbm_params *p)
     *out = c;
     return LBM_OK;
 }
+}  // namespace lbm
 
-lbm::StepView view(lbm_ctx *c, int in) { return lbm::state_view(c, in); }
+namespace {
 
 // Stats reduction of the mom arrays into c->result_host (synchronises).
 int reduce_stats(lbm_ctx *c)
@@ -206,6 +226,9 @@ int init_from_mom(lbm_ctx *c, const float *ghost_lo, const float *ghost_hi)
     return rc;
 }
 
+}  // namespace
+
+namespace lbm {
 // The step kernel's error flag (it stays set): bit 1 a bounded wait gave up
 // (LBM_ETIMEOUT), bit 2 a shared-memory stage was misaligned, bit 4 a checked
 // build found a global index outside its field (LBM_ECUDA).
@@ -219,10 +242,14 @@ int device_error(lbm_ctx *c)
     return LBM_OK;
 }
 
-// lbm_stats_out from the 16 raw stats values (the reference's formulas of
-// src/stats.c:60-91 and src/logsave.c:152-167, in FP64).
-int fill_stats(const lbm_ctx *c, const double *r, lbm_stats_out *s);
+}  // namespace lbm
 
+namespace {
+using lbm::device_error;
+int fill_stats(const lbm_ctx *c, const double *r, lbm_stats_out *s)
+{
+    return lbm::fill_stats_raw((double)c->box.n, c->p, c->st.steps, r, s);
+}
 }  // namespace
 
 namespace lbm {
@@ -322,6 +349,7 @@ extern "C" int lbm_step(lbm_ctx *c, int nsteps, float grav)
     if (!c) return fail(LBM_EINVAL, "context is NULL");
     if (nsteps < 0) return fail(LBM_EINVAL, "nsteps < 0");
     if (!std::isfinite(grav)) return fail(LBM_EINVAL, "grav is not finite");
+    if (c->box.zghost) return fail(LBM_EINVAL, "lbm_step: a z-slab steps with lbm_slab_step / lbm_slab_step_local");
     LBM_ON_DEVICE(c->p.device);
     const lbm::StepConst k = lbm::step_const(c->d, c->p, grav);
     for (int s = 0; s < nsteps; s++) {
@@ -341,6 +369,7 @@ extern "C" int lbm_stats(lbm_ctx *c, lbm_stats_out *s, float *phi, float *rho, f
 {
     const lbm::Range nvtx_range("lbm_stats");
     if (!c) return fail(LBM_EINVAL, "context is NULL");
+    if (s && c->box.zghost) return fail(LBM_EINVAL, "lbm_stats: the statistics of z-slabs come from lbm_slab_stats");
     LBM_ON_DEVICE(c->p.device);
     const size_t n = (size_t)c->box.n, bytes = sizeof(float) * n;
     if (s) {
@@ -367,6 +396,7 @@ extern "C" int lbm_stats_fields(lbm_ctx *c, lbm_stats_out *s, const float *phi, 
 {
     if (!c || !s) return fail(LBM_EINVAL, "lbm_stats_fields: NULL context or output");
     if (!phi || !rho || !ux || !uy || !uz) return fail(LBM_EINVAL, "lbm_stats_fields: every field is required");
+    if (c->box.zghost) return fail(LBM_EINVAL, "lbm_stats_fields: not available on a z-slab context");
     LBM_ON_DEVICE(c->p.device);
     const size_t n = (size_t)c->box.n, bytes = sizeof(float) * n;
     float *tmp = nullptr;
@@ -389,6 +419,7 @@ extern "C" int lbm_stats_fields(lbm_ctx *c, lbm_stats_out *s, const float *phi, 
 extern "C" int lbm_pressure(lbm_ctx *c, float *p)
 {
     if (!c || !p) return fail(LBM_EINVAL, "lbm_pressure: NULL argument");
+    if (c->box.zghost) return fail(LBM_EINVAL, "lbm_pressure: not available on a z-slab context");
     LBM_ON_DEVICE(c->p.device);
     const size_t n = (size_t)c->box.n;
     float *tmp = nullptr;
@@ -412,22 +443,24 @@ extern "C" int lbm_device_name(int device, char *name, int len, double *total_by
     return LBM_OK;
 }
 
-namespace {
-int fill_stats(const lbm_ctx *c, const double *r, lbm_stats_out *s)
+namespace lbm {
+// lbm_stats_out from the 16 raw stats values of a box of n nodes (the
+// reference's formulas of src/stats.c:60-91 and src/logsave.c:152-167, in FP64).
+int fill_stats_raw(double n, const lbm_params &p, long long steps, const double *r, lbm_stats_out *s)
 {
     std::memset(s, 0, sizeof(*s));
-    s->step = c->st.steps;
+    s->step = steps;
     s->umax = std::sqrt(r[0]);
     s->vol = r[1];
     s->ux_av = r[1] > 0 ? r[2] / r[1] : 0.0;
     s->uy_av = r[1] > 0 ? r[3] / r[1] : 0.0;
     s->uz_av = r[1] > 0 ? r[4] / r[1] : 0.0;
     s->ref = std::pow(r[1] * 0.75 / M_PI, 1.0 / 3.0);
-    const double vol_out = (double)c->box.n - r[1];
+    const double vol_out = n - r[1];
     s->p_in = r[1] > 0 ? r[5] / r[1] : 0.0;
     s->p_out = vol_out > 0 ? r[6] / vol_out : 0.0;
     s->p_dif = s->p_in - s->p_out;
-    s->p_err = c->p.rc0 > 0.f ? 0.5 * (2.0 * c->p.sigma / c->p.rc0 - s->p_dif) * c->p.rc0 / c->p.sigma : 0.0;
+    s->p_err = p.rc0 > 0.f ? 0.5 * (2.0 * p.sigma / p.rc0 - s->p_dif) * p.rc0 / p.sigma : 0.0;
     s->phi_sum = r[7];
     s->rho_sum = r[8];
     s->mom_x = r[9];
@@ -439,13 +472,14 @@ int fill_stats(const lbm_ctx *c, const double *r, lbm_stats_out *s)
     if (s->nonfinite > 0) return fail(LBM_ENAN, std::to_string(s->nonfinite) + " non-finite nodes");
     return LBM_OK;
 }
-}  // namespace
+}  // namespace lbm
 
 extern "C" int lbm_get_dist(lbm_ctx *c, float *f, float *g)
 {
     const lbm::Range nvtx_range("lbm_get_dist");
     if (!c) return fail(LBM_EINVAL, "context is NULL");
     if (!f && !g) return LBM_OK;
+    if (c->box.zghost) return fail(LBM_EINVAL, "lbm_get_dist: not available on a z-slab context");
     LBM_ON_DEVICE(c->p.device);
     const size_t n = (size_t)c->box.n;
     float *tmp = nullptr;
@@ -469,6 +503,7 @@ extern "C" int lbm_set_dist(lbm_ctx *c, const float *f, const float *g)
 {
     const lbm::Range nvtx_range("lbm_set_dist");
     if (!c || !f || !g) return fail(LBM_EINVAL, "NULL argument");
+    if (c->box.zghost) return fail(LBM_EINVAL, "lbm_set_dist: not available on a z-slab context");
     LBM_ON_DEVICE(c->p.device);
     const size_t n = (size_t)c->box.n;
     LBM_CUDA(cudaStreamSynchronize(c->stream), "lbm_set_dist");
@@ -515,6 +550,7 @@ extern "C" int lbm_save_state(lbm_ctx *c, void *buf)
 {
     const lbm::Range nvtx_range("lbm_save_state");
     if (!c || !buf) return fail(LBM_EINVAL, "lbm_save_state: NULL argument");
+    if (c->box.zghost) return fail(LBM_EINVAL, "lbm_save_state: not available on a z-slab context");
     LBM_ON_DEVICE(c->p.device);
     SnapshotHeader h;
     std::memset(&h, 0, sizeof(h));
@@ -546,6 +582,7 @@ extern "C" int lbm_load_state(lbm_ctx *c, const void *buf)
 {
     const lbm::Range nvtx_range("lbm_load_state");
     if (!c || !buf) return fail(LBM_EINVAL, "lbm_load_state: NULL argument");
+    if (c->box.zghost) return fail(LBM_EINVAL, "lbm_load_state: not available on a z-slab context");
     SnapshotHeader h;
     std::memcpy(&h, buf, sizeof(h));
     if (std::memcmp(h.magic, kSnapMagic, sizeof(h.magic)) != 0 || h.version != 1)
@@ -613,6 +650,10 @@ extern "C" void lbm_destroy(lbm_ctx *c)
     cudaFree(c->err);
     cudaFree(c->adj_work);
     cudaFree(c->adj_slots);
+    cudaFree(c->halo_send);
+    cudaFree(c->phi_ghost);
+    if (c->ev_pack) cudaEventDestroy(c->ev_pack);
+    if (c->ev_unpack) cudaEventDestroy(c->ev_unpack);
     if (c->result_host) cudaFreeHost(c->result_host);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;

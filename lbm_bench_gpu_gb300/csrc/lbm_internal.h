@@ -28,10 +28,16 @@ struct StepConst {
     float grav;                               // body force on phi > 0 nodes
 };
 
-// Box of interior nodes, periodic in x, y, z.
+// Box of interior nodes, periodic in x and y.  In z it is periodic too, or a
+// z-slab of a larger box (zghost = 1): then the state's fields carry ghost
+// planes the neighbouring slabs fill, two below and two above the slab for
+// f_0..f_6 (nz + 4 planes, field length nf) and one below and one above for
+// g (nz + 2 planes, field length ng); the moment fields hold the nz planes.
 struct Box {
     int nx, ny, nz;
     long long nxy, n;
+    int zghost = 0;
+    long long nf = 0, ng = 0;   // elements per f / g field (n when periodic)
 };
 
 // Affine map of the 16-bit storage formats, one power-of-two scale per set:
@@ -136,8 +142,10 @@ cudaError_t launch_quantize(const Box &b, const Quant &q, int storage, const flo
 cudaError_t launch_field_maxabs(const Box &b, const float *f, const float *g, const float *g_shift_dev,
                                 unsigned *out_bits, cudaStream_t s);
 cudaError_t launch_moments(const Box &b, const float *f, const float *g, float *mom, cudaStream_t s);
+// phi_lo / phi_hi: the phi planes below and above a z-slab (NULL: periodic z).
 cudaError_t launch_stats(const Box &b, const lbm_derived &d, const float *mom, double *partials,
-                         size_t partial_count, double *result, unsigned long long *counters, cudaStream_t s);
+                         size_t partial_count, double *result, unsigned long long *counters, cudaStream_t s,
+                         const float *phi_lo = nullptr, const float *phi_hi = nullptr);
 size_t stats_partial_count(const Box &b);
 // Pressure field (n floats) of the mom arrays (src/vtksave.c:63-127).
 cudaError_t launch_pressure(const Box &b, const lbm_derived &d, const float *mom, float *out, cudaStream_t s);
@@ -189,21 +197,33 @@ struct lbm_ctx {
     size_t adj_work_bytes = 0;
     void *adj_slots = nullptr;
     size_t adj_slot_bytes = 0;
+    // z-slab contexts (lbm_split_z): planes [z0, z0 + nz) of a box of
+    // nz_total planes, the device buffers the halo exchange packs into (one
+    // per side, halo_bytes each), the phi planes around the slab for the
+    // statistics, events that order the exchange across the slabs' streams,
+    // and whether the last step was odd (its ghost-plane g writes still have
+    // to reach the neighbours)
+    int z0 = 0, nz_total = 0;
+    void *halo_send = nullptr;
+    size_t halo_bytes = 0;
+    float *phi_ghost = nullptr;
+    cudaEvent_t ev_pack = nullptr, ev_unpack = nullptr;
+    bool post_pending = false;
 };
 
 namespace lbm {
 // The buffers of a step that reads half `in` of f.
 inline StepView state_view(lbm_ctx *c, int in)
 {
-    const size_t n = (size_t)c->box.n;
     const int out = 1 - in;
     unsigned char *fq = static_cast<unsigned char *>(c->st.fq);
     StepView v;
     v.storage = c->p.storage;
-    v.f0_in = c->st.f0 + (size_t)in * n;
-    v.f0_out = c->st.f0 + (size_t)out * n;
-    v.fq_in = fq + (size_t)in * (kQf - 1) * n * c->esz;
-    v.fq_out = fq + (size_t)out * (kQf - 1) * n * c->esz;
+    const size_t nf = (size_t)c->box.nf;
+    v.f0_in = c->st.f0 + (size_t)in * nf;
+    v.f0_out = c->st.f0 + (size_t)out * nf;
+    v.fq_in = fq + (size_t)in * (kQf - 1) * nf * c->esz;
+    v.fq_out = fq + (size_t)out * (kQf - 1) * nf * c->esz;
     v.g = c->st.g;
     v.g_in = nullptr;
     v.mom = c->st.mom;
@@ -212,6 +232,12 @@ inline StepView state_view(lbm_ctx *c, int in)
 }
 int fail(int code, const std::string &msg);
 int cuda_fail(cudaError_t e, const char *what);
+// Allocate a context (zghost: a z-slab with ghost planes, lbm_split_z).
+int create_context(lbm_ctx **out, const lbm_params *p, int zghost);
+// The kernels' error flag as a status (LBM_ETIMEOUT, LBM_ECUDA) after a sync.
+int device_error(lbm_ctx *c);
+// lbm_stats_out from the raw statistics of a box of n nodes.
+int fill_stats_raw(double n, const lbm_params &p, long long steps, const double *raw, lbm_stats_out *s);
 
 // Makes `device` current for the length of a C-ABI call and gives the caller
 // its own current device back afterwards.  Every entry point that queues or

@@ -92,10 +92,14 @@ struct Sum2 {
 // One block works on whole x-rows (row r = y + ny z, grid-stride over rows);
 // |u|^2 and the pressure are evaluated in float as the reference does
 // (src/stats.c:45, src/logsave.c:94-137); sums are compensated, counts exact.
+// phi_lo / phi_hi: the phi planes just below and above a z-slab (NULL for a
+// periodic box, whose z neighbours wrap).
 __global__ void __launch_bounds__(kThreads) stats_kernel(Box b, StatsConst c, const float *__restrict__ phi,
                                                          const float *__restrict__ rho, const float *__restrict__ ux,
                                                          const float *__restrict__ uy, const float *__restrict__ uz,
-                                                         double *__restrict__ partials)
+                                                         double *__restrict__ partials,
+                                                         const float *__restrict__ phi_lo = nullptr,
+                                                         const float *__restrict__ phi_hi = nullptr)
 {
     Sum2 sum[kStatsValues];
     unsigned cnt_in = 0, cnt_all = 0, cnt_bad = 0;
@@ -110,9 +114,12 @@ __global__ void __launch_bounds__(kThreads) stats_kernel(Box b, StatsConst c, co
         const int kt = k == nz - 1 ? 0 : k + 1, kb = k == 0 ? nz - 1 : k - 1;
         const size_t row_c = (size_t)r * nx;
         const size_t row_n = ((size_t)kk_row(jn, k, ny)) * nx, row_s = ((size_t)kk_row(js, k, ny)) * nx;
-        const size_t row_t = ((size_t)kk_row(j, kt, ny)) * nx, row_b = ((size_t)kk_row(j, kb, ny)) * nx;
-        const size_t row_nt = ((size_t)kk_row(jn, kt, ny)) * nx, row_sb = ((size_t)kk_row(js, kb, ny)) * nx;
-        const size_t row_nb = ((size_t)kk_row(jn, kb, ny)) * nx, row_st = ((size_t)kk_row(js, kt, ny)) * nx;
+        // the planes above and below: the neighbouring slab's at a slab's edge
+        const float *pt = (k == nz - 1 && phi_hi) ? phi_hi : phi + (size_t)kt * b.nxy;
+        const float *pb = (k == 0 && phi_lo) ? phi_lo : phi + (size_t)kb * b.nxy;
+        const float *rt = pt + (size_t)j * nx, *rb = pb + (size_t)j * nx;
+        const float *rnt = pt + (size_t)jn * nx, *rsb = pb + (size_t)js * nx;
+        const float *rnb = pb + (size_t)jn * nx, *rst = pt + (size_t)js * nx;
         for (int i = threadIdx.x; i < nx; i += blockDim.x) {
             const size_t t = row_c + i;
             const float ph = phi[t], rh = rho[t], vx = ux[t], vy = uy[t], vz = uz[t];
@@ -133,10 +140,10 @@ __global__ void __launch_bounds__(kThreads) stats_kernel(Box b, StatsConst c, co
 
             const int ie = i == nx - 1 ? 0 : i + 1, iw = i == 0 ? nx - 1 : i - 1;
             const float p01 = phi[row_c + ie], p02 = phi[row_c + iw], p03 = phi[row_n + i], p04 = phi[row_s + i];
-            const float p05 = phi[row_t + i], p06 = phi[row_b + i], p07 = phi[row_n + ie], p08 = phi[row_s + iw];
-            const float p09 = phi[row_s + ie], p10 = phi[row_n + iw], p11 = phi[row_t + ie], p12 = phi[row_b + iw];
-            const float p13 = phi[row_b + ie], p14 = phi[row_t + iw], p15 = phi[row_nt + i], p16 = phi[row_sb + i];
-            const float p17 = phi[row_nb + i], p18 = phi[row_st + i];
+            const float p05 = rt[i], p06 = rb[i], p07 = phi[row_n + ie], p08 = phi[row_s + iw];
+            const float p09 = phi[row_s + ie], p10 = phi[row_n + iw], p11 = rt[ie], p12 = rb[iw];
+            const float p13 = rb[ie], p14 = rt[iw], p15 = rnt[i], p16 = rsb[i];
+            const float p17 = rnb[i], p18 = rst[i];
             const float lap = (p07 + p08 + p09 + p10 + p11 + p12 + p13 + p14 + p15 + p16 + p17 + p18
                                + 2.f * (p01 + p02 + p03 + p04 + p05 + p06 - 12.f * ph)) * kInv6;
             const float gx = (2.f * (p01 - p02) + p07 - p08 + p09 - p10 + p11 - p12 + p13 - p14) * kInv12;
@@ -233,13 +240,14 @@ unsigned stats_blocks(const Box &b)
 size_t stats_partial_count(const Box &b) { return stats_blocks(b); }
 
 cudaError_t launch_stats(const Box &b, const lbm_derived &d, const float *mom, double *partials,
-                         size_t partial_count, double *result, unsigned long long *, cudaStream_t s)
+                         size_t partial_count, double *result, unsigned long long *, cudaStream_t s,
+                         const float *phi_lo, const float *phi_hi)
 {
     const unsigned blocks = stats_blocks(b);
     if (partial_count < blocks) return cudaErrorInvalidValue;
     StatsConst c{d.alpha, d.kappa, d.phiStarSq};
     stats_kernel<<<blocks, kThreads, 0, s>>>(b, c, mom, mom + b.n, mom + 2 * b.n, mom + 3 * b.n, mom + 4 * b.n,
-                                             partials);
+                                             partials, phi_lo, phi_hi);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     fold_kernel<<<1, kThreads, 0, s>>>(partials, (int)blocks, result);

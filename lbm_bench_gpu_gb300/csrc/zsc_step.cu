@@ -385,6 +385,13 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
     const int x0 = bx * TX, y0 = by * TY;
     const int x = x0 + XPT * tx, y = y0 + ty;   // (first) node of the thread
 
+    // memory plane of P_f plane p and of g plane p: periodic wrap, or in a
+    // z-slab the ghost-extended fields (two planes below the slab for f, one
+    // for g; the moment fields have none)
+    const bool zg = b.zghost != 0;
+    auto zf = [&](int p) { return zg ? p + 2 : wrap(p, b.nz); };
+    auto zgm = [&](int p) { return zg ? p + 1 : wrap(p, b.nz); };
+
     uint64_t *const mbar = reinterpret_cast<uint64_t *>(smem + Gm::MBAR_OFF);
     constexpr bool g_tma = TMA && !ODD;   // the even step's g tile: one TMA copy per plane
     // P_f planes by TMA: the staged rows y0 - 2 .. y0 + TY + 1 and columns
@@ -479,7 +486,7 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
         if (tile_tma_f) {
             if (tid == 32) {   // lane 0 of warp 1 (warp 0 issues the g copies)
                 unsigned char *st = fstage(p);
-                const int zp = wrap(p, b.nz);
+                const int zp = zf(p);
                 fence_proxy_async();
                 mbar_expect_tx(fbar(p), (unsigned)Gm::F_STAGE);
                 tma_load_3d(f0part(st), &f0map, x0 - 4, y0 - 2, zp, fbar(p));
@@ -487,16 +494,16 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
             }
             return;
         }
-        const unsigned zb = (unsigned)wrap(p, b.nz) * (unsigned)b.nxy;
+        const unsigned zb = (unsigned)zf(p) * (unsigned)b.nxy;
         unsigned char *st = fstage(p);
-        if (f0_issuer && in_field((long long)zb + f0_xy, 4, b.n, P.err))
+        if (f0_issuer && in_field((long long)zb + f0_xy, 4, b.nf, P.err))
             cp_async16(f0part(st) + f0_dst, P.f0in + (zb + (unsigned)f0_xy));
         if (fq_issuer) {
             ST *dst = fqpart(st) + fq_dst;
             const unsigned base = zb + (unsigned)fq_xy;
 #pragma unroll
             for (int a = 0; a < kQf - 1; a++)
-                if (in_field(base, E, b.n, P.err)) cp_async16(dst + a * FR * W, P.fin[a] + base);
+                if (in_field(base, E, b.nf, P.err)) cp_async16(dst + a * FR * W, P.fin[a] + base);
         }
     };
 
@@ -523,22 +530,22 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
             if (tid == 0) {
                 fence_proxy_async();
                 mbar_expect_tx(&mbar[s], (unsigned)Gm::G_TMA_BYTES);
-                tma_load_4d(G + s * G_ELEMS, &gmap, x0, y0, z, 0, &mbar[s]);
+                tma_load_4d(G + s * G_ELEMS, &gmap, x0, y0, zgm(z), 0, &mbar[s]);
             }
             return;
         }
         if (!g_issuer) return;
         ST *dst = G + s * G_ELEMS + g_r * GW;
         if (!ODD) {
-            const unsigned base = (unsigned)z * (unsigned)b.nxy + (unsigned)(g_row_0 + g_x_hi);
+            const unsigned base = (unsigned)zgm(z) * (unsigned)b.nxy + (unsigned)(g_row_0 + g_x_hi);
             for_my_dirs([&](auto d) {
                 constexpr int i = decltype(d)::value;
-                if (in_field(base, E, b.n, P.err)) cp_async16(dst + i * TY * GW + E + E * g_k, P.gin[i] + base);
+                if (in_field(base, E, b.ng, P.err)) cp_async16(dst + i * TY * GW + E + E * g_k, P.gin[i] + base);
             });
         } else {
-            const unsigned zb0 = (unsigned)z * (unsigned)b.nxy;
-            const unsigned zbp = (unsigned)wrap(z - 1, b.nz) * (unsigned)b.nxy;   // c_z = +1 reads z - 1
-            const unsigned zbm = (unsigned)wrap(z + 1, b.nz) * (unsigned)b.nxy;   // c_z = -1 reads z + 1
+            const unsigned zb0 = (unsigned)zgm(z) * (unsigned)b.nxy;
+            const unsigned zbp = (unsigned)zgm(z - 1) * (unsigned)b.nxy;   // c_z = +1 reads z - 1
+            const unsigned zbm = (unsigned)zgm(z + 1) * (unsigned)b.nxy;   // c_z = -1 reads z + 1
             for_my_dirs([&](auto d) {
                 constexpr int i = decltype(d)::value;
                 constexpr int cx = kCx(i), cy = kCy(i), cz = kCz(i);
@@ -549,13 +556,13 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
                 const long long r0 = (long long)zb + row;   // row start in the field
                 if (cx > 0) {
                     // columns 0 .. TX + E - 1 hold x0 - E .. x0 + TX - 1
-                    if (in_field(r0 + g_x_lo, E, b.n, P.err)) cp_async16(d_row + E * g_k, src + g_x_lo);
-                    if (g_k == 0 && in_field(r0 + x0 + TX - E, E, b.n, P.err))
+                    if (in_field(r0 + g_x_lo, E, b.ng, P.err)) cp_async16(d_row + E * g_k, src + g_x_lo);
+                    if (g_k == 0 && in_field(r0 + x0 + TX - E, E, b.ng, P.err))
                         cp_async16(d_row + TX, src + (x0 + TX - E));
                 } else {
                     // columns GX0 .. hold x0 .. x0 + TX (+ E for cx < 0)
-                    if (in_field(r0 + g_x_hi, E, b.n, P.err)) cp_async16(d_row + GX0 + E * g_k, src + g_x_hi);
-                    if (cx < 0 && g_k == 0 && in_field(r0 + g_x_wrap, E, b.n, P.err))
+                    if (in_field(r0 + g_x_hi, E, b.ng, P.err)) cp_async16(d_row + GX0 + E * g_k, src + g_x_hi);
+                    if (cx < 0 && g_k == 0 && in_field(r0 + g_x_wrap, E, b.ng, P.err))
                         cp_async16(d_row + TX + GX0, src + g_x_wrap);
                 }
             });
@@ -807,7 +814,8 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
         const float ux = ((g[1] - g[2]) + d7 + d9 + d11 + d13) * invRhoG;
         const float uy = ((g[3] - g[4]) + d7 - d9 + d15 + d17) * invRhoG;
         const float uz = ((g[5] - g[6]) + d11 - d13 + d15 - d17) * invRhoG;
-        const unsigned id = node_index(b, x, y, z);
+        const unsigned id = node_index(b, x, y, z);   // moment fields
+        const unsigned idf = id + (zg ? 2u * (unsigned)b.nxy : 0u), idg = id + (zg ? (unsigned)b.nxy : 0u);
         if (write_moments && in_field(id, 1, b.n, P.err)) {
             P.mom[0][id] = pc;
             P.mom[1][id] = rho;
@@ -825,12 +833,12 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
         {
             const float Af = 0.5f * c.Gamma * c.invTauPhi * mu;
             const float a = c.invTauPhiOne;
-            if (in_field(id, 1, b.n, P.err)) P.f0out[id] = a * fcur[0][0] - 6.0f * Af + c.invTauPhi * pc;
+            if (in_field(idf, 1, b.nf, P.err)) P.f0out[idf] = a * fcur[0][0] - 6.0f * Af + c.invTauPhi * pc;
             // f_1..f_6 in stored units: terms scaled by f_scale
             const float Afk = Fm::kMapped ? m.Af * mu : Af;
             const float Cf = (Fm::kMapped ? m.Cf : c.invTauPhi * c.invEta2) * pc;
             auto put = [&](int k, float v) {
-                if (in_field(id, 1, b.n, P.err)) P.fout[k][id] = Fm::store(v);
+                if (in_field(idf, 1, b.nf, P.err)) P.fout[k][idf] = Fm::store(v);
             };
             put(0, a * fcur[0][1] + Afk + Cf * usx);
             put(1, a * fcur[0][2] + Afk - Cf * usx);
@@ -942,18 +950,19 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
                 // even: own node, reversed slots
 #pragma unroll
                 for (int i = 0; i < kQg; i++)
-                    if (in_field(id, 1, b.n, P.err)) P.g[kOpp(i)][id] = enc(i, qv[i]);
+                    if (in_field(idg, 1, b.ng, P.err)) P.g[kOpp(i)][idg] = enc(i, qv[i]);
             } else {
-                // odd: downstream neighbour x + c_i, natural slot i
-                const int o_zm = (z == 0) ? (b.nz - 1) * (int)b.nxy : -(int)b.nxy;
-                const int o_zp = (z == b.nz - 1) ? -(b.nz - 1) * (int)b.nxy : (int)b.nxy;
+                // odd: downstream neighbour x + c_i, natural slot i (in a
+                // z-slab the planes just outside it are ghost planes)
+                const int o_zm = (z == 0 && !zg) ? (b.nz - 1) * (int)b.nxy : -(int)b.nxy;
+                const int o_zp = (z == b.nz - 1 && !zg) ? -(b.nz - 1) * (int)b.nxy : (int)b.nxy;
                 auto off = [&](int i) {
                     return (kCx(i) > 0 ? o_xp : kCx(i) < 0 ? o_xm : 0) + (kCy(i) > 0 ? o_yp : kCy(i) < 0 ? o_ym : 0)
                            + (kCz(i) > 0 ? o_zp : kCz(i) < 0 ? o_zm : 0);
                 };
 #pragma unroll
                 for (int i = 0; i < kQg; i++)
-                    if (in_field((long long)id + off(i), 1, b.n, P.err)) P.g[i][id + off(i)] = enc(i, qv[i]);
+                    if (in_field((long long)idg + off(i), 1, b.ng, P.err)) P.g[i][idg + off(i)] = enc(i, qv[i]);
             }
         }
 
@@ -1033,6 +1042,7 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
             const float2 uz = mul(sub(add(sub(add(sub(g[5], g[6]), d11), d13), d15), d17), invRhoG);
             // element index of the word (its A half) in every pair-layout field
             const unsigned id = node_index(b, x, y, z);
+            const unsigned idf = id + (zg ? 2u * (unsigned)b.nxy : 0u), idg = id + (zg ? (unsigned)b.nxy : 0u);
             const int half = b.nx / 2;
             if (write_moments) {
                 // the moment fields are in the natural layout: A and B apart
@@ -1052,13 +1062,13 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
                 const float2 a2 = splat(c.invTauPhiOne);
                 auto fc = [&](int k) { return fcur2[k]; };
                 const float2 Af = mul(splat(0.5f * c.Gamma * c.invTauPhi), mu);
-                if (in_field(id, 2, b.n, P.err))
-                    *reinterpret_cast<float2 *>(P.f0out + id) =
+                if (in_field(idf, 2, b.nf, P.err))
+                    *reinterpret_cast<float2 *>(P.f0out + idf) =
                         fma(a2, fc(0), fma(splat(-6.f), Af, mul(splat(c.invTauPhi), pc)));
                 const float2 Afk = mul(splat(m.Af), mu), Cf = mul(splat(m.Cf), pc);
                 const float2 cux = mul(Cf, usx), cuy = mul(Cf, usy), cuz = mul(Cf, usz);
                 auto put2 = [&](int k, float2 v) {
-                    if (in_field(id, 2, b.n, P.err)) *reinterpret_cast<T2 *>(P.fout[k] + id) = Fm::store2(v);
+                    if (in_field(idf, 2, b.nf, P.err)) *reinterpret_cast<T2 *>(P.fout[k] + idf) = Fm::store2(v);
                 };
                 put2(0, fma(a2, fc(1), add(Afk, cux)));
                 put2(1, fma(a2, fc(2), sub(Afk, cux)));
@@ -1111,14 +1121,15 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
                     // even: own nodes, reversed slots
 #pragma unroll
                     for (int i = 0; i < kQg; i++)
-                        if (in_field(id, 2, b.n, P.err)) *reinterpret_cast<T2 *>(P.g[kOpp(i)] + id) = Fm::store2(qv[i]);
+                        if (in_field(idg, 2, b.ng, P.err))
+                            *reinterpret_cast<T2 *>(P.g[kOpp(i)] + idg) = Fm::store2(qv[i]);
                 } else {
                     // odd: downstream neighbours x + c_i, natural slot i.  Both
                     // nodes of the word move to the neighbouring word together;
                     // past the x seam (word nx/2 - 1 -> 0 and back) the pair
                     // lands swapped.
-                    const int o_zm = (z == 0) ? (b.nz - 1) * (int)b.nxy : -(int)b.nxy;
-                    const int o_zp = (z == b.nz - 1) ? -(b.nz - 1) * (int)b.nxy : (int)b.nxy;
+                    const int o_zm = (z == 0 && !zg) ? (b.nz - 1) * (int)b.nxy : -(int)b.nxy;
+                    const int o_zp = (z == b.nz - 1 && !zg) ? -(b.nz - 1) * (int)b.nxy : (int)b.nxy;
                     const int o_wp = wrap_r ? -2 * (half - 1) : 2;   // element offset of word w + 1
                     const int o_wm = wrap_l ? 2 * (half - 1) : -2;   // ... of word w - 1
 #pragma unroll
@@ -1128,7 +1139,7 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
                                       (kCz(i) > 0 ? o_zp : kCz(i) < 0 ? o_zm : 0);
                         T2 h = Fm::store2(qv[i]);
                         if (kCx(i) != 0) h = Fm::perm2(h, kCx(i) > 0 ? sel_r : sel_l);
-                        if (in_field((long long)id + o, 2, b.n, P.err)) *reinterpret_cast<T2 *>(P.g[i] + id + o) = h;
+                        if (in_field((long long)idg + o, 2, b.ng, P.err)) *reinterpret_cast<T2 *>(P.g[i] + idg + o) = h;
                     }
                 }
             }
@@ -1199,8 +1210,8 @@ bool encode_g_map(const Box &b, const ST *g, CUtensorMap *map)
     const EncodeTiled encode = tensor_map_encoder();
     if (!encode) return false;
     const cuuint64_t es = sizeof(ST);
-    const cuuint64_t dims[4] = {(cuuint64_t)b.nx, (cuuint64_t)b.ny, (cuuint64_t)b.nz, (cuuint64_t)kQg};
-    const cuuint64_t strides[3] = {(cuuint64_t)b.nx * es, (cuuint64_t)b.nxy * es, (cuuint64_t)b.n * es};
+    const cuuint64_t dims[4] = {(cuuint64_t)b.nx, (cuuint64_t)b.ny, (cuuint64_t)(b.ng / b.nxy), (cuuint64_t)kQg};
+    const cuuint64_t strides[3] = {(cuuint64_t)b.nx * es, (cuuint64_t)b.nxy * es, (cuuint64_t)b.ng * es};
     const cuuint32_t box[4] = {(cuuint32_t)TX, (cuuint32_t)TY, 1u, (cuuint32_t)kQg};
     const cuuint32_t elem[4] = {1u, 1u, 1u, 1u};
     if ((reinterpret_cast<uintptr_t>(g) & 15u) != 0) return false;
@@ -1219,7 +1230,7 @@ bool encode_f_maps(const Box &b, const float *f0, const ST *fq, CUtensorMap *f0m
     if (!encode) return false;
     if ((reinterpret_cast<uintptr_t>(f0) & 15u) != 0 || (reinterpret_cast<uintptr_t>(fq) & 15u) != 0) return false;
     const cuuint32_t elem[4] = {1u, 1u, 1u, 1u};
-    const cuuint64_t dims0[3] = {(cuuint64_t)b.nx, (cuuint64_t)b.ny, (cuuint64_t)b.nz};
+    const cuuint64_t dims0[3] = {(cuuint64_t)b.nx, (cuuint64_t)b.ny, (cuuint64_t)(b.nf / b.nxy)};
     const cuuint64_t strides0[2] = {(cuuint64_t)b.nx * 4, (cuuint64_t)b.nxy * 4};
     const cuuint32_t box0[3] = {(cuuint32_t)W0, (cuuint32_t)FR, 1u};
     if (encode(f0map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float *>(f0), dims0, strides0, box0, elem,
@@ -1227,8 +1238,8 @@ bool encode_f_maps(const Box &b, const float *f0, const ST *fq, CUtensorMap *f0m
                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
         return false;
     const cuuint64_t es = sizeof(ST);
-    const cuuint64_t dims[4] = {(cuuint64_t)b.nx, (cuuint64_t)b.ny, (cuuint64_t)b.nz, (cuuint64_t)(kQf - 1)};
-    const cuuint64_t strides[3] = {(cuuint64_t)b.nx * es, (cuuint64_t)b.nxy * es, (cuuint64_t)b.n * es};
+    const cuuint64_t dims[4] = {(cuuint64_t)b.nx, (cuuint64_t)b.ny, (cuuint64_t)(b.nf / b.nxy), (cuuint64_t)(kQf - 1)};
+    const cuuint64_t strides[3] = {(cuuint64_t)b.nx * es, (cuuint64_t)b.nxy * es, (cuuint64_t)b.nf * es};
     const cuuint32_t box[4] = {(cuuint32_t)Geo<ST>::W, (cuuint32_t)FR, 1u, (cuuint32_t)(kQf - 1)};
     return encode(fqmap, tensor_type<ST>(), 4, const_cast<ST *>(fq), dims, strides, box, elem,
                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
@@ -1300,12 +1311,12 @@ cudaError_t launch_typed(const Box &b, const StepConst &c, const Quant &q, const
     ST *g = static_cast<ST *>(v.g);
     const ST *gin = static_cast<const ST *>(v.g_in ? v.g_in : v.g);
     for (int a = 0; a < kQf - 1; a++) {
-        P.fin[a] = fin + (size_t)a * b.n;
-        P.fout[a] = fout + (size_t)a * b.n;
+        P.fin[a] = fin + (size_t)a * b.nf;
+        P.fout[a] = fout + (size_t)a * b.nf;
     }
     for (int i = 0; i < kQg; i++) {
-        P.gin[i] = gin + (size_t)i * b.n;
-        P.g[i] = g + (size_t)i * b.n;
+        P.gin[i] = gin + (size_t)i * b.ng;
+        P.g[i] = g + (size_t)i * b.ng;
     }
     for (int i = 0; i < 5; i++) P.mom[i] = v.mom + (size_t)i * b.n;
     P.err = v.err;

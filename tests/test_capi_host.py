@@ -206,7 +206,8 @@ def test_every_context_entry_point_holds_the_context_device():
     on the sources, since one GPU cannot show a device mix-up."""
     import re
     csrc = Path(__file__).resolve().parents[1] / "lbm_bench_gpu_gb300" / "csrc"
-    no_device_work = {"lbm_state_bytes", "lbm_steps_done", "lbm_stream"}
+    # no device work, or only through other guarded entry points
+    no_device_work = {"lbm_state_bytes", "lbm_steps_done", "lbm_stream", "lbm_halo_bytes", "lbm_slab_stats"}
     seen = set()
     for src in sorted(csrc.glob("*.cu")):
         text = src.read_text()
@@ -224,3 +225,26 @@ def test_every_context_entry_point_holds_the_context_device():
     for name in ("lbm_step", "lbm_stats", "lbm_get_dist", "lbm_set_dist", "lbm_save_state", "lbm_load_state",
                  "lbm_sync", "lbm_destroy", "lbm_step_adjoint", "lbm_objective", "lbm_init", "lbm_init_bubbles"):
         assert name in seen, name
+
+
+def test_stats_combine_adds_sums_and_counts_and_takes_maxima(lib):
+    """lbm_stats_combine (host only): the per-slab raw statistics of a box add
+    up, apart from the two max |u|^2 entries, and the compat means divide by
+    the whole box (Pout by nx*ny*nz - vol, src/logsave.c:158-160)."""
+    import numpy as np
+    from lbm_bench_gpu_gb300 import capi
+    p = capi.make_params(32, 8, 12, rhoL=0.1, rhoH=1.0, tauRho=0.7, tauPhi=1.0, width=4.0, sigma=1e-3, Gamma=1.0,
+                         Eo=-0.4, rc0=5.0)
+    a = np.linspace(1.0, 16.0, 16)
+    b = np.linspace(0.5, 40.0, 16)
+    a[14] = b[14] = 0.0          # no non-finite nodes
+    s = capi.stats_combine(p, 7, np.stack([a, b]))
+    r = a + b
+    r[0], r[13] = max(a[0], b[0]), max(a[13], b[13])
+    n = 32 * 8 * 12
+    assert s["step"] == 7
+    assert s["vol"] == r[1] and s["vol_full"] == r[12]
+    assert s["umax"] == pytest.approx(np.sqrt(r[0])) and s["umax_full"] == pytest.approx(np.sqrt(r[13]))
+    assert s["uz_av"] == pytest.approx(r[4] / r[1])
+    assert s["p_in"] == pytest.approx(r[5] / r[1]) and s["p_out"] == pytest.approx(r[6] / (n - r[1]))
+    assert s["phi_sum"] == r[7] and s["rho_sum"] == r[8] and s["mom_z"] == r[11]
