@@ -174,11 +174,6 @@ struct StepPtrs {
     int *err;                 // set when a bounded wait gives up
 };
 
-__device__ __forceinline__ unsigned node_index(const Box &b, int x, int y, int z)
-{
-    return (unsigned)x + (unsigned)b.nx * ((unsigned)y + (unsigned)b.ny * (unsigned)z);
-}
-
 __device__ __forceinline__ int wrap(int a, int n) { return a < 0 ? a + n : (a >= n ? a - n : a); }
 
 // 16-byte global -> shared copy, cached in L2 only; completes asynchronously.
@@ -354,9 +349,23 @@ StepMap step_map(const StepConst &c, const Quant &q)
 // TMA: on even steps the g tile comes by one tensor copy per plane (gmap) in
 // the dense layout [field][TY][TX]; odd steps stage their shifted rows with
 // cp.async into [dir][TY][W].  Without TMA gmap is unused.
-template <typename ST, bool STREAMED, bool ODD, bool TMA>
+// The box as the step kernel sees it (the field lengths of a z-slab follow
+// from nz and ZG).
+struct StepBox {
+    int nx, ny, nz;
+    long long nxy, n;
+};
+
+__device__ __forceinline__ unsigned node_index(const StepBox &b, int x, int y, int z)
+{
+    return (unsigned)x + (unsigned)b.nx * ((unsigned)y + (unsigned)b.ny * (unsigned)z);
+}
+
+// ZG: the box is a z-slab whose fields carry ghost planes (Box::zghost): a
+// separate instance, so the periodic kernels keep their registers.
+template <typename ST, bool STREAMED, bool ODD, bool TMA, bool ZG>
 __global__ void __launch_bounds__(threads_of<ST>(), Fmt<ST>::kMinBlocks)
-zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const StepMap m, const int tz,
+zsc_step_kernel(const StepPtrs<ST> P, const StepBox b, const StepConst c, const StepMap m, const int tz,
                 const int write_moments, const __grid_constant__ CUtensorMap gmap,
                 const __grid_constant__ CUtensorMap f0map, const __grid_constant__ CUtensorMap fqmap)
 {
@@ -388,9 +397,12 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
     // memory plane of P_f plane p and of g plane p: periodic wrap, or in a
     // z-slab the ghost-extended fields (two planes below the slab for f, one
     // for g; the moment fields have none)
-    const bool zg = b.zghost != 0;
+    constexpr bool zg = ZG;
+    // elements of an f / g field (checked builds test indices against them)
+    const long long nf = b.nxy * (b.nz + (zg ? 4 : 0)), ng = b.nxy * (b.nz + (zg ? 2 : 0));
     auto zf = [&](int p) { return zg ? p + 2 : wrap(p, b.nz); };
     auto zgm = [&](int p) { return zg ? p + 1 : wrap(p, b.nz); };
+    auto zg0 = [&](int p) { return zg ? p + 1 : p; };   // a plane of the box itself
 
     uint64_t *const mbar = reinterpret_cast<uint64_t *>(smem + Gm::MBAR_OFF);
     constexpr bool g_tma = TMA && !ODD;   // the even step's g tile: one TMA copy per plane
@@ -496,14 +508,14 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
         }
         const unsigned zb = (unsigned)zf(p) * (unsigned)b.nxy;
         unsigned char *st = fstage(p);
-        if (f0_issuer && in_field((long long)zb + f0_xy, 4, b.nf, P.err))
+        if (f0_issuer && in_field((long long)zb + f0_xy, 4, nf, P.err))
             cp_async16(f0part(st) + f0_dst, P.f0in + (zb + (unsigned)f0_xy));
         if (fq_issuer) {
             ST *dst = fqpart(st) + fq_dst;
             const unsigned base = zb + (unsigned)fq_xy;
 #pragma unroll
             for (int a = 0; a < kQf - 1; a++)
-                if (in_field(base, E, b.nf, P.err)) cp_async16(dst + a * FR * W, P.fin[a] + base);
+                if (in_field(base, E, nf, P.err)) cp_async16(dst + a * FR * W, P.fin[a] + base);
         }
     };
 
@@ -530,20 +542,20 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
             if (tid == 0) {
                 fence_proxy_async();
                 mbar_expect_tx(&mbar[s], (unsigned)Gm::G_TMA_BYTES);
-                tma_load_4d(G + s * G_ELEMS, &gmap, x0, y0, zgm(z), 0, &mbar[s]);
+                tma_load_4d(G + s * G_ELEMS, &gmap, x0, y0, zg0(z), 0, &mbar[s]);
             }
             return;
         }
         if (!g_issuer) return;
         ST *dst = G + s * G_ELEMS + g_r * GW;
         if (!ODD) {
-            const unsigned base = (unsigned)zgm(z) * (unsigned)b.nxy + (unsigned)(g_row_0 + g_x_hi);
+            const unsigned base = (unsigned)zg0(z) * (unsigned)b.nxy + (unsigned)(g_row_0 + g_x_hi);
             for_my_dirs([&](auto d) {
                 constexpr int i = decltype(d)::value;
-                if (in_field(base, E, b.ng, P.err)) cp_async16(dst + i * TY * GW + E + E * g_k, P.gin[i] + base);
+                if (in_field(base, E, ng, P.err)) cp_async16(dst + i * TY * GW + E + E * g_k, P.gin[i] + base);
             });
         } else {
-            const unsigned zb0 = (unsigned)zgm(z) * (unsigned)b.nxy;
+            const unsigned zb0 = (unsigned)zg0(z) * (unsigned)b.nxy;
             const unsigned zbp = (unsigned)zgm(z - 1) * (unsigned)b.nxy;   // c_z = +1 reads z - 1
             const unsigned zbm = (unsigned)zgm(z + 1) * (unsigned)b.nxy;   // c_z = -1 reads z + 1
             for_my_dirs([&](auto d) {
@@ -556,13 +568,13 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
                 const long long r0 = (long long)zb + row;   // row start in the field
                 if (cx > 0) {
                     // columns 0 .. TX + E - 1 hold x0 - E .. x0 + TX - 1
-                    if (in_field(r0 + g_x_lo, E, b.ng, P.err)) cp_async16(d_row + E * g_k, src + g_x_lo);
-                    if (g_k == 0 && in_field(r0 + x0 + TX - E, E, b.ng, P.err))
+                    if (in_field(r0 + g_x_lo, E, ng, P.err)) cp_async16(d_row + E * g_k, src + g_x_lo);
+                    if (g_k == 0 && in_field(r0 + x0 + TX - E, E, ng, P.err))
                         cp_async16(d_row + TX, src + (x0 + TX - E));
                 } else {
                     // columns GX0 .. hold x0 .. x0 + TX (+ E for cx < 0)
-                    if (in_field(r0 + g_x_hi, E, b.ng, P.err)) cp_async16(d_row + GX0 + E * g_k, src + g_x_hi);
-                    if (cx < 0 && g_k == 0 && in_field(r0 + g_x_wrap, E, b.ng, P.err))
+                    if (in_field(r0 + g_x_hi, E, ng, P.err)) cp_async16(d_row + GX0 + E * g_k, src + g_x_hi);
+                    if (cx < 0 && g_k == 0 && in_field(r0 + g_x_wrap, E, ng, P.err))
                         cp_async16(d_row + TX + GX0, src + g_x_wrap);
                 }
             });
@@ -833,12 +845,12 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
         {
             const float Af = 0.5f * c.Gamma * c.invTauPhi * mu;
             const float a = c.invTauPhiOne;
-            if (in_field(idf, 1, b.nf, P.err)) P.f0out[idf] = a * fcur[0][0] - 6.0f * Af + c.invTauPhi * pc;
+            if (in_field(idf, 1, nf, P.err)) P.f0out[idf] = a * fcur[0][0] - 6.0f * Af + c.invTauPhi * pc;
             // f_1..f_6 in stored units: terms scaled by f_scale
             const float Afk = Fm::kMapped ? m.Af * mu : Af;
             const float Cf = (Fm::kMapped ? m.Cf : c.invTauPhi * c.invEta2) * pc;
             auto put = [&](int k, float v) {
-                if (in_field(idf, 1, b.nf, P.err)) P.fout[k][idf] = Fm::store(v);
+                if (in_field(idf, 1, nf, P.err)) P.fout[k][idf] = Fm::store(v);
             };
             put(0, a * fcur[0][1] + Afk + Cf * usx);
             put(1, a * fcur[0][2] + Afk - Cf * usx);
@@ -950,7 +962,7 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
                 // even: own node, reversed slots
 #pragma unroll
                 for (int i = 0; i < kQg; i++)
-                    if (in_field(idg, 1, b.ng, P.err)) P.g[kOpp(i)][idg] = enc(i, qv[i]);
+                    if (in_field(idg, 1, ng, P.err)) P.g[kOpp(i)][idg] = enc(i, qv[i]);
             } else {
                 // odd: downstream neighbour x + c_i, natural slot i (in a
                 // z-slab the planes just outside it are ghost planes)
@@ -962,7 +974,7 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
                 };
 #pragma unroll
                 for (int i = 0; i < kQg; i++)
-                    if (in_field((long long)idg + off(i), 1, b.ng, P.err)) P.g[i][idg + off(i)] = enc(i, qv[i]);
+                    if (in_field((long long)idg + off(i), 1, ng, P.err)) P.g[i][idg + off(i)] = enc(i, qv[i]);
             }
         }
 
@@ -1062,13 +1074,13 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
                 const float2 a2 = splat(c.invTauPhiOne);
                 auto fc = [&](int k) { return fcur2[k]; };
                 const float2 Af = mul(splat(0.5f * c.Gamma * c.invTauPhi), mu);
-                if (in_field(idf, 2, b.nf, P.err))
+                if (in_field(idf, 2, nf, P.err))
                     *reinterpret_cast<float2 *>(P.f0out + idf) =
                         fma(a2, fc(0), fma(splat(-6.f), Af, mul(splat(c.invTauPhi), pc)));
                 const float2 Afk = mul(splat(m.Af), mu), Cf = mul(splat(m.Cf), pc);
                 const float2 cux = mul(Cf, usx), cuy = mul(Cf, usy), cuz = mul(Cf, usz);
                 auto put2 = [&](int k, float2 v) {
-                    if (in_field(idf, 2, b.nf, P.err)) *reinterpret_cast<T2 *>(P.fout[k] + idf) = Fm::store2(v);
+                    if (in_field(idf, 2, nf, P.err)) *reinterpret_cast<T2 *>(P.fout[k] + idf) = Fm::store2(v);
                 };
                 put2(0, fma(a2, fc(1), add(Afk, cux)));
                 put2(1, fma(a2, fc(2), sub(Afk, cux)));
@@ -1121,7 +1133,7 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
                     // even: own nodes, reversed slots
 #pragma unroll
                     for (int i = 0; i < kQg; i++)
-                        if (in_field(idg, 2, b.ng, P.err))
+                        if (in_field(idg, 2, ng, P.err))
                             *reinterpret_cast<T2 *>(P.g[kOpp(i)] + idg) = Fm::store2(qv[i]);
                 } else {
                     // odd: downstream neighbours x + c_i, natural slot i.  Both
@@ -1139,7 +1151,7 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
                                       (kCz(i) > 0 ? o_zp : kCz(i) < 0 ? o_zm : 0);
                         T2 h = Fm::store2(qv[i]);
                         if (kCx(i) != 0) h = Fm::perm2(h, kCx(i) > 0 ? sel_r : sel_l);
-                        if (in_field((long long)idg + o, 2, b.ng, P.err)) *reinterpret_cast<T2 *>(P.g[i] + idg + o) = h;
+                        if (in_field((long long)idg + o, 2, ng, P.err)) *reinterpret_cast<T2 *>(P.g[i] + idg + o) = h;
                     }
                 }
             }
@@ -1157,17 +1169,17 @@ zsc_step_kernel(const StepPtrs<ST> P, const Box b, const StepConst c, const Step
     }
 }
 
-template <typename ST, bool S, bool O, bool T>
+template <typename ST, bool S, bool O, bool T, bool Z>
 cudaError_t configure()
 {
     static bool done = false;   // per template instance, per process
     if (done) return cudaSuccess;
-    cudaError_t e = cudaFuncSetAttribute(zsc_step_kernel<ST, S, O, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(zsc_step_kernel<ST, S, O, T, Z>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          Geo<ST>::SMEM);
     // all of the unified L1 / shared storage as shared memory: the resident
     // blocks per SM the launch bounds ask for need it
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(zsc_step_kernel<ST, S, O, T>, cudaFuncAttributePreferredSharedMemoryCarveout,
+        e = cudaFuncSetAttribute(zsc_step_kernel<ST, S, O, T, Z>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                  (int)cudaSharedmemCarveoutMaxShared);
     if (e == cudaSuccess) done = true;
     return e;
@@ -1259,7 +1271,7 @@ int choose_tz(const Box &b)
         int dev = 0, sms = 0, per_sm = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, zsc_step_kernel<ST, false, false, false>,
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, zsc_step_kernel<ST, false, false, false, false>,
                                                       threads_of<ST>(), Geo<ST>::SMEM);
         slots = sms * per_sm > 0 ? sms * per_sm : 1;
     }
@@ -1298,7 +1310,7 @@ cudaError_t launch_step_kernel(void (*kernel)(KArgs...), unsigned nblocks, dim3 
     return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
 }
 
-template <typename ST>
+template <typename ST, bool ZG>
 cudaError_t launch_typed(const Box &b, const StepConst &c, const Quant &q, const StepView &v, bool f_streamed,
                          bool odd, bool write_moments, cudaStream_t s)
 {
@@ -1320,12 +1332,12 @@ cudaError_t launch_typed(const Box &b, const StepConst &c, const Quant &q, const
     }
     for (int i = 0; i < 5; i++) P.mom[i] = v.mom + (size_t)i * b.n;
     P.err = v.err;
-    cudaError_t e = configure<ST, true, false, false>();
-    if (e == cudaSuccess) e = configure<ST, false, true, false>();
-    if (e == cudaSuccess) e = configure<ST, false, false, false>();
-    if (e == cudaSuccess) e = configure<ST, true, false, true>();
-    if (e == cudaSuccess) e = configure<ST, false, false, true>();
-    if (e == cudaSuccess) e = configure<ST, false, true, true>();
+    cudaError_t e = configure<ST, true, false, false, ZG>();
+    if (e == cudaSuccess) e = configure<ST, false, true, false, ZG>();
+    if (e == cudaSuccess) e = configure<ST, false, false, false, ZG>();
+    if (e == cudaSuccess) e = configure<ST, true, false, true, ZG>();
+    if (e == cudaSuccess) e = configure<ST, false, false, true, ZG>();
+    if (e == cudaSuccess) e = configure<ST, false, true, true, ZG>();
     if (e != cudaSuccess) return e;
     // staging by TMA when the driver encodes every map the step needs: the g
     // tile (even steps) and the P_f planes (if enabled)
@@ -1343,13 +1355,25 @@ cudaError_t launch_typed(const Box &b, const StepConst &c, const Quant &q, const
     const dim3 block(TX / (use_pair<ST>() ? 2 : 1), TY, 1);
     const int wm = write_moments ? 1 : 0;
     constexpr int smem = Geo<ST>::SMEM;
-    auto go = [&](auto kernel) { return launch_step_kernel(kernel, nblocks, block, smem, s, P, b, c, m, tz, wm, gmap, f0map, fqmap); };
+    const StepBox kb{b.nx, b.ny, b.nz, b.nxy, b.n};
+    auto go = [&](auto kernel) {
+        return launch_step_kernel(kernel, nblocks, block, smem, s, P, kb, c, m, tz, wm, gmap, f0map, fqmap);
+    };
     if (f_streamed) {
         if (odd) return cudaErrorInvalidValue;  // the streamed initial state is always read by an even step
-        return tma ? go(zsc_step_kernel<ST, true, false, true>) : go(zsc_step_kernel<ST, true, false, false>);
+        return tma ? go(zsc_step_kernel<ST, true, false, true, ZG>) : go(zsc_step_kernel<ST, true, false, false, ZG>);
     }
-    if (odd) return tma ? go(zsc_step_kernel<ST, false, true, true>) : go(zsc_step_kernel<ST, false, true, false>);
-    return tma ? go(zsc_step_kernel<ST, false, false, true>) : go(zsc_step_kernel<ST, false, false, false>);
+    if (odd)
+        return tma ? go(zsc_step_kernel<ST, false, true, true, ZG>) : go(zsc_step_kernel<ST, false, true, false, ZG>);
+    return tma ? go(zsc_step_kernel<ST, false, false, true, ZG>) : go(zsc_step_kernel<ST, false, false, false, ZG>);
+}
+
+template <typename ST>
+cudaError_t launch_typed(const Box &b, const StepConst &c, const Quant &q, const StepView &v, bool f_streamed,
+                         bool odd, bool write_moments, cudaStream_t s)
+{
+    if (b.zghost) return launch_typed<ST, true>(b, c, q, v, f_streamed, odd, write_moments, s);
+    return launch_typed<ST, false>(b, c, q, v, f_streamed, odd, write_moments, s);
 }
 
 }  // namespace
