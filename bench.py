@@ -486,7 +486,8 @@ def run_adjoint(local, long_horizon=False):
     short: 128^3, 8 bubbles R = 10, tau_rho = 0.8, gravity -1e-6, T = 2000,
            J = light-phase mean u_z over the last 200 states, FP32 state; the
            workload names no checkpoint budget, so the headline is the
-           library's default (half of the free device memory), with a 40 GB
+           library's default (the free device memory less a reserve of
+           max(4 GiB, 5%)), with a 40 GB
            budget reported beside it;
     long:  256^3, 64 bubbles R ~ U[6, 10], T = 20000, J = final light-phase
            z-centroid, FP16 live state (native FP16 snapshots), 40 GB budget.
@@ -564,7 +565,7 @@ def run_adjoint(local, long_horizon=False):
                         "short: 128^3, 8 bubbles R=10, tau_rho=0.8, T=2000, light-phase mean u_z over the "
                         "last 200 states, FP32 state"),
            "T": T, "forward_s": round(t_fwd, 4),
-           "budget": "40 GB" if long_horizon else "library default: half of the free device memory"}
+           "budget": "40 GB" if long_horizon else "library default: free device memory less max(4 GiB, 5%)"}
     out.update(head)
     out.update({"J": r["J"], "dJ_dgrav": r["dJ_dgrav"],
                 "fd_dJ_dgrav": {f"{h:g}": v for h, v in fd.items()}, "fd_richardson": rich,

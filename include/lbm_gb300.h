@@ -180,7 +180,8 @@ typedef struct lbm_adjoint_opts {
     int nsteps;               /* T: steps of the run, starting from the initial state */
     int window;               /* states averaged by LBM_OBJ_LIGHT_UZ_MEAN (the last `window`) */
     float grav;               /* body force of the run */
-    double checkpoint_bytes;  /* device memory for checkpoints; <= 0: half of the free memory */
+    double checkpoint_bytes;  /* device memory for checkpoints; <= 0: the free memory less a reserve of
+                                 max(4 GiB, 5% of the device) */
 } lbm_adjoint_opts;
 
 typedef struct lbm_adjoint_out {

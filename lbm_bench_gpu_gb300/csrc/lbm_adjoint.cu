@@ -550,9 +550,13 @@ extern "C" int lbm_step_adjoint(lbm_ctx *c, const lbm_adjoint_opts *o, lbm_adjoi
     // checkpoint pool (a cached pool counts as free for the default budget)
     double budget = o->checkpoint_bytes;
     if (!(budget > 0)) {
+        // the free device memory (the cached pool counted as free) less a
+        // reserve of 5% of the device or 4 GiB, whichever is larger: every
+        // checkpoint slot saves forward recomputation
         size_t fr = 0, tot = 0;
         cudaMemGetInfo(&fr, &tot);
-        budget = 0.5 * ((double)fr + (double)c->adj_slot_bytes);
+        const double reserve = std::max(4.0 * 1073741824.0, 0.05 * (double)tot);
+        budget = (double)fr + (double)c->adj_slot_bytes - reserve;
     }
     long long nslots = (long long)(budget / (double)A.snap_bytes);
     nslots = std::min<long long>(nslots, (long long)o->nsteps + 1);

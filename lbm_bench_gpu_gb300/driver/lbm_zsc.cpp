@@ -54,7 +54,7 @@ struct Options {
     int adjoint = -1;          // LBM_OBJ_*, -1: the reference's run
     int adjoint_steps = 1000;
     int adjoint_window = 1;
-    double checkpoint_gb = 0.0;   // <= 0: half of the free device memory
+    double checkpoint_gb = 0.0;   // <= 0: the library's default (free device memory less a reserve)
 };
 
 [[noreturn]] void fatal(const std::string &what, int code)

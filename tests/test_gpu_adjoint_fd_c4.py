@@ -1,0 +1,90 @@
+"""lbm_step_adjoint at the short adjoint workload's own configuration against
+FP64 central finite differences of the oracle's forward run.
+
+128^3, 8 bubbles of radius 10 at seeded centres, tau_rho = 0.8, gravity
+-1e-6, T = 2000 steps, J = light-phase mean u_z over the last 200 states, FP32
+state with the library's default checkpoint budget.  As in
+tests/test_gpu_adjoint_fd64.py the finite differences replay the heavy set
+H(phi > 0) of the unperturbed run (the adjoint differentiates with it held
+fixed; src/collision_f.cu:96 switches gravity on with it).
+
+* dJ/dgrav: h = 1e-6 on the force, bar 1e-4 relative;
+* dJ/dphi0: h = 1e-5 on 16 seeded random nodes among those with |dJ/dphi0|
+  above 10% of its maximum (the interface shells), bar 1e-4 relative each.
+
+Each FP64 forward run takes ~1-3 minutes of the host (2.1M nodes x 2000
+steps), and the check needs 35 of them, so this test runs only when
+LBM_SLOW_TESTS=1 is set.  The measured errors are written to
+$LBM_PARITY_REPORT when that is set.
+"""
+from __future__ import annotations
+
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+T, WINDOW, OBJ = 2000, 200, "light_uz_mean"
+H_GRAV, H_PHI, NODES = 1e-6, 1e-5, 16
+
+
+def setup():
+    from lbm_bench_gpu_gb300 import capi, inputs
+    from oracle.oracle import Oracle
+    inp = inputs.adjoint_short()
+    p = capi.make_params(inp.nx, inp.ny, inp.nz, rhoL=inp.rhoL, rhoH=inp.rhoH, tauRho=inp.tauRho,
+                         tauPhi=inp.tauPhi, width=inp.width, sigma=inp.sigma, Gamma=inp.Gamma, Eo=inp.Eo,
+                         rc0=inp.rc0)
+    grav = float(capi.derive(p).grav)
+    o = Oracle.from_params(p)
+    phi0 = o.bubble_phi(inp.bubbles)[1:-1].astype(np.float32)
+    rho0 = np.full(phi0.shape, 0.5 * (inp.rhoL + inp.rhoH), np.float32)
+    return p, grav, o, phi0, rho0
+
+
+def gpu_gradient(p, grav, phi0, rho0) -> dict:
+    from lbm_bench_gpu_gb300 import capi
+    with capi.Lattice.from_fields(p, phi0, rho0) as lat:
+        r = lat.adjoint(T, grav, OBJ, WINDOW)
+    g0 = r["dJ_dphi0"]
+    big = np.flatnonzero(np.abs(g0) > 0.1 * np.abs(g0).max())
+    nodes = np.random.default_rng(20261203).choice(big, size=NODES, replace=False)
+    return {"J": r["J"], "dJ_dgrav": r["dJ_dgrav"], "nodes": nodes, "dJ_dphi0": g0.ravel()[nodes].astype(np.float64)}
+
+
+def fd_errors(o, grav, phi0, rho0, r: dict) -> dict:
+    def J64(phi, g):
+        o.init(phi, rho0.astype(np.float64))
+        return o.objective(T, g, OBJ, WINDOW)
+
+    base = phi0.astype(np.float64)
+    o.heavy_mask("record", T)
+    J = J64(base, grav)
+    o.heavy_mask("replay")
+    fd_g = (J64(base, grav + H_GRAV) - J64(base, grav - H_GRAV)) / (2 * H_GRAV)
+    errs = []
+    for k, gk in zip(r["nodes"], r["dJ_dphi0"]):
+        vals = []
+        for sgn in (1, -1):
+            ph = base.copy()
+            ph.flat[k] += sgn * H_PHI
+            vals.append(J64(ph, grav))
+        fd = (vals[0] - vals[1]) / (2 * H_PHI)
+        errs.append(abs(gk - fd) / abs(fd))
+    o.heavy_mask("off")
+    return {"J_rel": abs(r["J"] - J) / abs(J), "dJ_dgrav_rel": abs(r["dJ_dgrav"] - fd_g) / abs(fd_g),
+            "dJ_dphi0_rel_max": float(max(errs)), "dJ_dphi0_rel_median": float(np.median(errs)), "fd_dJ_dgrav": fd_g}
+
+
+@pytest.mark.skipif(os.environ.get("LBM_SLOW_TESTS") != "1", reason="35 FP64 runs of 128^3 x 2000 steps: set LBM_SLOW_TESTS=1")
+def test_adjoint_vs_fp64_fd_at_the_workload_configuration(lib):
+    from conftest import report
+    p, grav, o, phi0, rho0 = setup()
+    r = gpu_gradient(p, grav, phi0, rho0)
+    e = fd_errors(o, grav, phi0, rho0, r)
+    report("adjoint C4 vs FP64 FD (frozen heavy set)", e, {"dJ_dgrav_rel": 1e-4, "dJ_dphi0_rel_max": 1e-4})
+    assert e["J_rel"] <= 1e-4
+    assert e["dJ_dgrav_rel"] <= 1e-4
+    assert e["dJ_dphi0_rel_max"] <= 1e-4
