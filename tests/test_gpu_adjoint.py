@@ -118,3 +118,36 @@ def test_workspace_is_kept_between_calls_and_released(lib):
         assert r["J"] == tight["J"] and r["dJ_dgrav"] == tight["dJ_dgrav"]
         assert np.array_equal(r["dJ_dphi0"], tight["dJ_dphi0"])
     assert J == pytest.approx(tight["J"], rel=1e-14)
+
+
+# 16-bit states: the adjoint reads the forward state (checkpoints included)
+# in its storage format and layout; its arithmetic and lambda stay FP32.  The
+# gradient then follows the 16-bit trajectory, whose error against the FP64
+# oracle is the storage's: bounds (J, dJ/dgrav, dJ/dphi0 of its max) FP16
+# 1e-4 / 1e-3 / 1e-3, BF16 1e-3 / 1e-2 / 1e-2 (measured: FP16 4.2e-5 / 1.8e-7 /
+# 4.6e-5, BF16 2.7e-5 / 2.7e-7 / 4.1e-4).
+ADJ_STORAGE_BOUNDS = {"fp16": (1e-4, 1e-3, 1e-3), "bf16": (1e-3, 1e-2, 1e-2)}
+
+
+@pytest.mark.parametrize("storage", ["fp16", "bf16"])
+def test_gpu_adjoint_16bit_state_matches_oracle(lib, storage):
+    from conftest import report
+    from lbm_bench_gpu_gb300 import capi
+    o0 = Oracle(64, 32, 16, **KW)
+    pg = o0.bubble_phi(np.array([[40.5, 16.3, 8.4, 6.0], [12.0, 9.0, 7.0, 4.5]], np.float32))
+    phi0, rho0 = pg[1:-1].astype(np.float32), np.full((16, 32, 64), 0.55, np.float32)
+    T, window, grav = 12, 5, -3e-5
+    o = Oracle(64, 32, 16, **KW)
+    o.init(phi0.astype(np.float64), rho0.astype(np.float64))
+    J, dg, lf, lg = o.adjoint(T, grav, "light_uz_mean", window)
+    lphi, _ = o.init_adjoint(phi0.astype(np.float64), lf, lg)
+    p = capi.make_params(64, 32, 16, storage=storage, **KW)
+    with capi.Lattice.from_fields(p, phi0, rho0) as lat:
+        # few slots: the state is recomputed from 16-bit checkpoints
+        r = lat.adjoint(T, grav, "light_uz_mean", window, checkpoint_bytes=4.5 * 54 * 64 * 32 * 16)
+    bj, bg, bp = ADJ_STORAGE_BOUNDS[storage]
+    e = {"J": abs(r["J"] - J) / abs(J), "dJ_dgrav": abs(r["dJ_dgrav"] - dg) / abs(dg),
+         "dJ_dphi0": float(np.abs(r["dJ_dphi0"] - lphi).max() / np.abs(lphi).max())}
+    report(f"adjoint {storage} state vs FP64 oracle adjoint", e, {"J": bj, "dJ_dgrav": bg, "dJ_dphi0": bp})
+    assert r["slots"] < T + 1
+    assert e["J"] <= bj and e["dJ_dgrav"] <= bg and e["dJ_dphi0"] <= bp, e
