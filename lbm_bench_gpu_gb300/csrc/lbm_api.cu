@@ -235,7 +235,9 @@ namespace lbm {
 int device_error(lbm_ctx *c)
 {
     int flag = 0;
-    LBM_CUDA(cudaMemcpy(&flag, c->err, sizeof(int), cudaMemcpyDeviceToHost), "error flag");
+    // on the context's stream, after the kernels that set it
+    LBM_CUDA(cudaMemcpyAsync(&flag, c->err, sizeof(int), cudaMemcpyDeviceToHost, c->stream), "error flag");
+    LBM_CUDA(cudaStreamSynchronize(c->stream), "error flag");
     if (flag & 4) return fail(LBM_ECUDA, "a checked build found a global index outside its field");
     if (flag & 2) return fail(LBM_ECUDA, "a step kernel's shared-memory stage was misaligned for TMA");
     if (flag) return fail(LBM_ETIMEOUT, "a step kernel timed out waiting for its staged data");

@@ -248,22 +248,26 @@ extern "C" int lbm_split_z(lbm_ctx *whole, int nslabs, const int *depths, const 
         if (e == cudaSuccess) e = cudaMalloc(&c->phi_ghost, sizeof(float) * 2 * nxy);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_pack, cudaEventDisableTiming);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_unpack, cudaEventDisableTiming);
-        // the interior planes of the whole context's current state
+        // the interior planes of the whole context's current state, copied on
+        // the slab's stream (the context streams do not order with the legacy
+        // default stream, and a device-to-device cudaMemcpy does not wait)
         const int h = whole->st.f_cur;
         const size_t d = (size_t)depths[k];
         for (int f = 0; f < lbm::kQf && e == cudaSuccess; f++) {
             const size_t es = f == 0 ? sizeof(float) : whole->esz;
             const unsigned char *src = f_field(whole, h, f) + (size_t)z0 * nxy * es;
-            e = cudaMemcpy(f_field(c, 0, f) + 2 * nxy * es, src, d * nxy * es, cudaMemcpyDefault);
+            e = cudaMemcpyAsync(f_field(c, 0, f) + 2 * nxy * es, src, d * nxy * es, cudaMemcpyDefault, c->stream);
         }
         for (int i = 0; i < lbm::kQg && e == cudaSuccess; i++)
-            e = cudaMemcpy(g_field(c, i) + nxy * c->esz, g_field(whole, i) + (size_t)z0 * nxy * whole->esz,
-                           d * nxy * c->esz, cudaMemcpyDefault);
+            e = cudaMemcpyAsync(g_field(c, i) + nxy * c->esz, g_field(whole, i) + (size_t)z0 * nxy * whole->esz,
+                                d * nxy * c->esz, cudaMemcpyDefault, c->stream);
         for (int a = 0; a < 5 && e == cudaSuccess; a++)
-            e = cudaMemcpy(c->st.mom + (size_t)a * c->box.n, whole->st.mom + (size_t)a * n + (size_t)z0 * nxy,
-                           d * nxy * sizeof(float), cudaMemcpyDefault);
+            e = cudaMemcpyAsync(c->st.mom + (size_t)a * c->box.n, whole->st.mom + (size_t)a * n + (size_t)z0 * nxy,
+                                d * nxy * sizeof(float), cudaMemcpyDefault, c->stream);
         if (e == cudaSuccess) e = cudaEventRecord(c->ev_pack, c->stream);
         if (e == cudaSuccess) e = cudaEventRecord(c->ev_unpack, c->stream);
+        // the whole context may be stepped or freed once this returns
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
         if (e != cudaSuccess) rc = cuda_fail(e, "lbm_split_z");
         c->st.f_cur = 0;
         c->st.f_streamed = whole->st.f_streamed;
@@ -303,21 +307,24 @@ extern "C" int lbm_merge_z(lbm_ctx *const *slabs, int nslabs, lbm_ctx *whole)
         lbm_ctx *c = slabs[k];
         const size_t d = (size_t)c->box.nz, z0 = (size_t)c->z0;
         const int h = c->st.f_cur;
+        // on the whole context's stream, which its next work follows
         for (int f = 0; f < lbm::kQf; f++) {
             const size_t es = f == 0 ? sizeof(float) : c->esz;
-            LBM_CUDA(cudaMemcpy(f_field(whole, 0, f) + z0 * nxy * es, f_field(c, h, f) + 2 * nxy * es,
-                                d * nxy * es, cudaMemcpyDefault),
+            LBM_CUDA(cudaMemcpyAsync(f_field(whole, 0, f) + z0 * nxy * es, f_field(c, h, f) + 2 * nxy * es,
+                                     d * nxy * es, cudaMemcpyDefault, whole->stream),
                      "lbm_merge_z");
         }
         for (int i = 0; i < lbm::kQg; i++)
-            LBM_CUDA(cudaMemcpy(g_field(whole, i) + z0 * nxy * c->esz, g_field(c, i) + nxy * c->esz,
-                                d * nxy * c->esz, cudaMemcpyDefault),
+            LBM_CUDA(cudaMemcpyAsync(g_field(whole, i) + z0 * nxy * c->esz, g_field(c, i) + nxy * c->esz,
+                                     d * nxy * c->esz, cudaMemcpyDefault, whole->stream),
                      "lbm_merge_z");
         for (int a = 0; a < 5; a++)
-            LBM_CUDA(cudaMemcpy(whole->st.mom + (size_t)a * n + z0 * nxy, c->st.mom + (size_t)a * c->box.n,
-                                d * nxy * sizeof(float), cudaMemcpyDefault),
+            LBM_CUDA(cudaMemcpyAsync(whole->st.mom + (size_t)a * n + z0 * nxy, c->st.mom + (size_t)a * c->box.n,
+                                     d * nxy * sizeof(float), cudaMemcpyDefault, whole->stream),
                      "lbm_merge_z");
     }
+    // the slabs may step on (and overwrite what was read) once this returns
+    LBM_CUDA(cudaStreamSynchronize(whole->stream), "lbm_merge_z");
     whole->q = s0->q;
     whole->st.f_cur = 0;
     whole->st.f_streamed = s0->st.f_streamed;

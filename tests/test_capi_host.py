@@ -167,7 +167,7 @@ def test_bubble_placement_rules():
 
 def test_integration_examples_compile_and_link(lib, tmp_path):
     """The C examples of INTEGRATION.md (the reference's main loop on the C-ABI,
-    and the adjoint calls) compile with -Wall -Werror against the header and
+    the adjoint calls and the one-process z-slab loop) compile with -Wall -Werror against the header and
     link against the library: what a maintainer of the reference would build."""
     import re
     import shutil
@@ -187,13 +187,22 @@ def test_integration_examples_compile_and_link(lib, tmp_path):
         "#define CHECK(x) do { int rc_ = (x); if (rc_) { fprintf(stderr, \"%s\\n\", lbm_strerror(rc_)); "
         "return 1; } } while (0)\n"
         "int adjoint_example(lbm_ctx *c, lbm_derived d, float *grad)\n{\n" + blocks[1] + "    return 0;\n}\n")
+    # the one-process z-slab loop, inside a function with the main loop's variables
+    slab_block = next(b for b in blocks if "lbm_split_z(" in b)
+    slab_c = tmp_path / "slabs.c"
+    slab_c.write_text(
+        "#include <stdio.h>\n#include \"lbm_gb300.h\"\n"
+        "#define CHECK(x) do { int rc_ = (x); if (rc_) { fprintf(stderr, \"%s\\n\", lbm_strerror(rc_)); "
+        "return 1; } } while (0)\n"
+        "int slab_example(lbm_params p, lbm_run run, lbm_derived d, const float *bubbles, int nb)\n{\n"
+        "    lbm_stats_out s;\n" + slab_block + "    lbm_destroy(whole);\n    return 0;\n}\n")
     pkg = root / "lbm_bench_gpu_gb300"
-    for src in (main_c, adjoint_c):
+    for src in (main_c, adjoint_c, slab_c):
         args = [cc, "-std=c99", "-Wall", "-Werror", str(src), "-I", str(root / "include")]
         if src is main_c:
             args += ["-L", str(pkg), "-llbm_gb300", "-o", str(tmp_path / "main_loop")]
         else:
-            args += ["-c", "-o", str(tmp_path / "adjoint.o")]
+            args += ["-c", "-o", str(tmp_path / (src.stem + ".o"))]
         r = subprocess.run(args, capture_output=True, text=True)
         assert r.returncode == 0, r.stderr
 
