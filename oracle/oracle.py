@@ -75,6 +75,8 @@ def oracle_lib() -> C.CDLL:
         lib.zo_heavy_mask.argtypes = [C.c_void_p, C.c_int, C.c_long]
         lib.zo_heavy_mask.restype = C.c_int
         lib.zo_init_adjoint.argtypes = [C.c_void_p, _D, _D, _D, _D, _D]
+        lib.zo_set_rounding.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_int, C.c_double, _D]
+        lib.zo_round_array.argtypes = [C.c_int, _D, _D, C.c_long]
         _oracle_lib = lib
     return _oracle_lib
 
@@ -84,6 +86,18 @@ CONSTANT_NAMES = ["phiStar", "phiStarSq", "invTauRho", "invTauRhoOne", "invTauRh
                   "K0", "K1", "K2", "KC0", "KC1", "KC2"]
 STATS_NAMES = ["umax", "vol", "ux_av", "uy_av", "uz_av", "ref", "p_in", "p_out", "p_dif", "p_err",
                "phi_sum", "rho_sum", "mom_x", "mom_y", "mom_z", "vol_full", "umax_full"]
+
+
+FORMATS = {"none": 0, "fp32": 1, "fp16": 2, "bf16": 3}
+
+
+def round_to(fmt: str, a) -> np.ndarray:
+    """a rounded (from its FP32 value, to nearest even) to a storage format, as
+    the oracle's storage-rounding emulation does."""
+    a = np.ascontiguousarray(a, np.float64)
+    out = np.empty_like(a)
+    oracle_lib().zo_round_array(FORMATS[fmt], _dptr(a), _dptr(out), a.size)
+    return out
 
 
 class Oracle:
@@ -203,6 +217,16 @@ class Oracle:
         if self.lib.zo_adjoint_apply(self.h, float(grav), _dptr(lf), _dptr(lg), _dptr(of), _dptr(og), C.byref(dg)):
             raise MemoryError("zo_adjoint_apply")
         return of, og, dg.value
+
+    def set_rounding(self, f0: str = "none", f: str = "none", f_scale: float = 1.0, g: str = "none",
+                     g_scale: float = 1.0, g_shift=None) -> None:
+        """Storage-rounding emulation (zo_set_rounding in zsc_oracle.c): after
+        every collision round f_0 to format f0, f_1..f_6 to fmt(f_k * f_scale)
+        and g_i to fmt((g_i - g_shift[i]) * g_scale), formats "none", "fp32",
+        "fp16", "bf16".  All-"none" switches it off."""
+        sh = np.zeros(19) if g_shift is None else np.ascontiguousarray(g_shift, np.float64)
+        self.lib.zo_set_rounding(self.h, FORMATS[f0], FORMATS[f], float(f_scale), FORMATS[g], float(g_scale),
+                                 _dptr(sh))
 
     def heavy_mask(self, mode: str, steps: int = 0) -> None:
         """Heavy-node log: "record" H(phi > 0) of the next `steps` collisions

@@ -72,6 +72,11 @@ typedef struct zo_ctx {
      * (2 x 26 planes: side, then f 0..6, g 0..18). */
     int slab;
     double *phi_ghost, *post_ghost;
+    /* Storage-rounding emulation (precision studies, zo_set_rounding): the
+     * post-collision f_0, f_1..f_6 and g sets rounded after every collision
+     * to the formats a GPU build stores them in. */
+    int round_f0, round_f, round_g;
+    double f_scale, g_scale, g_shift[19];
 } zo_ctx;
 
 static inline long zo_idx(const zo_ctx *s, int x, int y, int z)
@@ -543,11 +548,84 @@ void zo_slab_stream(zo_ctx *s)
 
 /* One or more steps in the order of src/main.cu:363-473 (relaxation loop) and
  * src/main.cu:496-608 (evolution loop); grav is grav_d (0 while relaxing). */
+/*
+ * Storage-rounding emulation (test aid for precision studies; no counterpart
+ * in the reference, which stores FP32).  A GPU build that keeps the
+ * post-collision sets in a 16-bit format stores, per node and population,
+ *   f_0 as FP32, f_k (k = 1..6) as fmt(f_k * f_scale), g_i as
+ *   fmt((g_i - shift_i) * g_scale),
+ * the value formed in FP32 and rounded to nearest even.  zo_set_rounding
+ * makes zo_step apply that round trip to the post-collision arrays, between
+ * the collision and the streaming, with FP64 arithmetic everywhere else, so
+ * that a run isolates the storage format's share of the error.
+ * Formats: ZO_FMT_NONE, ZO_FMT_FP32, ZO_FMT_FP16 (IEEE binary16: 11
+ * significant bits, subnormals below 2^-14, overflow above 65504), ZO_FMT_BF16
+ * (8 significant bits, the FP32 exponent range).
+ */
+enum { ZO_FMT_NONE = 0, ZO_FMT_FP32 = 1, ZO_FMT_FP16 = 2, ZO_FMT_BF16 = 3 };
+
+/* x rounded to nearest even with `bits` significant bits, the exponent of
+ * its lowest bit at least `emin` (subnormals) */
+static double round_sig(double x, int bits, int emin)
+{
+    if (x == 0.0 || !isfinite(x)) return x;
+    int e;
+    frexp(x, &e);                     /* |x| in [2^(e-1), 2^e) */
+    int q = e - bits;                 /* exponent of the last kept bit */
+    if (q < emin) q = emin;
+    return ldexp(nearbyint(ldexp(x, -q)), q);
+}
+
+double zo_round(int fmt, double x)
+{
+    switch (fmt) {
+    case ZO_FMT_FP32: return (double)(float)x;
+    case ZO_FMT_FP16: {
+        const double v = round_sig((double)(float)x, 11, -24);
+        return fabs(v) > 65504.0 ? copysign(INFINITY, v) : v;
+    }
+    case ZO_FMT_BF16: return round_sig((double)(float)x, 8, -133);
+    default: return x;
+    }
+}
+
+void zo_round_array(int fmt, const double *in, double *out, long n)
+{
+    for (long i = 0; i < n; i++) out[i] = zo_round(fmt, in[i]);
+}
+
+void zo_set_rounding(zo_ctx *s, int f0_fmt, int f_fmt, double f_scale, int g_fmt, double g_scale,
+                     const double *g_shift)
+{
+    s->round_f0 = f0_fmt;
+    s->round_f = f_fmt;
+    s->round_g = g_fmt;
+    s->f_scale = f_scale;
+    s->g_scale = g_scale;
+    for (int i = 0; i < 19; i++) s->g_shift[i] = g_shift ? g_shift[i] : 0.0;
+}
+
+static void zo_round_post(zo_ctx *s)
+{
+    if (!s->round_f0 && !s->round_f && !s->round_g) return;
+    const double fi = 1.0 / s->f_scale, gi = 1.0 / s->g_scale;
+#pragma omp parallel for schedule(static)
+    for (long id = 0; id < s->n; id++) {
+        if (s->round_f0) s->fp[0][id] = zo_round(s->round_f0, s->fp[0][id]);
+        if (s->round_f)
+            for (int k = 1; k < 7; k++) s->fp[k][id] = zo_round(s->round_f, s->fp[k][id] * s->f_scale) * fi;
+        if (s->round_g)
+            for (int i = 0; i < 19; i++)
+                s->gp[i][id] = zo_round(s->round_g, (s->gp[i][id] - s->g_shift[i]) * s->g_scale) * gi + s->g_shift[i];
+    }
+}
+
 void zo_step(zo_ctx *s, int nsteps, double grav)
 {
     for (int t = 0; t < nsteps; t++) {
         zo_moments_update(s);
         zo_collide(s, grav);
+        zo_round_post(s);
         zo_stream(s);
         s->steps++;
     }
