@@ -34,8 +34,9 @@
 // whose blocks take kLocalPlanes (2) planes gridDim.z apart (with consecutive
 // planes the compiler keeps more values live across iterations and spills),
 // with the next plane's rows prefetched into L2.  Measured at 128^3 (T = 2000,
-// 40 GB): 1, 2, 4 local planes -> adjoint/forward 4.06, 3.99, 4.09; 8 and 16
-// stencil planes are slower.  32-bit node indices (n * 19 < 2^32 is checked at
+// 40 GB): 1, 2, 4 local planes -> adjoint/forward 4.06, 3.99, 4.09 (and, later,
+// 3.92, 3.81, 3.87; at 256^3 with an FP16 state, T = 400: 6.21, 6.07, 6.12);
+// 8 and 16 stencil planes are slower.  32-bit node indices (n * 19 < 2^32 is checked at
 // init).
 #include <algorithm>
 #include <type_traits>
@@ -49,9 +50,21 @@ constexpr int TXA = 32, TYA = 8, NTA = TXA * TYA;
 #ifndef ZSC_ADJ_PLANES
 #define ZSC_ADJ_PLANES 4
 #endif
-#ifndef ZSC_ADJ_MIN_BLOCKS
-#define ZSC_ADJ_MIN_BLOCKS 3
+// Resident blocks per SM the local kernel's launch bounds ask for: 3 (80
+// registers) for an FP32 state, 4 (64 registers, ~100 bytes spilled) for a
+// 16-bit state, whose two-byte gathers leave more latency to hide.  Measured
+// (adjoint / forward wall time): 256^3 FP16 state, T = 400, 40 GB: 2, 3, 4
+// blocks -> 6.18, 6.07, 5.79; 128^3 FP32 state, T = 2000, 40 GB: 4.03, 3.81,
+// 3.92.  ZSC_ADJ_MIN_BLOCKS overrides both.
+template <typename ST>
+constexpr int adj_min_blocks()
+{
+#ifdef ZSC_ADJ_MIN_BLOCKS
+    return ZSC_ADJ_MIN_BLOCKS;
+#else
+    return sizeof(ST) == 2 ? 4 : 3;
 #endif
+}
 #ifndef ZSC_ADJ_LOCAL_PLANES
 #define ZSC_ADJ_LOCAL_PLANES 2
 #endif
@@ -378,7 +391,7 @@ __device__ __forceinline__ void prefetch_plane(const Box &b, const AdjIn &a, int
 
 // The local part of one adjoint step (see the file comment).
 template <typename ST, bool ODD>
-__global__ void __launch_bounds__(NTA, ZSC_ADJ_MIN_BLOCKS) adjoint_local_kernel(Box b, StepConst c, float phiStar, Quant q, AdjIn a)
+__global__ void __launch_bounds__(NTA, adj_min_blocks<ST>()) adjoint_local_kernel(Box b, StepConst c, float phiStar, Quant q, AdjIn a)
 {
     __shared__ double red[NTA / 32];
     double dg = 0.0;
