@@ -304,6 +304,23 @@ int lbm_stats_noalloc(const lbm_params *p, const float *phi, const float *rho, c
  * slab from the input files).  The whole context is left as it was. */
 int lbm_split_z(lbm_ctx *whole, int nslabs, const int *depths, const int *devices, lbm_ctx **slabs);
 
+/* One process per GPU, without the whole box on any device: each process
+ * builds its own slab, planes [z0, z0 + depth) of the box p describes (p->nz
+ * the whole box's planes, p->device this slab's device), from the bubble list,
+ * as each rank of the reference builds its planes (src/init.c:39-59 with its
+ * z offset; the planes next to the slab take phi from the geometry, as the
+ * reference's ghost planes do).
+ * The 16-bit storage map (one scale per distribution set) comes from maxima
+ * over the whole box: lbm_slab_maxabs gives a slab's 26 maxima (|f_k|,
+ * |g_i - w_i rho_mean|; zeros for FP32), the processes reduce them with MAX
+ * (MPI_Allreduce, ncclAllReduce) and pass the result to
+ * lbm_slab_init_bubbles (NULL is accepted for FP32 storage only).  The slabs
+ * so made hold bit for bit what lbm_split_z of lbm_init_bubbles's whole box
+ * holds.  Both synchronise. */
+int lbm_slab_maxabs(const lbm_params *p, const float *bubbles, int nbubbles, int z0, int depth, float *maxabs);
+int lbm_slab_init_bubbles(lbm_ctx **out, const lbm_params *p, const float *bubbles, int nbubbles, int z0,
+                          int depth, const float *maxabs);
+
 /* Gather the states of the slabs (as lbm_split_z made them, in order) back
  * into the whole-box context they came from (or one created with the same
  * parameters).  LBM_ESTATE if a slab still owes its neighbours the

@@ -26,7 +26,8 @@ EXPORTS = [
     "lbm_objective", "lbm_stats_fields", "lbm_pressure", "lbm_device_name", "lbm_adjoint_release",
     "lbm_wait_selftest", "lbm_adjoint_forward_steps", "lbm_state_bytes", "lbm_save_state", "lbm_load_state",
     "lbm_split_z", "lbm_merge_z", "lbm_slab_step", "lbm_halo_bytes", "lbm_halo_pack", "lbm_halo_unpack",
-    "lbm_slab_step_local", "lbm_stats_raw", "lbm_stats_combine", "lbm_slab_stats",
+    "lbm_slab_step_local", "lbm_stats_raw", "lbm_stats_combine", "lbm_slab_stats", "lbm_slab_maxabs",
+    "lbm_slab_init_bubbles",
 ]
 OBJECTIVES = {"light_uz_mean": 0, "light_z_centroid": 1}
 
@@ -138,6 +139,9 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
     _V, _I, _D = C.POINTER(C.c_void_p), C.POINTER(C.c_int), C.POINTER(C.c_double)
     lib.lbm_split_z.argtypes = [C.c_void_p, C.c_int, _I, _I, _V]
     lib.lbm_merge_z.argtypes = [_V, C.c_int, C.c_void_p]
+    lib.lbm_slab_maxabs.argtypes = [C.POINTER(Params), _F, C.c_int, C.c_int, C.c_int, _F]
+    lib.lbm_slab_init_bubbles.argtypes = [C.POINTER(C.c_void_p), C.POINTER(Params), _F, C.c_int, C.c_int, C.c_int,
+                                          _F]
     lib.lbm_slab_step.argtypes = [_V, C.c_int, C.c_int, C.c_float]
     lib.lbm_halo_bytes.argtypes = [C.c_void_p, C.c_int]
     lib.lbm_halo_bytes.restype = C.c_longlong
@@ -359,14 +363,39 @@ class Slabs:
     depths[k] consecutive planes, on devices[k] (default: the whole context's
     device); lbm_slab_step steps them together with their halo exchanges."""
 
-    def __init__(self, whole: Lattice, depths, devices=None):
-        self.params = whole.params
+    def __init__(self, whole: Lattice | None, depths, devices=None):
         self.n = len(depths)
+        self.depths = list(depths)
+        self._h = (C.c_void_p * self.n)()
+        if whole is None:   # filled by from_bubbles
+            return
+        self.params = whole.params
         d = (C.c_int * self.n)(*[int(v) for v in depths])
         dev = (C.c_int * self.n)(*[int(v) for v in devices]) if devices is not None else None
-        self._h = (C.c_void_p * self.n)()
         check(load().lbm_split_z(whole._h, self.n, d, dev, self._h), "lbm_split_z")
-        self.depths = list(depths)
+
+    @classmethod
+    def from_bubbles(cls, p: Params, bubbles, depths, devices=None) -> "Slabs":
+        """Each slab built on its own from the bubble list (lbm_slab_maxabs,
+        the maxima reduced here as processes would with MPI_Allreduce(MAX),
+        then lbm_slab_init_bubbles): no whole box on any device."""
+        b = np.ascontiguousarray(bubbles, np.float32).reshape(-1, 4)
+        z0s = np.concatenate([[0], np.cumsum(depths)[:-1]]).astype(int)
+        per = []
+        for k, (z0, d) in enumerate(zip(z0s, depths)):
+            q = Params(**{**p.as_dict(), "device": devices[k] if devices is not None else p.device})
+            m = np.zeros(26, np.float32)
+            check(load().lbm_slab_maxabs(C.byref(q), fptr(b), len(b), int(z0), int(d), fptr(m)), "lbm_slab_maxabs")
+            per.append((q, m))
+        maxabs = np.max([m for _, m in per], axis=0).astype(np.float32)
+        self = cls(None, depths)
+        self.params = p
+        for k, (z0, d) in enumerate(zip(z0s, depths)):
+            h = C.c_void_p()
+            check(load().lbm_slab_init_bubbles(C.byref(h), C.byref(per[k][0]), fptr(b), len(b), int(z0), int(d),
+                                               fptr(maxabs)), "lbm_slab_init_bubbles")
+            self._h[k] = h.value
+        return self
 
     def step(self, nsteps: int, grav: float = 0.0) -> None:
         check(load().lbm_slab_step(self._h, self.n, int(nsteps), float(grav)), "lbm_slab_step")

@@ -128,9 +128,15 @@ int reduce_stats(lbm_ctx *c)
 
 // Load streamed FP32 distributions tf (7 x n) and tg (19 x n) into the state
 // (half 0, natural g layout), choosing the 16-bit storage map from the data.
-// c->st.mom must already hold the fields (for the mean density).
-int load_state(lbm_ctx *c, const float *tf, const float *tg)
+// c->st.mom must already hold the fields (for the mean density).  maxabs_in
+// (26 floats: |f_k| and |g_i - shift_i| maxima) replaces the maxima of this
+// context's data (a z-slab takes the maxima of the whole box, reduced over
+// its slabs); maxabs_out receives this context's maxima (zeros for FP32).
+int load_state(lbm_ctx *c, const float *tf, const float *tg, const float *maxabs_in = nullptr,
+               float *maxabs_out = nullptr)
 {
+    if (maxabs_out)
+        for (int k = 0; k < lbm::kQf + lbm::kQg; k++) maxabs_out[k] = 0.f;
     identity_quant(c->q);
     if (c->p.storage != LBM_STORAGE_FP32) {
         int rc = reduce_stats(c);
@@ -150,6 +156,10 @@ int load_state(lbm_ctx *c, const float *tf, const float *tg)
         cudaFree(shift_dev);
         cudaFree(bits_dev);
         if (e != cudaSuccess) return cuda_fail(e, "storage map");
+        for (int k = 0; k < lbm::kQf + lbm::kQg; k++) {
+            if (maxabs_out) std::memcpy(&maxabs_out[k], &bits[k], sizeof(float));
+            if (maxabs_in) std::memcpy(&bits[k], &maxabs_in[k], sizeof(float));
+        }
         // Scales: powers of two that put a generous bound on each field at
         // 2^12, leaving 16x headroom below the FP16 maximum (65504).  The bound
         // covers the flow developing later: |u| up to 0.1 moves g_i by about
@@ -198,8 +208,11 @@ int load_state(lbm_ctx *c, const float *tf, const float *tg)
 // holds the streamed FP32 distributions as they are, so the equilibrium is
 // written straight into half 0; the 16-bit formats go through FP32 scratch,
 // from which the storage map is chosen.
-int init_from_mom(lbm_ctx *c, const float *ghost_lo, const float *ghost_hi)
+int init_from_mom(lbm_ctx *c, const float *ghost_lo, const float *ghost_hi, const float *maxabs_in = nullptr,
+                  float *maxabs_out = nullptr)
 {
+    if (maxabs_out)
+        for (int k = 0; k < lbm::kQf + lbm::kQg; k++) maxabs_out[k] = 0.f;
     const size_t n = (size_t)c->box.n;
     if (c->p.storage == LBM_STORAGE_FP32) {
         identity_quant(c->q);
@@ -219,7 +232,8 @@ int init_from_mom(lbm_ctx *c, const float *ghost_lo, const float *ghost_hi)
     LBM_CUDA(cudaMalloc(&tmp, sizeof(float) * (lbm::kQf + lbm::kQg) * n), "init scratch");
     cudaError_t e = lbm::launch_equilibrium(c->box, c->d, c->p.Gamma, c->st.mom, c->st.mom + n, ghost_lo, ghost_hi,
                                             tmp, tmp + n, tmp + lbm::kQf * n, c->stream);
-    int rc = e == cudaSuccess ? load_state(c, tmp, tmp + lbm::kQf * n) : cuda_fail(e, "equilibrium kernel");
+    int rc = e == cudaSuccess ? load_state(c, tmp, tmp + lbm::kQf * n, maxabs_in, maxabs_out)
+                              : cuda_fail(e, "equilibrium kernel");
     cudaStreamSynchronize(c->stream);
     cudaFree(tmp);
     c->st.steps = 0;
@@ -310,6 +324,67 @@ extern "C" int lbm_init(lbm_ctx **out, const lbm_params *p, const float *phi0, c
     return LBM_OK;
 }
 
+namespace {
+
+// The initial state of a created context from the bubble list (src/init.c:39-59,
+// src/init_f.cu, src/init_g.cu): phi from the bubbles on the box's planes and on
+// the planes just below and above it (from the geometry, as the reference's
+// ghost planes), rho = (rhoH + rhoL) / 2, u = 0, the at-rest equilibrium.  The
+// box's plane 0 is plane z0 of the bubbles' frame (a slab of a larger box).
+int init_bubbles_into(lbm_ctx *c, const float *bubbles, int nbubbles, int z0, const float *maxabs_in,
+                      float *maxabs_out)
+{
+    const size_t n = (size_t)c->box.n, nxy = (size_t)c->box.nxy;
+    float *phig = nullptr, *bub = nullptr;
+    float *mom = c->st.mom;
+    cudaError_t e = cudaMalloc(&phig, sizeof(float) * nxy * (c->box.nz + 2));
+    if (e == cudaSuccess && nbubbles > 0) e = cudaMalloc(&bub, sizeof(float) * 4 * nbubbles);
+    if (e == cudaSuccess && nbubbles > 0)
+        e = cudaMemcpyAsync(bub, bubbles, sizeof(float) * 4 * nbubbles, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess)
+        e = lbm::launch_bubble_phi(c->box, bub, nbubbles, c->d.phiStar, c->p.width, z0, phig, c->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(mom, phig + nxy, sizeof(float) * n, cudaMemcpyDeviceToDevice, c->stream);
+    if (e == cudaSuccess) e = lbm::launch_fill(mom + n, (long long)n, 0.5f * (c->p.rhoH + c->p.rhoL), c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(mom + 2 * n, 0, sizeof(float) * 3 * n, c->stream);
+    const int rc = e == cudaSuccess
+                       ? init_from_mom(c, phig, phig + nxy * (c->box.nz + 1), maxabs_in, maxabs_out)
+                       : cuda_fail(e, "bubble initial state");
+    cudaStreamSynchronize(c->stream);
+    if (phig) cudaFree(phig);
+    if (bub) cudaFree(bub);
+    return rc;
+}
+
+// Checks of a slab request of the whole box p, before any CUDA call.
+int check_slab_request(const lbm_params *p, const float *bubbles, int nbubbles, int z0, int depth)
+{
+    if (nbubbles < 0 || (nbubbles > 0 && !bubbles)) return fail(LBM_EINVAL, "bad bubble list");
+    if (int rc = validate(p)) return rc;
+    if (depth < 2 || z0 < 0 || z0 + depth > p->nz)
+        return fail(LBM_EINVAL, "slab planes outside the box (need depth >= 2 and 0 <= z0, z0 + depth <= nz)");
+    return LBM_OK;
+}
+
+// A created context holding the box's planes [z0, z0 + depth) as a whole box of
+// its own (no ghost planes), initialised from the bubbles.
+int slab_as_box(lbm_ctx **out, const lbm_params *p, const float *bubbles, int nbubbles, int z0, int depth,
+                const float *maxabs_in, float *maxabs_out)
+{
+    lbm_params q = *p;
+    q.nz = depth;
+    lbm_ctx *c = nullptr;
+    if (int rc = lbm::create_context(&c, &q, 0)) return rc;
+    if (int rc = init_bubbles_into(c, bubbles, nbubbles, z0, maxabs_in, maxabs_out)) {
+        lbm_destroy(c);
+        return rc;
+    }
+    *out = c;
+    return LBM_OK;
+}
+
+}  // namespace
+
 extern "C" int lbm_init_bubbles(lbm_ctx **out, const lbm_params *p, const float *bubbles, int nbubbles)
 {
     const lbm::Range nvtx_range("lbm_init_bubbles");
@@ -320,28 +395,47 @@ extern "C" int lbm_init_bubbles(lbm_ctx **out, const lbm_params *p, const float 
     lbm_ctx *c = nullptr;
     int rc = create(&c, p);
     if (rc) return rc;
-    const size_t n = (size_t)c->box.n, nxy = (size_t)c->box.nxy;
-    float *phig = nullptr, *bub = nullptr;
-    float *mom = c->st.mom;
-    cudaError_t e = cudaMalloc(&phig, sizeof(float) * nxy * (c->box.nz + 2));
-    if (e == cudaSuccess && nbubbles > 0) e = cudaMalloc(&bub, sizeof(float) * 4 * nbubbles);
-    if (e == cudaSuccess && nbubbles > 0)
-        e = cudaMemcpyAsync(bub, bubbles, sizeof(float) * 4 * nbubbles, cudaMemcpyHostToDevice, c->stream);
-    if (e == cudaSuccess)
-        e = lbm::launch_bubble_phi(c->box, bub, nbubbles, c->d.phiStar, c->p.width, phig, c->stream);
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(mom, phig + nxy, sizeof(float) * n, cudaMemcpyDeviceToDevice, c->stream);
-    if (e == cudaSuccess) e = lbm::launch_fill(mom + n, (long long)n, 0.5f * (c->p.rhoH + c->p.rhoL), c->stream);
-    if (e == cudaSuccess) e = cudaMemsetAsync(mom + 2 * n, 0, sizeof(float) * 3 * n, c->stream);
-    rc = e == cudaSuccess ? init_from_mom(c, phig, phig + nxy * (c->box.nz + 1)) : cuda_fail(e, "lbm_init_bubbles");
-    cudaStreamSynchronize(c->stream);
-    if (phig) cudaFree(phig);
-    if (bub) cudaFree(bub);
-    if (rc) {
+    if ((rc = init_bubbles_into(c, bubbles, nbubbles, 0, nullptr, nullptr))) {
         lbm_destroy(c);
         return rc;
     }
     *out = c;
+    return LBM_OK;
+}
+
+extern "C" int lbm_slab_maxabs(const lbm_params *p, const float *bubbles, int nbubbles, int z0, int depth,
+                               float *maxabs)
+{
+    const lbm::Range nvtx_range("lbm_slab_maxabs");
+    if (!maxabs) return fail(LBM_EINVAL, "lbm_slab_maxabs: maxabs is NULL");
+    if (int rc = check_slab_request(p, bubbles, nbubbles, z0, depth)) return rc;
+    LBM_ON_DEVICE(p->device);
+    lbm_ctx *c = nullptr;
+    if (int rc = slab_as_box(&c, p, bubbles, nbubbles, z0, depth, nullptr, maxabs)) return rc;
+    lbm_destroy(c);
+    return LBM_OK;
+}
+
+extern "C" int lbm_slab_init_bubbles(lbm_ctx **out, const lbm_params *p, const float *bubbles, int nbubbles, int z0,
+                                     int depth, const float *maxabs)
+{
+    const lbm::Range nvtx_range("lbm_slab_init_bubbles");
+    if (!out) return fail(LBM_EINVAL, "out is NULL");
+    *out = nullptr;
+    if (int rc = check_slab_request(p, bubbles, nbubbles, z0, depth)) return rc;
+    if (p->storage != LBM_STORAGE_FP32 && !maxabs)
+        return fail(LBM_EINVAL, "lbm_slab_init_bubbles: 16-bit storage needs the box's maxima (lbm_slab_maxabs)");
+    LBM_ON_DEVICE(p->device);
+    lbm_ctx *box = nullptr;
+    if (int rc = slab_as_box(&box, p, bubbles, nbubbles, z0, depth, maxabs, nullptr)) return rc;
+    lbm_ctx *slab = nullptr;
+    const int device = p->device;
+    const int rc = lbm_split_z(box, 1, &depth, &device, &slab);
+    lbm_destroy(box);
+    if (rc) return rc;
+    slab->z0 = z0;
+    slab->nz_total = p->nz;
+    *out = slab;
     return LBM_OK;
 }
 

@@ -120,8 +120,10 @@ const char *physics_error(const lbm_params &p);
 StepConst step_const(const lbm_derived &d, const lbm_params &p, float grav);
 
 // Kernel launchers (defined in the .cu files); all return the cudaError_t of the launch.
+// phi of planes -1 .. nz of the box from the bubble list, the box's plane 0
+// being plane z0 of the bubbles' frame (0 for a whole box).
 cudaError_t launch_bubble_phi(const Box &b, const float *bubbles_dev, int nbubbles, float phiStar, float width,
-                              float *phi_ghosted, cudaStream_t s);
+                              int z0, float *phi_ghosted, cudaStream_t s);
 // At-rest equilibrium into FP32 arrays f_0 (n), f_1..f_6 (6 x n) and g (19 x n),
 // streamed natural layout.
 cudaError_t launch_equilibrium(const Box &b, const lbm_derived &d, float Gamma, const float *phi, const float *rho,

@@ -12,14 +12,16 @@ constexpr float kW1 = 0.05555555555555555556f;
 constexpr float kW2 = 0.02777777777777777778f;
 constexpr float kInv6 = 0.16666666666666666667f;
 
-// phi on nx * ny * (nz + 2) nodes: plane kk is the reference's plane k = kk
-// (the two ghost planes included), x and y 0-based.  For each bubble in file
+// phi on nx * ny * (nz + 2) nodes: plane kk is the reference's plane
+// k = kk + kk0 (the two ghost planes included; kk0 = z0 for a z-slab starting
+// at plane z0 of a larger box, as a rank of the reference sets its own planes
+// from the bubble list), x and y 0-based.  For each bubble in file
 // order, nodes with R <= Rc + width take phiStar * tanh(2 (Rc - R) / width),
 // the others keep -phiStar; the last bubble that covers a node wins.  The
 // distance and the comparison use round-to-nearest float operations without
 // contraction, so the covered set is the one the reference's host code gets.
 __global__ void bubble_phi_kernel(Box b, const float *__restrict__ bubbles, int nbubbles, float phiStar,
-                                  float width, float *__restrict__ phig)
+                                  float width, int kk0, float *__restrict__ phig)
 {
     const long long total = b.nxy * (long long)(b.nz + 2);
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
@@ -33,7 +35,7 @@ __global__ void bubble_phi_kernel(Box b, const float *__restrict__ bubbles, int 
             const float zc = __ldg(bubbles + 4 * m + 2), rc = __ldg(bubbles + 4 * m + 3);
             const float dx = __fsub_rn((float)i, xc);
             const float dy = __fsub_rn((float)j, yc);
-            const float dz = __fsub_rn((float)kk, zc);
+            const float dz = __fsub_rn((float)(kk + kk0), zc);
             const float s = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
             const float R = __fsqrt_rn(s);
             if (R <= __fadd_rn(rc, width)) v = phiStar * tanhf(__fdiv_rn(2.f * __fsub_rn(rc, R), width));
@@ -96,9 +98,9 @@ unsigned grid_for(long long n)
 }  // namespace
 
 cudaError_t launch_bubble_phi(const Box &b, const float *bubbles_dev, int nbubbles, float phiStar, float width,
-                              float *phi_ghosted, cudaStream_t s)
+                              int z0, float *phi_ghosted, cudaStream_t s)
 {
-    bubble_phi_kernel<<<grid_for(b.nxy * (b.nz + 2)), 256, 0, s>>>(b, bubbles_dev, nbubbles, phiStar, width,
+    bubble_phi_kernel<<<grid_for(b.nxy * (b.nz + 2)), 256, 0, s>>>(b, bubbles_dev, nbubbles, phiStar, width, z0,
                                                                     phi_ghosted);
     return cudaGetLastError();
 }

@@ -257,3 +257,29 @@ def test_stats_combine_adds_sums_and_counts_and_takes_maxima(lib):
     assert s["uz_av"] == pytest.approx(r[4] / r[1])
     assert s["p_in"] == pytest.approx(r[5] / r[1]) and s["p_out"] == pytest.approx(r[6] / (n - r[1]))
     assert s["phi_sum"] == r[7] and s["rho_sum"] == r[8] and s["mom_z"] == r[11]
+
+
+def test_slab_init_rejects_bad_requests_without_touching_the_gpu(lib):
+    """lbm_slab_maxabs / lbm_slab_init_bubbles check the slab's planes and the
+    16-bit maxima before any CUDA call."""
+    import ctypes as C
+    from lbm_bench_gpu_gb300 import capi
+    lib_ = capi.load()
+    BUB = np.array([[30.3, 14.2, 21.7, 9.0], [8.5, 22.1, 40.2, 6.0], [50.0, 8.0, 3.5, 5.0]], np.float32)
+
+    def params(shape, storage):
+        return capi.make_params(*shape, storage=storage, rhoL=0.1, rhoH=1.0, tauRho=0.8, tauPhi=0.9, width=4.0,
+                                sigma=1e-3, Gamma=1.0, Eo=-0.8, rc0=9.0)
+
+    m = np.zeros(26, np.float32)
+    h = C.c_void_p()
+    for storage in ("fp32", "fp16"):
+        p = params((64, 32, 48), storage)
+        for z0, depth in ((-1, 8), (40, 9), (0, 1), (47, 2)):
+            assert lib_.lbm_slab_maxabs(C.byref(p), capi.fptr(BUB), 3, z0, depth, capi.fptr(m)) == capi.LBM_EINVAL
+            assert lib_.lbm_slab_init_bubbles(C.byref(h), C.byref(p), capi.fptr(BUB), 3, z0, depth,
+                                              capi.fptr(m)) == capi.LBM_EINVAL
+    # 16-bit storage without the box's maxima
+    p = params((64, 32, 48), "fp16")
+    assert lib_.lbm_slab_init_bubbles(C.byref(h), C.byref(p), capi.fptr(BUB), 3, 0, 24, None) == capi.LBM_EINVAL
+    assert not h.value

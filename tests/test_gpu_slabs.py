@@ -57,6 +57,28 @@ def test_slabs_step_like_the_whole_box(lib, storage, depths):
         assert s[k] == pytest.approx(sr[k], rel=1e-9, abs=1e-15), k
 
 
+@pytest.mark.parametrize("storage", ["fp32", "fp16", "bf16"])
+@pytest.mark.parametrize("depths", [(20, 12, 16), (24, 24)])
+def test_slabs_built_on_their_own_equal_the_split(lib, storage, depths):
+    """lbm_slab_maxabs + lbm_slab_init_bubbles (each slab from the bubble list,
+    the 16-bit maxima reduced over the slabs) give the slabs lbm_split_z makes
+    of lbm_init_bubbles's whole box, bit for bit (the bubbles cross the slab
+    boundaries and the box's bottom plane), and they step on like it."""
+    from lbm_bench_gpu_gb300 import capi
+    p = params((64, 32, 48), storage)
+    grav = float(capi.derive(p).grav)
+    with capi.Lattice.from_bubbles(p, BUB) as ref, capi.Lattice.from_bubbles(p, BUB) as target:
+        target.step(3, grav)      # overwritten by the merge
+        with capi.Slabs.from_bubbles(p, BUB, depths) as slabs:
+            slabs.merge_into(target)
+            assert target.steps == 0
+            assert_same_state(target, ref, f"init {storage} {depths}")
+            slabs.step(7, grav)
+            ref.step(7, grav)
+            slabs.merge_into(target)
+        assert_same_state(target, ref, f"7 steps {storage} {depths}")
+
+
 def test_slab_rejects_whole_box_calls(lib):
     from lbm_bench_gpu_gb300 import capi
     p = params((64, 32, 48), "fp32")

@@ -50,3 +50,36 @@ def test_rounded_run_stays_near_the_fp64_run(fmt, bound):
         o.close()
     err = np.linalg.norm(runs[1] - runs[0]) / np.linalg.norm(runs[0])
     assert 0.0 < err < bound
+
+
+def test_bf16_phi_error_comes_from_the_momentum_set():
+    """Which 16-bit set drives BF16's phi error: with the momentum set g in
+    BF16 (f_1..f_6 in FP16) phi ends far further from the FP64 run than with
+    f_1..f_6 in BF16 (g in FP16), while f in BF16 drives the drift of sum(phi).
+    24^3, one bubble rising under gravity, 1000 steps, the library's shifts and
+    scales (64^3 x 10 000 steps: phi L2 2.1e-2 vs 5.3e-4, drift of sum(phi)
+    1.3e-6 vs 5.5e-5)."""
+    bub = np.array([[12.3, 11.2, 10.7, 6.0]], np.float32)
+    w = np.array([1 / 3] + [1 / 18] * 6 + [1 / 36] * 12)
+
+    def run(f_fmt, g_fmt):
+        o = Oracle(24, 24, 24, **PHYS)
+        o.init_bubbles(bub)
+        if f_fmt != "none":
+            shift = w * o.moments()["rho"].mean()
+            fs = 32768.0 if f_fmt == "fp16" else 1.0
+            gs = 65536.0 if g_fmt == "fp16" else 1.0
+            o.set_rounding(f0="fp32", f=f_fmt, f_scale=fs, g=g_fmt, g_scale=gs, g_shift=shift)
+        o.step(1000, -2e-5)
+        out = (o.moments()["phi"], o.stats()["phi_sum"])
+        o.close()
+        return out
+
+    phi64, sum64 = run("none", "none")
+    errs = {}
+    for f_fmt, g_fmt in (("fp16", "bf16"), ("bf16", "fp16")):
+        phi, s = run(f_fmt, g_fmt)
+        errs[(f_fmt, g_fmt)] = (np.linalg.norm(phi - phi64) / np.linalg.norm(phi64), abs(s - sum64) / abs(sum64))
+    g_bf16, f_bf16 = errs[("fp16", "bf16")], errs[("bf16", "fp16")]
+    assert g_bf16[0] > 5 * f_bf16[0], errs
+    assert f_bf16[1] > 5 * g_bf16[1], errs

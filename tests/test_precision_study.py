@@ -12,7 +12,10 @@ report is also written to $LBM_REPORT_DIR/precision_study.json when that
 variable names a directory.
 Bar: relative phi L2 error <= 1e-3 for FP32 and FP16 storage.  BF16 (8-bit
 mantissa) is reported, with a looser sanity bound: its phi error after 10 000
-steps is ~2e-2 relative, driven by the rounding of f_1..f_6."""
+steps is ~2e-2 relative, driven by the rounding of the momentum set g (the
+oracle's storage-rounding emulation, tests/test_oracle_rounding.py, splits it:
+FP16 f_1..f_6 with BF16 g stay at 2.1e-2, BF16 f_1..f_6 with FP16 g reach
+5.3e-4)."""
 from __future__ import annotations
 
 import json
