@@ -421,7 +421,7 @@ struct Adjoint {
         lst[1] = w.take<float>(n);
         lsrc = w.take<float4>(n);
         phi0 = w.take<float>(n);
-        dgrav = w.take<double>(nblocks);
+        dgrav = w.take<double>(lbm::adjoint_dgrav_parts(c->box));
     }
 };
 
@@ -571,7 +571,8 @@ extern "C" int lbm_step_adjoint(lbm_ctx *c, const lbm_adjoint_opts *o, lbm_adjoi
     for (long long s = nslots - 1; s >= 1; s--) A.free_slots.push_back((int)s);
 
     e = cudaMemsetAsync(A.acc, 0, sizeof(double) * 2, c->stream);
-    if (e == cudaSuccess) e = cudaMemsetAsync(A.dgrav, 0, sizeof(double) * nblocks, c->stream);
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(A.dgrav, 0, sizeof(double) * lbm::adjoint_dgrav_parts(c->box), c->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(A.phi0, c->st.mom, sizeof(float) * n, cudaMemcpyDeviceToDevice, c->stream);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(A.mom_save, c->st.mom, sizeof(float) * 5 * n, cudaMemcpyDeviceToDevice, c->stream);

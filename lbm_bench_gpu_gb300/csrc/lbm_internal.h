@@ -106,7 +106,7 @@ struct AdjointBuffers {
     const float *lst_in;               //   stencil term of lambda^{n+1}, common to the 7 f fields
     float *lf_out, *lg_out, *lst_out;  // lambda^n
     float4 *lsrc;                      // scratch per node: (lambda_lap, mu lambda_F)
-    double *dgrav;                     // per-block running sums of the dJ/dgrav terms
+    double *dgrav;                     // per-warp running sums of the dJ/dgrav terms
     const double *ab;                  // objective sums of s^n
 };
 
@@ -157,6 +157,8 @@ cudaError_t launch_pressure(const Box &b, const lbm_derived &d, const float *mom
 // marching a few z planes; adjoint_blocks is its block count (the length of
 // the dgrav array, and half the length of the objective partials).
 size_t adjoint_blocks(const Box &b);
+// Length of the dgrav array: one running sum per warp of the local kernel's grid.
+size_t adjoint_dgrav_parts(const Box &b);
 cudaError_t launch_adjoint_phi(const Box &b, float eta, const Quant &q, const NativeState &st, float *phi,
                                cudaStream_t s);
 cudaError_t launch_objective(const Box &b, int objective, float phiStar, double scale, const Quant &q,
@@ -168,7 +170,7 @@ cudaError_t launch_source_init(const Box &b, int objective, double scale, const 
 cudaError_t launch_adjoint_step(const Box &b, const StepConst &c, float phiStar, const Quant &q,
                                 const NativeState &st, const AdjointBuffers &a, bool add_source, int objective,
                                 double scale, cudaStream_t s);
-// acc[1] = sum of the per-block dgrav sums.
+// acc[1] = sum of the per-warp dgrav sums.
 cudaError_t launch_dgrav_fold(const Box &b, const double *dgrav, double *acc, cudaStream_t s);
 cudaError_t launch_init_adjoint(const Box &b, const lbm_derived &d, float Gamma, const float *phi0, const float *lf,
                                 const float *lst, const float *lg, float *lphi0, float *llap, cudaStream_t s);
