@@ -1,0 +1,76 @@
+"""The storage-precision study on the benchmark's own box: 256^3, 64 bubbles
+(the bench workload, radii U[6, 10], seeded), 10 000 steps under gravity, FP32,
+FP16 and BF16 storage against the FP64 oracle run of the same steps.
+
+Reported per format: phi L2 relative error, relative drift of sum(phi) and
+sum(rho) against the oracle, and the largest distance between matching
+heavy-phase centroids (the per-format JSON goes to
+$LBM_REPORT_DIR/precision_study_256.json).  Bar: phi L2 <= 1e-3 for FP32 and
+FP16; BF16 reported with a sanity bound.
+
+The FP64 oracle needs ~50 minutes of 16 host cores for 10 000 steps at 256^3,
+so this runs only when LBM_SLOW_TESTS=1 is set."""
+from __future__ import annotations
+
+import json
+import os
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from oracle.oracle import Oracle
+
+pytestmark = pytest.mark.gpu
+
+STEPS = int(os.environ.get("LBM_PRECISION_STEPS", "10000"))
+
+
+@pytest.mark.skipif(os.environ.get("LBM_SLOW_TESTS") != "1",
+                    reason="FP64 oracle at 256^3 for 10 000 steps (~50 min): set LBM_SLOW_TESTS=1")
+def test_storage_precision_at_256cube(lib):
+    pytest.importorskip("scipy")
+    from test_precision_study import centroids
+    from lbm_bench_gpu_gb300 import capi, inputs
+    inp = inputs.bubbly(256, 64)
+    base = dict(rhoL=inp.rhoL, rhoH=inp.rhoH, tauRho=inp.tauRho, tauPhi=inp.tauPhi, width=inp.width,
+                sigma=inp.sigma, Gamma=inp.Gamma, Eo=inp.Eo, rc0=inp.rc0)
+    p32 = capi.make_params(256, 256, 256, **base)
+    grav = float(capi.derive(p32).grav)
+
+    runs = {}
+    for storage in ("fp32", "fp16", "bf16"):
+        p = capi.make_params(256, 256, 256, storage=storage, **base)
+        with capi.Lattice.from_bubbles(p, inp.bubbles) as lat:
+            lat.step(STEPS, grav)
+            s, f = lat.stats(fields=True)
+        runs[storage] = (s, f["phi"].copy())
+        del f
+
+    o = Oracle.from_params(p32)
+    o.init_bubbles(inp.bubbles)
+    o.step(STEPS, grav)
+    ref_phi = o.moments()["phi"]
+    ref_stats = o.stats()
+    o.close()
+    ref_c = centroids(ref_phi)
+    norm = np.linalg.norm(ref_phi)
+
+    report = {"box": "256^3, 64 bubbles R~U[6,10] (bench workload), gravity -1e-6", "steps": STEPS,
+              "oracle_bubbles": int(len(ref_c)), "formats": {}}
+    for storage, (s, phi) in runs.items():
+        d = phi.astype(np.float64) - ref_phi
+        cg = centroids(phi)
+        report["formats"][storage] = {
+            "phi_l2_rel": float(np.linalg.norm(d) / norm),
+            "mass_phi_drift_rel": abs(s["phi_sum"] - ref_stats["phi_sum"]) / abs(ref_stats["phi_sum"]),
+            "mass_rho_drift_rel": abs(s["rho_sum"] - ref_stats["rho_sum"]) / abs(ref_stats["rho_sum"]),
+            "centroid_err_max": float(np.abs(cg - ref_c).max()) if cg.shape == ref_c.shape else None,
+            "bubbles": int(len(cg)),
+        }
+    out = Path(os.environ.get("LBM_REPORT_DIR", ""))
+    if os.environ.get("LBM_REPORT_DIR") and out.is_dir():
+        (out / "precision_study_256.json").write_text(json.dumps(report, indent=1))
+    print(json.dumps(report))
+    for storage, r in report["formats"].items():
+        assert r["phi_l2_rel"] <= (1e-3 if storage != "bf16" else 5e-2), (storage, r)
