@@ -91,16 +91,30 @@ int create_context(lbm_ctx **out, const lbm_params *p, int zghost)
     c->box.nf = c->box.nxy * (p->nz + (zghost ? 4 : 0));
     c->box.ng = c->box.nxy * (p->nz + (zghost ? 2 : 0));
     const size_t n = (size_t)c->box.n, nf = (size_t)c->box.nf, ng = (size_t)c->box.ng;
-    cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaMalloc(&c->st.f0, sizeof(float) * 2 * nf);
-    if (e == cudaSuccess) e = cudaMalloc(&c->st.fq, c->esz * 2 * (lbm::kQf - 1) * nf);
-    if (e == cudaSuccess) e = cudaMalloc(&c->st.g, c->esz * lbm::kQg * ng);
-    if (e == cudaSuccess) e = cudaMalloc(&c->st.mom, sizeof(float) * 5 * n);
     c->partial_count = lbm::stats_partial_count(c->box);
-    if (e == cudaSuccess) e = cudaMalloc(&c->partials, sizeof(double) * lbm::kStatsValues * c->partial_count);
-    if (e == cudaSuccess) e = cudaMalloc(&c->result, sizeof(double) * lbm::kStatsValues);
+    // the device buffers, 256-byte aligned pieces of one allocation (the TMA
+    // tensor maps need 16-byte aligned field bases)
+    const size_t sizes[7] = {sizeof(float) * 2 * nf, c->esz * 2 * (lbm::kQf - 1) * nf, c->esz * lbm::kQg * ng,
+                             sizeof(float) * 5 * n, sizeof(double) * lbm::kStatsValues * c->partial_count,
+                             sizeof(double) * lbm::kStatsValues, sizeof(int)};
+    size_t offs[7], total = 0;
+    for (int k = 0; k < 7; k++) {
+        offs[k] = total;
+        total += (sizes[k] + 255) & ~(size_t)255;
+    }
+    cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&c->arena, total);
+    if (e == cudaSuccess) {
+        unsigned char *a = static_cast<unsigned char *>(c->arena);
+        c->st.f0 = reinterpret_cast<float *>(a + offs[0]);
+        c->st.fq = a + offs[1];
+        c->st.g = a + offs[2];
+        c->st.mom = reinterpret_cast<float *>(a + offs[3]);
+        c->partials = reinterpret_cast<double *>(a + offs[4]);
+        c->result = reinterpret_cast<double *>(a + offs[5]);
+        c->err = reinterpret_cast<int *>(a + offs[6]);
+    }
     if (e == cudaSuccess) e = cudaMallocHost(&c->result_host, sizeof(double) * lbm::kStatsValues);
-    if (e == cudaSuccess) e = cudaMalloc(&c->err, sizeof(int));
     if (e == cudaSuccess) e = cudaMemsetAsync(c->err, 0, sizeof(int), c->stream);
     if (e != cudaSuccess) {
         lbm_destroy(c);
@@ -296,25 +310,44 @@ extern "C" int lbm_init(lbm_ctx **out, const lbm_params *p, const float *phi0, c
     const size_t n = (size_t)c->box.n, bytes = sizeof(float) * n;
     float *mom = c->st.mom;
     float *ghost = nullptr;
-    cudaError_t e = cudaMemcpyAsync(mom, phi0, bytes, cudaMemcpyHostToDevice, c->stream);
+    // The at-rest equilibrium reads phi and rho only (src/init_f.cu,
+    // src/init_g.cu), so u goes up on a second stream while the FP32
+    // equilibrium runs; the 16-bit storage map reads all five fields first.
+    cudaStream_t side = nullptr;
+    cudaEvent_t u_done = nullptr;
+    cudaError_t e = cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&u_done, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(mom, phi0, bytes, cudaMemcpyHostToDevice, c->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(mom + n, rho0, bytes, cudaMemcpyHostToDevice, c->stream);
     const float *u[3] = {ux0, uy0, uz0};
     for (int a = 0; a < 3 && e == cudaSuccess; a++) {
-        if (u[a]) e = cudaMemcpyAsync(mom + (2 + a) * n, u[a], bytes, cudaMemcpyHostToDevice, c->stream);
-        else e = cudaMemsetAsync(mom + (2 + a) * n, 0, bytes, c->stream);
+        if (u[a]) e = cudaMemcpyAsync(mom + (2 + a) * n, u[a], bytes, cudaMemcpyHostToDevice, side);
+        else e = cudaMemsetAsync(mom + (2 + a) * n, 0, bytes, side);
     }
+    if (e == cudaSuccess) e = cudaEventRecord(u_done, side);
+    if (e == cudaSuccess && c->p.storage != LBM_STORAGE_FP32) e = cudaStreamWaitEvent(c->stream, u_done, 0);
     if (e == cudaSuccess && phi_ghost) {
         e = cudaMalloc(&ghost, sizeof(float) * 2 * c->box.nxy);
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(ghost, phi_ghost, sizeof(float) * 2 * c->box.nxy, cudaMemcpyHostToDevice, c->stream);
     }
+    auto release_side = [&]() {
+        if (side) cudaStreamSynchronize(side);
+        if (u_done) cudaEventDestroy(u_done);
+        if (side) cudaStreamDestroy(side);
+    };
     if (e != cudaSuccess) {
         cudaStreamSynchronize(c->stream);
+        release_side();
         if (ghost) cudaFree(ghost);
         lbm_destroy(c);
         return cuda_fail(e, "lbm_init");
     }
     rc = init_from_mom(c, ghost, ghost ? ghost + c->box.nxy : nullptr);
+    // the context's later work follows u's upload
+    const cudaError_t ew = cudaStreamWaitEvent(c->stream, u_done, 0);
+    if (ew != cudaSuccess && !rc) rc = cuda_fail(ew, "lbm_init");
+    release_side();
     if (ghost) cudaFree(ghost);
     if (rc) {
         lbm_destroy(c);
@@ -737,13 +770,7 @@ extern "C" void lbm_destroy(lbm_ctx *c)
     if (!c) return;
     const lbm::DeviceGuard device_guard(c->p.device);
     if (c->stream) cudaStreamSynchronize(c->stream);
-    cudaFree(c->st.f0);
-    cudaFree(c->st.fq);
-    cudaFree(c->st.g);
-    cudaFree(c->st.mom);
-    cudaFree(c->partials);
-    cudaFree(c->result);
-    cudaFree(c->err);
+    cudaFree(c->arena);   // st.f0, st.fq, st.g, st.mom, partials, result, err
     cudaFree(c->adj_work);
     cudaFree(c->adj_slots);
     cudaFree(c->halo_send);

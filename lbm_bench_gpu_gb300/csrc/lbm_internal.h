@@ -194,6 +194,9 @@ struct lbm_ctx {
     double *result = nullptr;      // stats result (device)
     double *result_host = nullptr; // pinned copy
     int *err = nullptr;            // device error flag of the kernels (0 = none)
+    // one device allocation holding st.f0, st.fq, st.g, st.mom, partials,
+    // result and err (one cudaMalloc per context instead of seven)
+    void *arena = nullptr;
     // adjoint workspace, kept between lbm_step_adjoint / lbm_objective calls
     // (freeing tens of GB costs ~0.4 ms per GB) until lbm_adjoint_release or
     // lbm_destroy: the work buffers as one arena, and the checkpoint pool
