@@ -5,8 +5,8 @@
  *
  * The reference (carlosrosales/lbm_bench_gpu) has no library boundary: its
  * driver src/main.cu allocates ~40 device arrays, copies constants with
- * cudaMemcpyToSymbol and launches nine kernels plus three host-staged halo
- * exchanges per step.  Each entry point below replaces one stage of that
+ * cudaMemcpyToSymbol and launches thirteen kernels (seven compute, six
+ * pack/unpack) plus three host-staged halo exchanges per step.  Each entry point below replaces one stage of that
  * driver; the citation next to it names the reference lines it stands for.
  *
  * Conventions
@@ -348,6 +348,18 @@ int lbm_halo_unpack(lbm_ctx *slab, int phase, const void *recv_lo, const void *r
  * an odd step the LBM_HALO_POST exchange follows.  Writes the phi, rho, u
  * fields.  Asynchronous. */
 int lbm_slab_step_local(lbm_ctx *slab, float grav);
+
+/* The same step in two parts, so that the halo planes move while the slab
+ * computes: lbm_slab_step_interior steps planes [2, nz - 2), which read
+ * nothing the LBM_HALO_PRE exchange brings and write nothing it moves, and
+ * may be queued between lbm_halo_pack and lbm_halo_unpack of that exchange
+ * (and while the last step's LBM_HALO_POST exchange is still under way);
+ * lbm_slab_step_boundary steps planes [0, 2) and [nz - 2, nz) after the
+ * unpack (and after the LBM_HALO_POST exchange of the last step).  Once
+ * each, in that order (LBM_ESTATE otherwise).  Asynchronous.  lbm_slab_step
+ * runs its steps this way. */
+int lbm_slab_step_interior(lbm_ctx *slab, float grav);
+int lbm_slab_step_boundary(lbm_ctx *slab, float grav);
 
 /* The 16 raw FP64 sums and maxima behind lbm_stats_out of a context's phi,
  * rho, u fields (layout of lbm_stats_noalloc's raw_out), for combining over

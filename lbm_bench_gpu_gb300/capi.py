@@ -27,7 +27,7 @@ EXPORTS = [
     "lbm_wait_selftest", "lbm_adjoint_forward_steps", "lbm_state_bytes", "lbm_save_state", "lbm_load_state",
     "lbm_split_z", "lbm_merge_z", "lbm_slab_step", "lbm_halo_bytes", "lbm_halo_pack", "lbm_halo_unpack",
     "lbm_slab_step_local", "lbm_stats_raw", "lbm_stats_combine", "lbm_slab_stats", "lbm_slab_maxabs",
-    "lbm_slab_init_bubbles",
+    "lbm_slab_init_bubbles", "lbm_slab_step_interior", "lbm_slab_step_boundary",
 ]
 OBJECTIVES = {"light_uz_mean": 0, "light_z_centroid": 1}
 
@@ -148,6 +148,8 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.lbm_halo_pack.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
     lib.lbm_halo_unpack.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
     lib.lbm_slab_step_local.argtypes = [C.c_void_p, C.c_float]
+    lib.lbm_slab_step_interior.argtypes = [C.c_void_p, C.c_float]
+    lib.lbm_slab_step_boundary.argtypes = [C.c_void_p, C.c_float]
     lib.lbm_stats_raw.argtypes = [C.c_void_p, _D]
     lib.lbm_stats_combine.argtypes = [C.POINTER(Params), C.c_longlong, _D, C.c_int, C.POINTER(StatsOut)]
     lib.lbm_slab_stats.argtypes = [_V, C.c_int, C.POINTER(StatsOut)]

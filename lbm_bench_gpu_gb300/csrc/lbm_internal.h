@@ -130,8 +130,10 @@ cudaError_t launch_equilibrium(const Box &b, const lbm_derived &d, float Gamma, 
                                const float *ghost_lo, const float *ghost_hi, float *f0, float *fq, float *g,
                                cudaStream_t s);
 cudaError_t launch_fill(float *p, long long n, float v, cudaStream_t s);
+// One step of the state in v; a z-slab (Box::zghost) may step planes
+// [zlo, zhi) of it only (zhi < 0: all), a periodic box steps whole.
 cudaError_t launch_step(const Box &b, const StepConst &c, const Quant &q, const StepView &v, bool f_streamed,
-                        bool odd, bool write_moments, cudaStream_t s);
+                        bool odd, bool write_moments, cudaStream_t s, int zlo = 0, int zhi = -1);
 // One block whose bounded mbarrier wait gives up and sets *err (the step's wait).
 cudaError_t launch_wait_selftest(int *err, cudaStream_t s);
 // State (post-collision / AA layout, any storage) -> streamed FP32 f (7 x n) and g (19 x n).
@@ -211,6 +213,7 @@ struct lbm_ctx {
     // and whether the last step was odd (its ghost-plane g writes still have
     // to reach the neighbours)
     int z0 = 0, nz_total = 0;
+    bool interior_done = false;    // lbm_slab_step_interior ran, the boundary part of the step not yet
     void *halo_send = nullptr;
     size_t halo_bytes = 0;
     float *phi_ghost = nullptr;

@@ -140,28 +140,62 @@ int check_phase(int phase, const char *what)
     return LBM_OK;
 }
 
-// One step of a slab whose LBM_HALO_PRE exchange is done.
-int slab_step(lbm_ctx *c, float grav, bool write_moments)
+// The planes of a step.  The interior planes [2, nz - 2) read nothing the
+// LBM_HALO_PRE exchange brings (phi of a plane needs the f planes up to two
+// away, an odd step's g the planes one away) and write nothing it moves, so
+// they can step while the halo planes are in flight; the boundary planes
+// [0, 2) and [nz - 2, nz) step after it.  The in-place g update touches every
+// memory slot from one node only, so the parts can run as separate launches.
+struct Planes {
+    int lo, hi;
+};
+Planes interior(const lbm_ctx *c) { return c->box.nz > 4 ? Planes{2, c->box.nz - 2} : Planes{2, 2}; }
+void boundary(const lbm_ctx *c, Planes out[2])
 {
+    const int nz = c->box.nz, lo_end = nz < 2 ? nz : 2;
+    out[0] = Planes{0, lo_end};
+    out[1] = Planes{nz - 2 > lo_end ? nz - 2 : lo_end, nz};
+}
+
+// Launch the step kernel of the slab's current state over planes [r.lo, r.hi).
+int slab_launch(lbm_ctx *c, float grav, bool write_moments, Planes r)
+{
+    if (r.lo >= r.hi) return LBM_OK;
     const lbm::StepConst k = lbm::step_const(c->d, c->p, grav);
+    cudaError_t e = lbm::launch_step(c->box, k, c->q, lbm::state_view(c, c->st.f_cur), c->st.f_streamed,
+                                     c->st.g_odd_next, write_moments, c->stream, r.lo, r.hi);
+    return e == cudaSuccess ? LBM_OK : cuda_fail(e, "slab step kernel launch");
+}
+
+// The state after a step's launches.
+void slab_advance(lbm_ctx *c)
+{
     const bool odd = c->st.g_odd_next;
-    const int in = c->st.f_cur;
-    cudaError_t e = lbm::launch_step(c->box, k, c->q, lbm::state_view(c, in), c->st.f_streamed, odd,
-                                     write_moments, c->stream);
-    if (e != cudaSuccess) return cuda_fail(e, "slab step kernel launch");
-    c->st.f_cur = 1 - in;
+    c->st.f_cur = 1 - c->st.f_cur;
     c->st.f_streamed = false;
     c->st.g_odd_next = !odd;
     c->st.steps++;
     c->post_pending = odd;
+    c->interior_done = false;
+}
+
+// The boundary planes of a step whose interior ran, and the state update.
+int slab_finish(lbm_ctx *c, float grav, bool write_moments)
+{
+    Planes b[2];
+    boundary(c, b);
+    for (const Planes &r : b)
+        if (int rc = slab_launch(c, grav, write_moments, r)) return rc;
+    slab_advance(c);
     return LBM_OK;
 }
 
 // Halo exchange of one phase between the slabs of one process: every slab
 // packs its two sides into its own buffer (after its neighbours finished
 // reading that buffer), then unpacks what its neighbours packed.  All writes
-// to a slab's memory happen on its own stream.
-int exchange(lbm_ctx *const *s, int n, int phase)
+// to a slab's memory happen on its own stream.  exchange_pack and
+// exchange_unpack are the two halves (a step's interior goes between them).
+int exchange_pack(lbm_ctx *const *s, int n, int phase)
 {
     for (int k = 0; k < n; k++) {
         lbm_ctx *c = s[k];
@@ -174,6 +208,11 @@ int exchange(lbm_ctx *const *s, int n, int phase)
         if (int rc = copy_runs(c, phase, 1, true, buf + c->halo_bytes)) return rc;
         LBM_CUDA(cudaEventRecord(c->ev_pack, c->stream), "halo order");
     }
+    return LBM_OK;
+}
+
+int exchange_unpack(lbm_ctx *const *s, int n, int phase)
+{
     for (int k = 0; k < n; k++) {
         lbm_ctx *c = s[k];
         LBM_ON_DEVICE(c->p.device);
@@ -190,6 +229,12 @@ int exchange(lbm_ctx *const *s, int n, int phase)
     if (phase == LBM_HALO_POST)
         for (int k = 0; k < n; k++) s[k]->post_pending = false;
     return LBM_OK;
+}
+
+int exchange(lbm_ctx *const *s, int n, int phase)
+{
+    if (int rc = exchange_pack(s, n, phase)) return rc;
+    return exchange_unpack(s, n, phase);
 }
 
 int check_slabs(lbm_ctx *const *s, int n, const char *what)
@@ -362,6 +407,32 @@ extern "C" int lbm_halo_unpack(lbm_ctx *slab, int phase, const void *recv_lo, co
     return LBM_OK;
 }
 
+extern "C" int lbm_slab_step_interior(lbm_ctx *slab, float grav)
+{
+    const lbm::Range nvtx_range("lbm_slab_step_interior");
+    if (int rc = check_slab(slab, "lbm_slab_step_interior")) return rc;
+    if (!std::isfinite(grav)) return fail(LBM_EINVAL, "grav is not finite");
+    if (slab->interior_done)
+        return fail(LBM_ESTATE, "lbm_slab_step_interior: the boundary part of the last step is missing");
+    LBM_ON_DEVICE(slab->p.device);
+    if (int rc = slab_launch(slab, grav, true, interior(slab))) return rc;
+    slab->interior_done = true;
+    return LBM_OK;
+}
+
+extern "C" int lbm_slab_step_boundary(lbm_ctx *slab, float grav)
+{
+    const lbm::Range nvtx_range("lbm_slab_step_boundary");
+    if (int rc = check_slab(slab, "lbm_slab_step_boundary")) return rc;
+    if (!std::isfinite(grav)) return fail(LBM_EINVAL, "grav is not finite");
+    if (!slab->interior_done)
+        return fail(LBM_ESTATE, "lbm_slab_step_boundary: lbm_slab_step_interior of this step is missing");
+    if (slab->post_pending)
+        return fail(LBM_ESTATE, "lbm_slab_step_boundary: the LBM_HALO_POST exchange of the last (odd) step is missing");
+    LBM_ON_DEVICE(slab->p.device);
+    return slab_finish(slab, grav, true);
+}
+
 extern "C" int lbm_slab_step_local(lbm_ctx *slab, float grav)
 {
     const lbm::Range nvtx_range("lbm_slab_step_local");
@@ -369,8 +440,11 @@ extern "C" int lbm_slab_step_local(lbm_ctx *slab, float grav)
     if (!std::isfinite(grav)) return fail(LBM_EINVAL, "grav is not finite");
     if (slab->post_pending)
         return fail(LBM_ESTATE, "lbm_slab_step_local: the LBM_HALO_POST exchange of the last (odd) step is missing");
+    if (slab->interior_done)
+        return fail(LBM_ESTATE, "lbm_slab_step_local: the boundary part of the last step is missing");
     LBM_ON_DEVICE(slab->p.device);
-    return slab_step(slab, grav, true);
+    if (int rc = slab_launch(slab, grav, true, interior(slab))) return rc;
+    return slab_finish(slab, grav, true);
 }
 
 extern "C" int lbm_slab_step(lbm_ctx *const *slabs, int nslabs, int nsteps, float grav)
@@ -380,15 +454,26 @@ extern "C" int lbm_slab_step(lbm_ctx *const *slabs, int nslabs, int nsteps, floa
     if (nsteps < 0) return fail(LBM_EINVAL, "nsteps < 0");
     if (!std::isfinite(grav)) return fail(LBM_EINVAL, "grav is not finite");
     for (int k = 0; k < nslabs; k++)
+        if (slabs[k]->interior_done)
+            return fail(LBM_ESTATE, "lbm_slab_step: a slab is between lbm_slab_step_interior and _boundary");
+    for (int k = 0; k < nslabs; k++)
         if (slabs[k]->post_pending) {
             if (int rc = exchange(slabs, nslabs, LBM_HALO_POST)) return rc;
             break;
         }
     for (int t = 0; t < nsteps; t++) {
-        if (int rc = exchange(slabs, nslabs, LBM_HALO_PRE)) return rc;
+        const bool wm = t == nsteps - 1;
+        // pack the halo planes, step the interiors while the neighbours'
+        // planes come in, then the boundary planes
+        if (int rc = exchange_pack(slabs, nslabs, LBM_HALO_PRE)) return rc;
         for (int k = 0; k < nslabs; k++) {
             LBM_ON_DEVICE(slabs[k]->p.device);
-            if (int rc = slab_step(slabs[k], grav, t == nsteps - 1)) return rc;
+            if (int rc = slab_launch(slabs[k], grav, wm, interior(slabs[k]))) return rc;
+        }
+        if (int rc = exchange_unpack(slabs, nslabs, LBM_HALO_PRE)) return rc;
+        for (int k = 0; k < nslabs; k++) {
+            LBM_ON_DEVICE(slabs[k]->p.device);
+            if (int rc = slab_finish(slabs[k], grav, wm)) return rc;
         }
         if (slabs[0]->post_pending)
             if (int rc = exchange(slabs, nslabs, LBM_HALO_POST)) return rc;

@@ -366,7 +366,7 @@ __device__ __forceinline__ unsigned node_index(const StepBox &b, int x, int y, i
 template <typename ST, bool STREAMED, bool ODD, bool TMA, bool ZG>
 __global__ void __launch_bounds__(threads_of<ST>(), Fmt<ST>::kMinBlocks)
 zsc_step_kernel(const StepPtrs<ST> P, const StepBox b, const StepConst c, const StepMap m, const int tz,
-                const int write_moments, const __grid_constant__ CUtensorMap gmap,
+                const int write_moments, const int zlo, const int zhi, const __grid_constant__ CUtensorMap gmap,
                 const __grid_constant__ CUtensorMap f0map, const __grid_constant__ CUtensorMap fqmap)
 {
     using Gm = Geo<ST>;
@@ -389,8 +389,10 @@ zsc_step_kernel(const StepPtrs<ST> P, const StepBox b, const StepConst c, const 
     bid /= ntx;
     const int by = bid % nty;
     bid /= nty;
-    const int z0 = bid * tz;
-    const int nzc = min(tz, b.nz - z0);       // planes of this chunk
+    // a z-slab launch may cover planes [zlo, zhi) only (its interior while the
+    // halo planes are in flight, then its boundary planes)
+    const int z0 = (ZG ? zlo : 0) + bid * tz;
+    const int nzc = min(tz, (ZG ? zhi : b.nz) - z0);   // planes of this chunk
     const int x0 = bx * TX, y0 = by * TY;
     const int x = x0 + XPT * tx, y = y0 + ty;   // (first) node of the thread
 
@@ -1312,7 +1314,7 @@ cudaError_t launch_step_kernel(void (*kernel)(KArgs...), unsigned nblocks, dim3 
 
 template <typename ST, bool ZG>
 cudaError_t launch_typed(const Box &b, const StepConst &c, const Quant &q, const StepView &v, bool f_streamed,
-                         bool odd, bool write_moments, cudaStream_t s)
+                         bool odd, bool write_moments, cudaStream_t s, int zlo, int zhi)
 {
     const StepMap m = step_map(c, q);
     StepPtrs<ST> P;
@@ -1349,15 +1351,18 @@ cudaError_t launch_typed(const Box &b, const StepConst &c, const Quant &q, const
     bool tma = kUseTma && (need_g || use_tma_f<ST>());
     if (tma && need_g) tma = encode_g_map<ST>(b, gin, &gmap);
     if (tma && use_tma_f<ST>()) tma = encode_f_maps<ST>(b, P.f0in, fin, &f0map, &fqmap);
-    const int tz = choose_tz<ST>(b);
-    const int nchunks = (b.nz + tz - 1) / tz;
+    Box range = b;   // the chunk depth for the planes this launch covers
+    range.nz = zhi - zlo;
+    const int tz = choose_tz<ST>(range);
+    const int nchunks = (range.nz + tz - 1) / tz;
     const unsigned nblocks = (unsigned)((b.nx / TX) * (b.ny / TY) * nchunks);
     const dim3 block(TX / (use_pair<ST>() ? 2 : 1), TY, 1);
     const int wm = write_moments ? 1 : 0;
     constexpr int smem = Geo<ST>::SMEM;
     const StepBox kb{b.nx, b.ny, b.nz, b.nxy, b.n};
     auto go = [&](auto kernel) {
-        return launch_step_kernel(kernel, nblocks, block, smem, s, P, kb, c, m, tz, wm, gmap, f0map, fqmap);
+        return launch_step_kernel(kernel, nblocks, block, smem, s, P, kb, c, m, tz, wm, zlo, zhi, gmap, f0map,
+                                  fqmap);
     };
     if (f_streamed) {
         if (odd) return cudaErrorInvalidValue;  // the streamed initial state is always read by an even step
@@ -1370,10 +1375,10 @@ cudaError_t launch_typed(const Box &b, const StepConst &c, const Quant &q, const
 
 template <typename ST>
 cudaError_t launch_typed(const Box &b, const StepConst &c, const Quant &q, const StepView &v, bool f_streamed,
-                         bool odd, bool write_moments, cudaStream_t s)
+                         bool odd, bool write_moments, cudaStream_t s, int zlo, int zhi)
 {
-    if (b.zghost) return launch_typed<ST, true>(b, c, q, v, f_streamed, odd, write_moments, s);
-    return launch_typed<ST, false>(b, c, q, v, f_streamed, odd, write_moments, s);
+    if (b.zghost) return launch_typed<ST, true>(b, c, q, v, f_streamed, odd, write_moments, s, zlo, zhi);
+    return launch_typed<ST, false>(b, c, q, v, f_streamed, odd, write_moments, s, 0, b.nz);
 }
 
 }  // namespace
@@ -1385,13 +1390,18 @@ cudaError_t launch_wait_selftest(int *err, cudaStream_t s)
 }
 
 cudaError_t launch_step(const Box &b, const StepConst &c, const Quant &q, const StepView &v, bool f_streamed,
-                        bool odd, bool write_moments, cudaStream_t s)
+                        bool odd, bool write_moments, cudaStream_t s, int zlo, int zhi)
 {
     if (b.nx % TX != 0 || b.ny % TY != 0) return cudaErrorInvalidValue;
+    if (zhi < 0) zhi = b.nz;
+    // a periodic box steps whole; a z-slab any nonempty range of its planes
+    if (zlo < 0 || zhi > b.nz || zlo >= zhi || (!b.zghost && (zlo != 0 || zhi != b.nz)))
+        return cudaErrorInvalidValue;
     switch (v.storage) {
-    case LBM_STORAGE_FP32: return launch_typed<float>(b, c, q, v, f_streamed, odd, write_moments, s);
-    case LBM_STORAGE_FP16: return launch_typed<__half>(b, c, q, v, f_streamed, odd, write_moments, s);
-    case LBM_STORAGE_BF16: return launch_typed<__nv_bfloat16>(b, c, q, v, f_streamed, odd, write_moments, s);
+    case LBM_STORAGE_FP32: return launch_typed<float>(b, c, q, v, f_streamed, odd, write_moments, s, zlo, zhi);
+    case LBM_STORAGE_FP16: return launch_typed<__half>(b, c, q, v, f_streamed, odd, write_moments, s, zlo, zhi);
+    case LBM_STORAGE_BF16:
+        return launch_typed<__nv_bfloat16>(b, c, q, v, f_streamed, odd, write_moments, s, zlo, zhi);
     default: return cudaErrorInvalidValue;
     }
 }

@@ -92,15 +92,27 @@ def test_slab_rejects_whole_box_calls(lib):
         assert lib_.lbm_split_z(slabs.handle(0), 2, (C.c_int * 2)(12, 12), None, out) == capi.LBM_EINVAL
         assert lib_.lbm_split_z(whole._h, 2, (C.c_int * 2)(24, 20), None, out) == capi.LBM_EINVAL
         assert lib_.lbm_split_z(whole._h, 2, (C.c_int * 2)(47, 1), None, out) == capi.LBM_EINVAL
+        # the two parts of a step in order, once each
+        h = slabs.handle(0)
+        assert lib_.lbm_slab_step_boundary(h, 0.0) == capi.LBM_ESTATE
+        assert lib_.lbm_slab_step_interior(h, 0.0) == capi.LBM_OK
+        assert lib_.lbm_slab_step_interior(h, 0.0) == capi.LBM_ESTATE
+        assert lib_.lbm_slab_step_local(h, 0.0) == capi.LBM_ESTATE
+        assert lib_.lbm_slab_step(slabs._h, 2, 1, 0.0) == capi.LBM_ESTATE
+        assert lib_.lbm_slab_step_interior(whole._h, 0.0) == capi.LBM_EINVAL
 
 
+@pytest.mark.parametrize("order", ["whole step", "interior while the halo moves"])
 @pytest.mark.parametrize("storage", ["fp32", "fp16"])
-def test_halo_pack_unpack_protocol(lib, storage):
+def test_halo_pack_unpack_protocol(lib, storage, order):
     """The per-process protocol: each slab packs its halo planes into buffers
     the caller owns (here torch device tensors), the buffers go to the
     neighbours (here a device copy; across processes NCCL or MPI), each slab
     unpacks what it received and steps alone; after an odd step the
-    LBM_HALO_POST exchange returns the ghost-plane writes."""
+    LBM_HALO_POST exchange returns the ghost-plane writes.  Either the whole
+    step after the exchange (lbm_slab_step_local), or its interior planes
+    between pack and unpack and its boundary planes after
+    (lbm_slab_step_interior / lbm_slab_step_boundary)."""
     import torch
     from lbm_bench_gpu_gb300 import capi
     p = params((64, 32, 48), storage)
@@ -111,17 +123,22 @@ def test_halo_pack_unpack_protocol(lib, storage):
         with capi.Slabs(whole, (20, 28)) as slabs:
             hs = [slabs.handle(k) for k in range(2)]
 
-            def exchange(phase):
+            def pack(phase):
                 nbytes = [int(lib_.lbm_halo_bytes(h, phase)) for h in hs]
                 assert nbytes[0] == nbytes[1] >= 0
                 if nbytes[0] == 0:
-                    return
+                    return None
                 send = [(torch.empty(nbytes[0], dtype=torch.uint8, device=dev),
                          torch.empty(nbytes[0], dtype=torch.uint8, device=dev)) for _ in hs]
                 for h, (lo, hi) in zip(hs, send):
                     capi.check(lib_.lbm_halo_pack(h, phase, C.c_void_p(lo.data_ptr()), C.c_void_p(hi.data_ptr())),
                                "pack")
                     capi.check(lib_.lbm_sync(h), "sync")
+                return send
+
+            def unpack(phase, send):
+                if send is None:
+                    return
                 for k, h in enumerate(hs):
                     below, above = send[(k - 1) % 2], send[(k + 1) % 2]
                     # from below its "hi" buffer, from above its "lo" buffer
@@ -131,10 +148,18 @@ def test_halo_pack_unpack_protocol(lib, storage):
                     capi.check(lib_.lbm_sync(h), "sync")
 
             for _ in range(5):
-                exchange(capi.LBM_HALO_PRE)
-                for h in hs:
-                    capi.check(lib_.lbm_slab_step_local(h, grav), "lbm_slab_step_local")
-                exchange(capi.LBM_HALO_POST)
+                if order == "whole step":
+                    unpack(capi.LBM_HALO_PRE, pack(capi.LBM_HALO_PRE))
+                    for h in hs:
+                        capi.check(lib_.lbm_slab_step_local(h, grav), "lbm_slab_step_local")
+                else:
+                    send = pack(capi.LBM_HALO_PRE)
+                    for h in hs:
+                        capi.check(lib_.lbm_slab_step_interior(h, grav), "lbm_slab_step_interior")
+                    unpack(capi.LBM_HALO_PRE, send)
+                    for h in hs:
+                        capi.check(lib_.lbm_slab_step_boundary(h, grav), "lbm_slab_step_boundary")
+                unpack(capi.LBM_HALO_POST, pack(capi.LBM_HALO_POST))
             ref.step(5, grav)
             slabs.merge_into(whole)
         assert_same_state(whole, ref, f"protocol {storage}")
