@@ -11,7 +11,7 @@ L2 flush is needed between steps.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
---impl reference times the reference's own step (its nine kernels and three
+--impl reference times the reference's own step (its seven kernels and three
 halo exchanges, compiled for the host CPU from the reference sources) on the
 host cores, on a slab of the same workload sized so the run stays within a
 few minutes.  For N > 1 (torchrun) every rank runs an independent replica of
@@ -429,8 +429,8 @@ def run_reference_cuda(inp, steps, local, ours_mlups):
     bubbles), relaxStep = 0 and `steps` evolution steps, stats and VTK output
     outside the loop (its three ASCII VTK files go to /dev/null).  The value is
     its own "Evolution time" (CUDA events around the evolution loop,
-    src/main.cu:613-624) per step; every step includes its nine kernels and
-    the three host-staged halo exchanges.  Its final stats.out line is
+    src/main.cu:613-624) per step; every step includes its seven kernels, six
+    pack/unpack kernels and three host-staged halo exchanges.  Its final stats.out line is
     compared with lbm_stats of this library after the same steps from the same
     input."""
     import dataclasses

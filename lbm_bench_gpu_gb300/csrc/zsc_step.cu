@@ -1,7 +1,7 @@
 // zsc_step.cu -- one fused sm_103a kernel per ZSC lattice Boltzmann step.
 //
-// One launch does what the reference does with nine kernels and three
-// host-staged halo exchanges per step (src/main.cu:496-608):
+// One launch does what the reference does with seven kernels (plus six
+// pack/unpack kernels) and three host-staged halo exchanges per step (src/main.cu:496-608):
 //   update_phi / update_rho / update_velocity   (moments)
 //   collision_f (D3Q7 phi) / collision_g (D3Q19 momentum, forcing)
 //   stream_f (ZSC eta-interpolated) / stream_g (plain)

@@ -346,7 +346,7 @@ REF_CONSTANT_NAMES = ["phiStar", "phiStarSq", "invTauRhoOne", "eta", "eta2", "in
 
 
 class RefCPU:
-    """The reference's own step (FP32, its nine kernels and three halo
+    """The reference's own step (FP32, its seven kernels and three halo
     exchanges) run on the CPU.  One instance at a time (the reference keeps
     its state in globals)."""
 

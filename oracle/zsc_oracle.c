@@ -7,7 +7,7 @@
  * (liblbm_gb300.so) never links or calls it.
  *
  * It restates, in double precision and on a fully periodic box, the update that
- * carlosrosales/lbm_bench_gpu performs with nine kernels and three host-staged
+ * carlosrosales/lbm_bench_gpu performs with seven kernels and three host-staged
  * halo exchanges per step.  Every function cites the reference lines it follows
  * (paths relative to the reference project root).  Naming follows the
  * reference: f = D3Q7 order-parameter distribution (relaxed with tauPhi),
