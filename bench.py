@@ -340,8 +340,10 @@ def run_ours(args, rank, world, local):
                             "roofline_frac": round(b_v * nodes / (ms_v / K / 1e3) / 1e9 / peak, 4),
                             "bytes_per_node": b_v, "speedup_vs_headline": round(mlups / value, 3)}
         result["storage_variants"] = variants
-    if rank == 0 and not args.no_e2e:
-        result["e2e"] = run_e2e(args, inp, p, grav, local)
+    if not args.no_e2e:
+        # every rank runs its replica's end-to-end sequence; the job's time is
+        # the slowest rank's
+        result["e2e"] = run_e2e(args, inp, p, grav, local, world)
     if rank == 0 and not args.no_adjoint:
         result["adjoint"] = run_adjoint(local)
         if args.adjoint_long:
@@ -577,7 +579,7 @@ def run_adjoint(local, long_horizon=False):
     return out
 
 
-def run_e2e(args, inp, p, grav, local):
+def run_e2e(args, inp, p, grav, local, world: int = 1):
     """Same metric through the C-ABI with host buffers: lbm_init from pinned host
     fields (upload inside the timed region), K steps with lbm_stats every
     `stat_every` steps (scalar diagnostics back to the host, as the reference
@@ -620,15 +622,15 @@ def run_e2e(args, inp, p, grav, local):
     capi.check(capi.load().lbm_stats(lat._h, None, *[capi.fptr(host_out[k]) for k in
                                                       ("phi", "rho", "ux", "uy", "uz")]), "lbm_stats")
     t_down = time.perf_counter() - ta
-    dt = time.perf_counter() - t0
+    dt = max_over_ranks(time.perf_counter() - t0, local)
     lat.close()
-    h2d = 5 * nodes * 4
-    d2h = n_stats * 16 * 8 + 5 * nodes * 4
-    return {"value": round(nodes * K / dt / 1e6, 1), "unit": "MLUPS",
+    h2d = world * 5 * nodes * 4                 # every replica's upload and read-back
+    d2h = world * (n_stats * 16 * 8 + 5 * nodes * 4)
+    return {"value": round(world * nodes * K / dt / 1e6, 1), "unit": "MLUPS",
             "h2d_bytes_per_step": round(h2d / K, 1), "d2h_bytes_per_step": round(d2h / K, 1),
             "breakdown_s": {"init_s": round(t_init, 5), "steps_s": round(t_steps, 5), "stats_s": round(t_stats, 5),
                             "download_s": round(t_down, 5), "total_s": round(dt, 5)},
-            "steps_only_mlups": round(nodes * K / t_steps / 1e6, 1) if t_steps > 0 else None,
+            "steps_only_mlups": round(world * nodes * K / t_steps / 1e6, 1) if t_steps > 0 else None,
             "what": f"lbm_init from pinned host phi/rho/u (context allocation, upload, initial equilibrium: "
                     f"init_s), {K} x lbm_step (steps_s) with lbm_stats every {args.stat_every} steps and at step "
                     f"{K} (stats_s), the final fields copied back (download_s); wall clock {dt:.3f} s"}
