@@ -533,29 +533,36 @@ def run_adjoint(local, long_horizon=False):
 
     t_fwd = min(forward_time(grav) for _ in range(2))
 
-    def measure(lat, budget, want_phi0):
+    def measure(lat, budget, want_phi0, host=0.0):
         lat.adjoint_release()
         torch.cuda.synchronize()
         free0 = torch.cuda.mem_get_info()[0]
-        first = lat.adjoint(T, grav, objective, window, checkpoint_bytes=budget, want_phi0=want_phi0)
+        first = lat.adjoint(T, grav, objective, window, checkpoint_bytes=budget, want_phi0=want_phi0,
+                            host_checkpoint_bytes=host)
         held = free0 - torch.cuda.mem_get_info()[0]
-        warm = lat.adjoint(T, grav, objective, window, checkpoint_bytes=budget, want_phi0=want_phi0)
+        warm = lat.adjoint(T, grav, objective, window, checkpoint_bytes=budget, want_phi0=want_phi0,
+                           host_checkpoint_bytes=host)
         return {"adjoint_s": round(warm["seconds"], 4), "ratio": round(warm["seconds"] / t_fwd, 3),
                 "first_call": {"adjoint_s": round(first["seconds"], 4),
                                "ratio": round(first["seconds"] / t_fwd, 3),
                                "same_gradient": first["dJ_dgrav"] == warm["dJ_dgrav"]},
                 "slots": warm["slots"], "checkpoint_GB": round(warm["checkpoint_bytes_used"] / 1e9, 2),
                 "device_GB": round((held + state_bytes) / 1e9, 2),
-                "forward_steps": warm["forward_steps"]}, warm
+                "forward_steps": warm["forward_steps"], "host_slots": warm["host_slots"]}, warm
 
     with capi.Lattice.from_fields(p, phi0, rho0) as lat:
         lat.sync()
         torch.cuda.synchronize()
         head, r = measure(lat, 40e9 if long_horizon else 0.0, True)
-        other = None
+        other = host_tier = None
         if not long_horizon:
             other, r40 = measure(lat, 40e9, False)
             other["same_gradient"] = r40["dJ_dgrav"] == r["dJ_dgrav"]
+        else:
+            # the same 40 GB of device checkpoints and a second tier of 60 GB
+            # of pinned host memory
+            host_tier, rh = measure(lat, 40e9, False, host=60e9)
+            host_tier["same_gradient"] = rh["dJ_dgrav"] == r["dJ_dgrav"]
         fd = {}
         hs = (1e-6, 5e-7, 2.5e-7) if not long_horizon else (1e-6, 5e-7, 2.5e-7, 1.25e-7, 6.25e-8)
         for h in hs:
@@ -576,6 +583,8 @@ def run_adjoint(local, long_horizon=False):
                 "dJ_dphi0_norm": float(np.sqrt((r["dJ_dphi0"].astype(np.float64) ** 2).sum()))})
     if other is not None:
         out["budget_40GB"] = other
+    if host_tier is not None:
+        out["host_tier_60GB"] = host_tier
     return out
 
 

@@ -182,6 +182,10 @@ typedef struct lbm_adjoint_opts {
     float grav;               /* body force of the run */
     double checkpoint_bytes;  /* device memory for checkpoints; <= 0: the free memory less a reserve of
                                  max(4 GiB, 5% of the device) */
+    double host_checkpoint_bytes;   /* pinned host memory for a second checkpoint tier (0: none): the
+                                       states at the starts of equal segments go to the host during
+                                       the first forward sweep, and each segment is reversed from its
+                                       start with the device checkpoints */
 } lbm_adjoint_opts;
 
 typedef struct lbm_adjoint_out {
@@ -193,6 +197,7 @@ typedef struct lbm_adjoint_out {
     long long adjoint_steps;  /* = nsteps */
     double seconds;           /* wall time of the call */
     double checkpoint_bytes_used;
+    int host_slots;           /* segment starts held in host memory (0: one tier) */
 } lbm_adjoint_out;
 
 /* Gradient of an objective over T steps with respect to the body force and

@@ -72,13 +72,13 @@ class StatsOut(C.Structure):
 
 class AdjointOpts(C.Structure):
     _fields_ = [("objective", C.c_int), ("nsteps", C.c_int), ("window", C.c_int), ("grav", C.c_float),
-                ("checkpoint_bytes", C.c_double)]
+                ("checkpoint_bytes", C.c_double), ("host_checkpoint_bytes", C.c_double)]
 
 
 class AdjointOut(C.Structure):
     _fields_ = [("J", C.c_double), ("dJ_dgrav", C.c_double), ("dJ_dphi0", C.POINTER(C.c_float)),
                 ("slots", C.c_int), ("forward_steps", C.c_longlong), ("adjoint_steps", C.c_longlong),
-                ("seconds", C.c_double), ("checkpoint_bytes_used", C.c_double)]
+                ("seconds", C.c_double), ("checkpoint_bytes_used", C.c_double), ("host_slots", C.c_int)]
 
 
 class LbmError(RuntimeError):
@@ -294,16 +294,18 @@ class Lattice:
         check(load().lbm_set_dist(self._h, fptr(f), fptr(g)), "lbm_set_dist")
 
     def adjoint(self, nsteps: int, grav: float, objective: str = "light_uz_mean", window: int = 1,
-                checkpoint_bytes: float = 0.0, want_phi0: bool = True) -> dict:
-        """lbm_step_adjoint: J, dJ/dgrav and dJ/dphi0 over nsteps from the initial state."""
-        o = AdjointOpts(OBJECTIVES[objective], int(nsteps), int(window), float(grav), float(checkpoint_bytes))
+                checkpoint_bytes: float = 0.0, want_phi0: bool = True, host_checkpoint_bytes: float = 0.0) -> dict:
+        """lbm_step_adjoint: J, dJ/dgrav and dJ/dphi0 over nsteps from the initial state
+        (host_checkpoint_bytes > 0: a second checkpoint tier in pinned host memory)."""
+        o = AdjointOpts(OBJECTIVES[objective], int(nsteps), int(window), float(grav), float(checkpoint_bytes),
+                        float(host_checkpoint_bytes))
         out = AdjointOut()
         grad = np.zeros(self.shape, np.float32) if want_phi0 else None
         out.dJ_dphi0 = fptr(grad) if want_phi0 else None
         check(load().lbm_step_adjoint(self._h, C.byref(o), C.byref(out)), "lbm_step_adjoint")
         return {"J": out.J, "dJ_dgrav": out.dJ_dgrav, "dJ_dphi0": grad, "slots": out.slots,
                 "forward_steps": out.forward_steps, "adjoint_steps": out.adjoint_steps, "seconds": out.seconds,
-                "checkpoint_bytes_used": out.checkpoint_bytes_used}
+                "checkpoint_bytes_used": out.checkpoint_bytes_used, "host_slots": out.host_slots}
 
     def objective(self, nsteps: int, grav: float, objective: str = "light_uz_mean", window: int = 1) -> float:
         """lbm_objective: J alone over nsteps from the initial state (forward run)."""

@@ -121,6 +121,8 @@ struct Adjoint {
     double *partials = nullptr, *dgrav = nullptr, *ab = nullptr, *acc = nullptr;
     unsigned char *slots = nullptr;   // the context's checkpoint pool
     std::vector<Snapshot> snaps;
+    unsigned char *host = nullptr;    // pinned host checkpoints (second tier), slot layout
+    std::vector<Snapshot> hsnaps;
     std::vector<int> free_slots;
     int cur = 0;                 // lam[cur] holds lambda^{k+1}
     bool lambda_ready = false;
@@ -194,6 +196,33 @@ struct Adjoint {
         snaps[s].step = step;
         snaps[s].f_streamed = c->st.f_streamed;
         snaps[s].g_odd_next = c->st.g_odd_next;
+        return slot_ev.empty() ? LBM_OK : record(slot_ev[s], c->stream);
+    }
+
+    // the context's current state (at `step`) into host slot h, in the slot
+    // layout; on the main stream, so the next step waits for the copy
+    int to_host(int h, long long step)
+    {
+        lbm::StepView v = lbm::state_view(c, c->st.f_cur);
+        unsigned char *d = host + (size_t)h * snap_bytes;
+        const size_t b0 = sizeof(float) * n, bq = c->esz * (lbm::kQf - 1) * n, bg = c->esz * lbm::kQg * n;
+        cudaError_t e = cudaMemcpyAsync(d, v.f0_in, b0, cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(d + b0, v.fq_in, bq, cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(d + b0 + bq, c->st.g, bg, cudaMemcpyDeviceToHost, c->stream);
+        if (e != cudaSuccess) return cuda_fail(e, "adjoint: host checkpoint");
+        hsnaps[h].step = step;
+        hsnaps[h].f_streamed = c->st.f_streamed;
+        hsnaps[h].g_odd_next = c->st.g_odd_next;
+        return LBM_OK;
+    }
+
+    // host slot h into device slot s (one copy: the layouts agree)
+    int from_host(int h, int s)
+    {
+        cudaError_t e = cudaMemcpyAsync(slot_ptr(s), host + (size_t)h * snap_bytes, snap_bytes,
+                                        cudaMemcpyHostToDevice, c->stream);
+        if (e != cudaSuccess) return cuda_fail(e, "adjoint: host checkpoint restore");
+        snaps[s] = hsnaps[h];
         return slot_ev.empty() ? LBM_OK : record(slot_ev[s], c->stream);
     }
 
@@ -392,6 +421,36 @@ struct Adjoint {
         return revolve(s, m, si, cfree);
     }
 
+    // Two tiers: the trajectory in K segments of L steps; the first forward
+    // sweep leaves the start of every segment but the first and the last in
+    // host memory (the last one's start is still in the context when the sweep
+    // ends), then the segments are reversed last to first, each from its start
+    // in device slot `base` with the other device slots (segment 0 from slot 0,
+    // which holds s^0, with all of them).  hslots host slots give K = hslots + 2
+    // segments at most.
+    int two_level(long long hslots, long long nslots)
+    {
+        const long long T = o.nsteps;
+        const long long L = (T + hslots + 1) / (hslots + 2);   // ceil(T / (hslots + 2))
+        const long long K = (T + L - 1) / L;
+        hsnaps.assign((size_t)std::max<long long>(K - 2, 0), Snapshot());
+        const int base = take_slot();
+        if (base < 0) return fail(LBM_ESTATE, "adjoint: checkpoint pool exhausted");
+        int rc = LBM_OK;
+        for (long long k = 1; k < K && !rc; k++) {
+            rc = forward(L);                               // the context: s^{(k - 1) L} -> s^{k L}
+            if (!rc && k < K - 1) rc = to_host((int)(k - 1), k * L);
+        }
+        if (!rc) rc = save(base, (K - 1) * L);
+        for (long long k = K - 1; k >= 1 && !rc; k--) {
+            if (k < K - 1) rc = from_host((int)(k - 1), base);
+            if (!rc) rc = revolve(k * L, std::min(T, (k + 1) * L), base, (int)(nslots - 2));
+        }
+        free_slots.push_back(base);
+        if (!rc) rc = revolve(0, std::min(T, L), 0, (int)(nslots - 1));
+        return rc;
+    }
+
     void release()
     {
         cudaStreamSynchronize(c->stream);
@@ -569,6 +628,25 @@ extern "C" int lbm_step_adjoint(lbm_ctx *c, const lbm_adjoint_opts *o, lbm_adjoi
     A.slots = static_cast<unsigned char *>(c->adj_slots);
     A.snaps.assign((size_t)nslots, Snapshot());
     for (long long s = nslots - 1; s >= 1; s--) A.free_slots.push_back((int)s);
+    // the second tier: pinned host slots for segment starts (two device slots
+    // at least: s^0 and a segment's start)
+    long long hslots = 0;
+    if (o->host_checkpoint_bytes > 0 && nslots >= 2 && o->nsteps >= 3) {
+        hslots = (long long)(o->host_checkpoint_bytes / (double)A.snap_bytes);
+        hslots = std::min<long long>(hslots, (long long)o->nsteps - 2);
+    }
+    if (hslots >= 1 && c->adj_host_bytes < (size_t)hslots * A.snap_bytes) {
+        if (c->adj_host) cudaFreeHost(c->adj_host);
+        c->adj_host = nullptr;
+        c->adj_host_bytes = 0;
+        e = cudaHostAlloc(&c->adj_host, (size_t)hslots * A.snap_bytes, cudaHostAllocDefault);
+        if (e != cudaSuccess) {
+            c->adj_host = nullptr;
+            return cuda_fail(e, "lbm_step_adjoint: host checkpoint pool");
+        }
+        c->adj_host_bytes = (size_t)hslots * A.snap_bytes;
+    }
+    A.host = static_cast<unsigned char *>(c->adj_host);
 
     e = cudaMemsetAsync(A.acc, 0, sizeof(double) * 2, c->stream);
     if (e == cudaSuccess)
@@ -579,7 +657,7 @@ extern "C" int lbm_step_adjoint(lbm_ctx *c, const lbm_adjoint_opts *o, lbm_adjoi
     if (e != cudaSuccess) rc = cuda_fail(e, "lbm_step_adjoint: setup");
     if (!rc) rc = A.create_streams((int)nslots);
     if (!rc) rc = A.save(0, 0);
-    if (!rc) rc = A.revolve(0, o->nsteps, 0, (int)(nslots - 1));
+    if (!rc) rc = hslots >= 1 ? A.two_level(hslots, nslots) : A.revolve(0, o->nsteps, 0, (int)(nslots - 1));
     // lambda^0 -> dJ/dphi0 through the initial equilibrium (output in the
     // lsrc buffer, phi as the scratch for the Laplacian's adjoint)
     float *lphi0 = reinterpret_cast<float *>(A.lsrc);
@@ -610,6 +688,7 @@ extern "C" int lbm_step_adjoint(lbm_ctx *c, const lbm_adjoint_opts *o, lbm_adjoi
     out->forward_steps = A.fwd_steps;
     out->adjoint_steps = A.adj_steps;
     out->checkpoint_bytes_used = (double)nslots * (double)A.snap_bytes;
+    out->host_slots = (int)A.hsnaps.size();
     out->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     return LBM_OK;
 }
@@ -622,8 +701,9 @@ extern "C" int lbm_adjoint_release(lbm_ctx *c)
     if (e != cudaSuccess) return cuda_fail(e, "lbm_adjoint_release");
     cudaFree(c->adj_work);
     cudaFree(c->adj_slots);
-    c->adj_work = c->adj_slots = nullptr;
-    c->adj_work_bytes = c->adj_slot_bytes = 0;
+    if (c->adj_host) cudaFreeHost(c->adj_host);
+    c->adj_work = c->adj_slots = c->adj_host = nullptr;
+    c->adj_work_bytes = c->adj_slot_bytes = c->adj_host_bytes = 0;
     return LBM_OK;
 }
 

@@ -773,6 +773,7 @@ extern "C" void lbm_destroy(lbm_ctx *c)
     cudaFree(c->arena);   // st.f0, st.fq, st.g, st.mom, partials, result, err
     cudaFree(c->adj_work);
     cudaFree(c->adj_slots);
+    if (c->adj_host) cudaFreeHost(c->adj_host);
     cudaFree(c->halo_send);
     cudaFree(c->phi_ghost);
     if (c->ev_pack) cudaEventDestroy(c->ev_pack);

@@ -206,6 +206,8 @@ struct lbm_ctx {
     size_t adj_work_bytes = 0;
     void *adj_slots = nullptr;
     size_t adj_slot_bytes = 0;
+    void *adj_host = nullptr;          // pinned host checkpoints (the second tier)
+    size_t adj_host_bytes = 0;
     // z-slab contexts (lbm_split_z): planes [z0, z0 + nz) of a box of
     // nz_total planes, the device buffers the halo exchange packs into (one
     // per side, halo_bytes each), the phi planes around the slab for the
