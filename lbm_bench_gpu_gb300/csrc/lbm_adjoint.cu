@@ -425,15 +425,88 @@ struct Adjoint {
     // sweep leaves the start of every segment but the first and the last in
     // host memory (the last one's start is still in the context when the sweep
     // ends), then the segments are reversed last to first, each from its start
-    // in device slot `base` with the other device slots (segment 0 from slot 0,
+    // in a device base slot with the other device slots (segment 0 from slot 0,
     // which holds s^0, with all of them).  hslots host slots give K = hslots + 2
-    // segments at most.
+    // segments at most.  The host copies run on a copy stream beside the
+    // compute: each sweep checkpoint goes out through one of two device slots
+    // (a device copy on the main stream, then the host copy), and while a
+    // segment is reversed the next segment's start comes back into the other
+    // base slot.  With fewer than four device slots the copies are made on
+    // the main stream, one base slot.
     int two_level(long long hslots, long long nslots)
     {
         const long long T = o.nsteps;
         const long long L = (T + hslots + 1) / (hslots + 2);   // ceil(T / (hslots + 2))
         const long long K = (T + L - 1) / L;
         hsnaps.assign((size_t)std::max<long long>(K - 2, 0), Snapshot());
+        if (nslots < 4) return two_level_serial(T, L, K, nslots);
+        int b[2] = {take_slot(), take_slot()};   // the sweep's outbound slots, then the segment bases
+        if (b[0] < 0 || b[1] < 0) return fail(LBM_ESTATE, "adjoint: checkpoint pool exhausted");
+        cudaStream_t cp = nullptr;
+        cudaEvent_t saved = nullptr, done[2] = {nullptr, nullptr}, freed[2] = {nullptr, nullptr},
+                    in[2] = {nullptr, nullptr};
+        cudaError_t e = cudaStreamCreateWithFlags(&cp, cudaStreamNonBlocking);
+        for (cudaEvent_t *x : {&saved, &done[0], &done[1], &freed[0], &freed[1], &in[0], &in[1]})
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(x, cudaEventDisableTiming);
+        for (int i = 0; i < 2 && e == cudaSuccess; i++) {
+            e = cudaEventRecord(done[i], cp);
+            if (e == cudaSuccess) e = cudaEventRecord(freed[i], c->stream);
+        }
+        int rc = e == cudaSuccess ? LBM_OK : cuda_fail(e, "adjoint: host copy stream");
+        auto wait = [&](cudaStream_t st, cudaEvent_t ev) {
+            const cudaError_t w = cudaStreamWaitEvent(st, ev, 0);
+            return w == cudaSuccess ? LBM_OK : cuda_fail(w, "adjoint: host copy order");
+        };
+        auto rec = [&](cudaEvent_t ev, cudaStream_t st) {
+            const cudaError_t w = cudaEventRecord(ev, st);
+            return w == cudaSuccess ? LBM_OK : cuda_fail(w, "adjoint: host copy order");
+        };
+        // sweep: s^{kL} of k = 1 .. K - 2 to host slot k - 1 through b[k & 1]
+        for (long long k = 1; k < K && !rc; k++) {
+            rc = forward(L);
+            if (rc || k == K - 1) continue;
+            const int i = (int)(k & 1);
+            if (!(rc = wait(c->stream, done[i])) && !(rc = save(b[i], k * L)) && !(rc = rec(saved, c->stream)) &&
+                !(rc = wait(cp, saved))) {
+                e = cudaMemcpyAsync(host + (size_t)(k - 1) * snap_bytes, slot_ptr(b[i]), snap_bytes,
+                                    cudaMemcpyDeviceToHost, cp);
+                rc = e == cudaSuccess ? rec(done[i], cp) : cuda_fail(e, "adjoint: host checkpoint");
+                hsnaps[(size_t)(k - 1)] = snaps[b[i]];
+            }
+        }
+        // reverse: segment k from base b[cur]; segment k - 1's start comes into b[1 - cur] meanwhile
+        int cur = 0;
+        if (!rc && !(rc = wait(c->stream, done[0]))) rc = save(b[cur], (K - 1) * L);
+        for (long long k = K - 1; k >= 1 && !rc; k--) {
+            const bool next = k - 1 >= 1;
+            const int nx = 1 - cur;
+            if (next && !(rc = wait(cp, freed[nx])) && !(rc = wait(cp, done[nx]))) {
+                e = cudaMemcpyAsync(slot_ptr(b[nx]), host + (size_t)(k - 2) * snap_bytes, snap_bytes,
+                                    cudaMemcpyHostToDevice, cp);
+                rc = e == cudaSuccess ? rec(in[nx], cp) : cuda_fail(e, "adjoint: host checkpoint restore");
+                if (!rc) rc = rec(slot_ev[b[nx]], cp);
+                snaps[b[nx]] = hsnaps[(size_t)(k - 2)];
+            }
+            if (!rc) rc = revolve(k * L, std::min(T, (k + 1) * L), b[cur], (int)(nslots - 3));
+            if (!rc) rc = rec(freed[cur], c->stream);
+            if (!rc && next) {
+                rc = wait(c->stream, in[nx]);
+                cur = nx;
+            }
+        }
+        if (cp) cudaStreamSynchronize(cp);
+        for (cudaEvent_t x : {saved, done[0], done[1], freed[0], freed[1], in[0], in[1]})
+            if (x) cudaEventDestroy(x);
+        if (cp) cudaStreamDestroy(cp);
+        free_slots.push_back(b[1]);
+        free_slots.push_back(b[0]);
+        if (!rc) rc = revolve(0, std::min(T, L), 0, (int)(nslots - 1));
+        return rc;
+    }
+
+    // the same with the host copies on the main stream and one base slot
+    int two_level_serial(long long T, long long L, long long K, long long nslots)
+    {
         const int base = take_slot();
         if (base < 0) return fail(LBM_ESTATE, "adjoint: checkpoint pool exhausted");
         int rc = LBM_OK;

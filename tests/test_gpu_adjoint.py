@@ -42,23 +42,30 @@ def test_gpu_adjoint_matches_oracle(lib, objective, window, T):
     assert err <= 2e-3 * np.abs(lphi).max(), err / np.abs(lphi).max()
 
 
-def test_host_checkpoint_tier_does_not_change_the_gradient(lib):
+@pytest.mark.parametrize("device_slots", [3, 5])
+def test_host_checkpoint_tier_does_not_change_the_gradient(lib, device_slots):
     """A second checkpoint tier in pinned host memory (segment starts kept on
     the host during the first sweep, each segment reversed with the device
-    slots): the same trajectory, so J and the gradients are identical, with
-    fewer forward steps than one tier of 3 device slots takes."""
+    slots; with 3 device slots the host copies run on the main stream, with 5
+    on a copy stream beside the compute): the same trajectory, so J and the
+    gradients are identical; with 3 device slots in fewer forward steps than
+    one tier takes."""
     from lbm_bench_gpu_gb300 import capi
     phi0, rho0 = fields()
     p = capi.make_params(32, 32, 16, **KW)
     snap = 26 * 4 * 32 * 32 * 16
+    dev = (device_slots + 0.5) * snap
     with capi.Lattice.from_fields(p, phi0.astype(np.float32), rho0.astype(np.float32)) as lat:
-        one = lat.adjoint(20, -3e-5, "light_uz_mean", 6, checkpoint_bytes=3.5 * snap)
-        two = lat.adjoint(20, -3e-5, "light_uz_mean", 6, checkpoint_bytes=3.5 * snap, host_checkpoint_bytes=4.5 * snap)
+        one = lat.adjoint(20, -3e-5, "light_uz_mean", 6, checkpoint_bytes=dev)
+        two = lat.adjoint(20, -3e-5, "light_uz_mean", 6, checkpoint_bytes=dev, host_checkpoint_bytes=4.5 * snap)
+        again = lat.adjoint(20, -3e-5, "light_uz_mean", 6, checkpoint_bytes=dev, host_checkpoint_bytes=4.5 * snap)
         assert lat.steps == 0
-    assert one["host_slots"] == 0 and two["host_slots"] == 3 and two["slots"] == 3
-    assert two["forward_steps"] < one["forward_steps"]
-    assert two["J"] == one["J"] and two["dJ_dgrav"] == one["dJ_dgrav"]
-    assert np.array_equal(two["dJ_dphi0"], one["dJ_dphi0"])
+    assert one["host_slots"] == 0 and two["host_slots"] == 3 and two["slots"] == device_slots
+    if device_slots == 3:
+        assert two["forward_steps"] < one["forward_steps"]
+    for r in (two, again):
+        assert r["J"] == one["J"] and r["dJ_dgrav"] == one["dJ_dgrav"]
+        assert np.array_equal(r["dJ_dphi0"], one["dJ_dphi0"])
 
 
 def test_checkpoint_budget_does_not_change_the_gradient(lib):
