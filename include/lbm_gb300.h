@@ -226,6 +226,12 @@ int lbm_objective(lbm_ctx *c, const lbm_adjoint_opts *o, double *J);
  * Synchronises the context's stream. */
 int lbm_adjoint_release(lbm_ctx *c);
 
+/* Forward steps lbm_step_adjoint runs for nsteps steps with `slots` device
+ * checkpoint slots and `host_slots` host ones (host_checkpoint_bytes divided
+ * by the snapshot bytes; 0: lbm_adjoint_forward_steps), without running it.
+ * No counterpart in the reference.  -1 for bad arguments. */
+long long lbm_adjoint_forward_steps_tiers(long long nsteps, int slots, long long host_slots);
+
 /* Forward steps lbm_step_adjoint runs for nsteps steps with `slots` checkpoint
  * slots (the initial state included; a budget of B bytes gives
  * floor(B / snapshot bytes) slots, a snapshot being the state's 26

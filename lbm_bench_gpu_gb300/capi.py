@@ -28,6 +28,7 @@ EXPORTS = [
     "lbm_split_z", "lbm_merge_z", "lbm_slab_step", "lbm_halo_bytes", "lbm_halo_pack", "lbm_halo_unpack",
     "lbm_slab_step_local", "lbm_stats_raw", "lbm_stats_combine", "lbm_slab_stats", "lbm_slab_maxabs",
     "lbm_slab_init_bubbles", "lbm_slab_step_interior", "lbm_slab_step_boundary",
+    "lbm_adjoint_forward_steps_tiers",
 ]
 OBJECTIVES = {"light_uz_mean": 0, "light_z_centroid": 1}
 
@@ -118,6 +119,8 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.lbm_wait_selftest.argtypes = [C.c_void_p]
     lib.lbm_adjoint_forward_steps.argtypes = [C.c_longlong, C.c_int]
     lib.lbm_adjoint_forward_steps.restype = C.c_longlong
+    lib.lbm_adjoint_forward_steps_tiers.argtypes = [C.c_longlong, C.c_int, C.c_longlong]
+    lib.lbm_adjoint_forward_steps_tiers.restype = C.c_longlong
     lib.lbm_state_bytes.argtypes = [C.c_void_p]
     lib.lbm_state_bytes.restype = C.c_longlong
     lib.lbm_save_state.argtypes = [C.c_void_p, C.c_void_p]
@@ -185,9 +188,13 @@ def make_params(nx: int, ny: int, nz: int, *, rhoL: float, rhoH: float, tauRho: 
     return p
 
 
-def adjoint_forward_steps(nsteps: int, slots: int) -> int:
-    """lbm_adjoint_forward_steps: forward steps of the checkpointing schedule (not run)."""
-    return int(load().lbm_adjoint_forward_steps(int(nsteps), int(slots)))
+def adjoint_forward_steps(nsteps: int, slots: int, host_slots: int = 0) -> int:
+    """lbm_adjoint_forward_steps(_tiers): forward steps of the checkpointing
+    schedule with `slots` device and `host_slots` host checkpoints (not run)."""
+    lib = load()
+    if host_slots:
+        return int(lib.lbm_adjoint_forward_steps_tiers(int(nsteps), int(slots), int(host_slots)))
+    return int(lib.lbm_adjoint_forward_steps(int(nsteps), int(slots)))
 
 
 def read_inputs(directory: str | os.PathLike, max_bubbles: int = 4096):

@@ -787,3 +787,22 @@ extern "C" long long lbm_adjoint_forward_steps(long long nsteps, int slots)
     bool terminal = true;
     return schedule_steps(nsteps, 0, nsteps, (int)(nslots - 1), terminal);
 }
+
+extern "C" long long lbm_adjoint_forward_steps_tiers(long long nsteps, int slots, long long host_slots)
+{
+    if (nsteps < 1 || slots < 1 || host_slots < 0) return -1;
+    const long long nslots = std::min<long long>(slots, nsteps + 1);
+    const long long hslots = nsteps >= 3 && nslots >= 2 ? std::min(host_slots, nsteps - 2) : 0;
+    if (hslots < 1) return lbm_adjoint_forward_steps(nsteps, slots);
+    // the accounting of Adjoint::two_level: the sweep, then the segments
+    // last to first from their base slots (two of them from four device slots
+    // up, one below), then segment 0 from slot 0 with all the others
+    const long long T = nsteps;
+    const long long L = (T + hslots + 1) / (hslots + 2);
+    const long long K = (T + L - 1) / L;
+    const int cfree = (int)(nslots >= 4 ? nslots - 3 : nslots - 2);
+    bool terminal = true;
+    long long steps = (K - 1) * L;
+    for (long long k = K - 1; k >= 1; k--) steps += schedule_steps(T, k * L, std::min(T, (k + 1) * L), cfree, terminal);
+    return steps + schedule_steps(T, 0, std::min(T, L), (int)(nslots - 1), terminal);
+}

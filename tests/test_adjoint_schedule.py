@@ -60,3 +60,19 @@ def test_schedule_edge_cases(lib):
     assert capi.adjoint_forward_steps(1, 1) == 1
     assert capi.adjoint_forward_steps(10, 1) == 10 + 45  # no free slot: recompute from the start
     assert capi.adjoint_forward_steps(0, 5) == -1 and capi.adjoint_forward_steps(5, 0) == -1
+
+
+def test_two_tier_schedule_counts():
+    """lbm_adjoint_forward_steps_tiers: the forward steps of the schedule with a
+    second tier of host checkpoints.  The long-horizon case (20 000 steps, 44
+    device slots, 66 host slots) is the count a GB300 run of lbm_step_adjoint
+    reported; no host slots is the one-tier count; host slots never add
+    forward steps there, and fewer device slots never take fewer."""
+    from lbm_bench_gpu_gb300 import capi
+    assert capi.adjoint_forward_steps(20000, 44, 66) == 56774
+    assert capi.load().lbm_adjoint_forward_steps_tiers(20000, 44, 0) == capi.adjoint_forward_steps(20000, 44)
+    assert capi.adjoint_forward_steps(20000, 44, 66) < capi.adjoint_forward_steps(20000, 44)
+    assert capi.adjoint_forward_steps(20, 3, 4) == 38 and capi.adjoint_forward_steps(20, 5, 4) == 33
+    for slots in (4, 8, 16):
+        assert capi.adjoint_forward_steps(2000, slots, 30) >= capi.adjoint_forward_steps(2000, slots + 1, 30)
+    assert capi.load().lbm_adjoint_forward_steps_tiers(0, 4, 3) == -1

@@ -61,6 +61,7 @@ def test_host_checkpoint_tier_does_not_change_the_gradient(lib, device_slots):
         again = lat.adjoint(20, -3e-5, "light_uz_mean", 6, checkpoint_bytes=dev, host_checkpoint_bytes=4.5 * snap)
         assert lat.steps == 0
     assert one["host_slots"] == 0 and two["host_slots"] == 3 and two["slots"] == device_slots
+    assert two["forward_steps"] == capi.adjoint_forward_steps(20, device_slots, 4)
     if device_slots == 3:
         assert two["forward_steps"] < one["forward_steps"]
     for r in (two, again):
