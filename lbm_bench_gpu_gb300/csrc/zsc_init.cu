@@ -44,6 +44,81 @@ __global__ void bubble_phi_kernel(Box b, const float *__restrict__ bubbles, int 
     }
 }
 
+// The same phi, per tile of 32 x 8 x 4 nodes of the ghosted grid: the block
+// first lists, in file order, the bubbles that can reach the tile (the
+// distance from the centre to the tile's box, in double, against
+// Rc + width + 0.01, which no rounding of the float test can exceed), then
+// makes the float test of bubble_phi_kernel for those only, so the node set
+// and the last covering bubble are the same.  A tile reached by more than
+// kTileBubbles bubbles tests them all.
+constexpr int BTX = 32, BTY = 8, BTZ = 4, kTileBubbles = 1024;
+
+__global__ void __launch_bounds__(BTX * BTY) bubble_phi_tiled_kernel(Box b, const float *__restrict__ bubbles,
+                                                                     int nbubbles, float phiStar, float width,
+                                                                     int kk0, float *__restrict__ phig)
+{
+    __shared__ int list[kTileBubbles];
+    __shared__ int warp_off[BTY];
+    __shared__ int count, overflow;
+    const int lane = threadIdx.x, warp = threadIdx.y;
+    const int x0 = blockIdx.x * BTX, y0 = blockIdx.y * BTY, k0 = blockIdx.z * BTZ;
+    const int k1 = min(k0 + BTZ, b.nz + 2) - 1;
+    if (lane == 0 && warp == 0) {
+        count = 0;
+        overflow = 0;
+    }
+    __syncthreads();
+    for (int base = 0; base < nbubbles; base += BTX * BTY) {
+        const int m = base + warp * BTX + lane;
+        bool hit = false;
+        if (m < nbubbles) {
+            const double xc = bubbles[4 * m + 0], yc = bubbles[4 * m + 1], zc = bubbles[4 * m + 2];
+            const double reach = (double)bubbles[4 * m + 3] + (double)width + 0.01;
+            const double dx = fmax(fmax((double)x0 - xc, xc - (double)(x0 + BTX - 1)), 0.0);
+            const double dy = fmax(fmax((double)y0 - yc, yc - (double)(y0 + BTY - 1)), 0.0);
+            const double dz = fmax(fmax((double)(k0 + kk0) - zc, zc - (double)(k1 + kk0)), 0.0);
+            hit = dx * dx + dy * dy + dz * dz <= reach * reach;
+        }
+        const unsigned ballot = __ballot_sync(0xffffffffu, hit);
+        if (lane == 0) warp_off[warp] = __popc(ballot);
+        __syncthreads();
+        if (lane == 0 && warp == 0) {   // exclusive prefix over the warps, in bubble order
+            int run = count;
+            for (int w = 0; w < BTY; w++) {
+                const int c = warp_off[w];
+                warp_off[w] = run;
+                run += c;
+            }
+            count = run;
+        }
+        __syncthreads();
+        if (hit) {
+            const int pos = warp_off[warp] + __popc(ballot & ((1u << lane) - 1u));
+            if (pos < kTileBubbles) list[pos] = m;
+            else overflow = 1;
+        }
+        __syncthreads();
+    }
+    const bool every = overflow != 0;
+    const int nlist = every ? nbubbles : min(count, kTileBubbles);
+    const int i = x0 + lane, j = y0 + warp;
+    for (int kk = k0; kk <= k1; kk++) {
+        float v = -phiStar;
+        for (int q = 0; q < nlist; q++) {
+            const int m = every ? q : list[q];
+            const float xc = __ldg(bubbles + 4 * m + 0), yc = __ldg(bubbles + 4 * m + 1);
+            const float zc = __ldg(bubbles + 4 * m + 2), rc = __ldg(bubbles + 4 * m + 3);
+            const float dx = __fsub_rn((float)i, xc);
+            const float dy = __fsub_rn((float)j, yc);
+            const float dz = __fsub_rn((float)(kk + kk0), zc);
+            const float s = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+            const float R = __fsqrt_rn(s);
+            if (R <= __fadd_rn(rc, width)) v = phiStar * tanhf(__fdiv_rn(2.f * __fsub_rn(rc, R), width));
+        }
+        phig[(size_t)kk * (size_t)b.nxy + (size_t)j * (size_t)b.nx + (size_t)i] = v;
+    }
+}
+
 // At-rest equilibrium from phi and rho.  z neighbours outside [0, nz) come
 // from ghost_lo / ghost_hi (nx*ny each) when given, else by periodic wrap.
 __global__ void equilibrium_kernel(Box b, float alpha4, float kappa, float phiStarSq, float Gamma,
@@ -100,8 +175,14 @@ unsigned grid_for(long long n)
 cudaError_t launch_bubble_phi(const Box &b, const float *bubbles_dev, int nbubbles, float phiStar, float width,
                               int z0, float *phi_ghosted, cudaStream_t s)
 {
-    bubble_phi_kernel<<<grid_for(b.nxy * (b.nz + 2)), 256, 0, s>>>(b, bubbles_dev, nbubbles, phiStar, width, z0,
-                                                                    phi_ghosted);
+    if (b.nx % BTX == 0 && b.ny % BTY == 0) {
+        const dim3 grid((unsigned)(b.nx / BTX), (unsigned)(b.ny / BTY), (unsigned)((b.nz + 2 + BTZ - 1) / BTZ));
+        bubble_phi_tiled_kernel<<<grid, dim3(BTX, BTY), 0, s>>>(b, bubbles_dev, nbubbles, phiStar, width, z0,
+                                                                 phi_ghosted);
+    } else {
+        bubble_phi_kernel<<<grid_for(b.nxy * (b.nz + 2)), 256, 0, s>>>(b, bubbles_dev, nbubbles, phiStar, width,
+                                                                        z0, phi_ghosted);
+    }
     return cudaGetLastError();
 }
 
