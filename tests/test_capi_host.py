@@ -283,3 +283,37 @@ def test_slab_init_rejects_bad_requests_without_touching_the_gpu(lib):
     p = params((64, 32, 48), "fp16")
     assert lib_.lbm_slab_init_bubbles(C.byref(h), C.byref(p), capi.fptr(BUB), 3, 0, 24, None) == capi.LBM_EINVAL
     assert not h.value
+
+
+def test_integration_per_rank_examples_compile(tmp_path):
+    """The per-rank z-slab examples of INTEGRATION.md (the halo exchange over
+    MPI, the step with its interior between pack and unpack, the statistics
+    reduced over the ranks, each rank's own slab) compile with -Wall -Werror
+    against the header, the CUDA runtime header and MPI's declarations."""
+    import re
+    import shutil
+    import subprocess
+    root = Path(__file__).resolve().parents[1]
+    cc = shutil.which("cc") or shutil.which("gcc")
+    cuda_inc = Path("/usr/local/cuda/include")
+    if cc is None or not (cuda_inc / "cuda_runtime_api.h").exists():
+        pytest.skip("no C compiler or CUDA headers")
+    blocks = re.findall(r"```c\n(.*?)```", (root / "INTEGRATION.md").read_text(), re.S)
+    rank_blocks = [b for b in blocks if "MPI_Sendrecv" in b or "lbm_slab_maxabs" in b]
+    assert len(rank_blocks) == 2
+    prelude = (
+        "#include <stdio.h>\n#include <cuda_runtime_api.h>\n#include \"lbm_gb300.h\"\n"
+        "typedef int MPI_Comm; typedef int MPI_Datatype; typedef int MPI_Op; typedef struct { int s; } MPI_Status;\n"
+        "#define MPI_BYTE 1\n#define MPI_FLOAT 2\n#define MPI_DOUBLE 3\n#define MPI_SUM 1\n#define MPI_MAX 2\n"
+        "#define MPI_STATUS_IGNORE ((MPI_Status *)0)\n"
+        "int MPI_Sendrecv(const void *, int, MPI_Datatype, int, int, void *, int, MPI_Datatype, int, int, MPI_Comm,"
+        " MPI_Status *);\n"
+        "int MPI_Reduce(const void *, void *, int, MPI_Datatype, MPI_Op, int, MPI_Comm);\n"
+        "int MPI_Allreduce(const void *, void *, int, MPI_Datatype, MPI_Op, MPI_Comm);\n"
+        "#define CHECK(x) do { int rc_ = (x); if (rc_) { fprintf(stderr, \"%s\\n\", lbm_strerror(rc_)); return 1; } }"
+        " while (0)\n")
+    src = tmp_path / "ranks.c"
+    src.write_text(prelude + "\n".join(rank_blocks))
+    r = subprocess.run([cc, "-std=c99", "-Wall", "-Werror", "-c", str(src), "-I", str(root / "include"),
+                        "-I", str(cuda_inc), "-o", str(tmp_path / "ranks.o")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
